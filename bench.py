@@ -1,0 +1,318 @@
+#!/usr/bin/env python
+"""Throughput of Kripke's source iteration on GB300 (and the CPU reference arm).
+
+Metric (src/kripke.cpp:495-503): unknowns / (seconds per source iteration),
+unknowns = zones * groups * directions.  A "step" is one source iteration
+(LTimes, scattering, source, LPlusTimes, full sweep of all octants,
+population) over the whole problem, with every field resident in HBM.
+
+Workload at N=1: the plain FP64 GPU drop-in problem -- 64^3 zones on the
+100 cm three-material cube, 64 groups, 128 Gauss-Legendre directions (16 per
+octant), Legendre order 4, seeded lower-triangular downscatter, DGZ host
+nesting, 1 group set, 8 direction sets.  psi and rhs are 17.2 GB each, far
+larger than L2, so no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--precision fp64|mixed]
+
+--gpus N > 1 (under torchrun) runs N independent replicas, one per GPU
+(the path has no data exchange); value = all replicas' unknowns / max time.
+--impl reference times the CPU restatement of the reference's OpenMP path
+(oracle/) on the host cores, on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(zones=(64, 64, 64), groups=64, quad=(8, 16), legendre=4, gset=1, dset=8, geometry=1, scatter=1,
+                layout="DGZ")
+WORKLOAD_NAME = "kripke 64^3 zones x 64 groups x 128 GL directions, P4, cube100, downscatter, DGZ, dset 8"
+# bounded CPU sample: same physics and per-zone work, 32^3 zones (1/8 of the unknowns)
+CPU_SAMPLE = dict(WORKLOAD, zones=(32, 32, 32))
+FP64_PEAK_GFLOPS = 1196.0  # measured DFMA rate on this machine's GB300 (profiles/fp64_peak_gb300.md)
+
+
+def unknowns(w):
+    z = w["zones"][0] * w["zones"][1] * w["zones"][2]
+    q = w["quad"]
+    d = q[0] * q[1] if isinstance(q, tuple) else q
+    return z * w["groups"] * d
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "_fallback": True}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic(w, prec_bytes):
+    """Per-iteration algorithmic flops and bytes per kernel family (inputs read once, outputs written once)."""
+    Z = w["zones"][0] * w["zones"][1] * w["zones"][2]
+    G = w["groups"]
+    q = w["quad"]
+    D = q[0] * q[1] if isinstance(q, tuple) else q
+    M = (w["legendre"] + 1) ** 2
+    U = Z * G * D
+    t = prec_bytes
+    lower = G * (G + 1) // 2 if w.get("scatter") == 1 else G
+    return {
+        "ltimes": {"flops": 2.0 * M * D * G * Z, "bytes": (D + M) * G * Z * t},
+        "lplustimes": {"flops": 2.0 * M * D * G * Z, "bytes": (D + M) * G * Z * t},
+        "scattering": {"flops": 2.0 * M * Z * lower, "bytes": 2.0 * M * G * Z * t},
+        # 13 flops + one divide (counted as 4) per unknown; rhs read, psi written, sigma_t per octant
+        "sweep": {"flops": 17.0 * U, "bytes": 2.0 * U * t + 8.0 * G * Z * t},
+        "population": {"flops": 2.0 * U, "bytes": 1.0 * U * t},
+        "source": {"flops": 0.0, "bytes": 0.0},
+    }
+
+
+def cpu_run(sample, threads, warmup, steps):
+    from oracle import pyoracle
+    p = pyoracle.Problem(threads=threads, **sample)
+    p.kconst("psi", 0.0)
+    for _ in range(warmup):
+        p.iterate()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        p.iterate()
+    dt = (time.perf_counter() - t0) / steps
+    return unknowns(sample) / dt, dt
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("KGB_BENCH_BACKEND") != "gloo" else "gloo")
+    return world, rank, local
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample_name = "32^3-zone sample of the workload (same groups, directions, order, physics), 1 iteration per step"
+    value, dt = cpu_run(CPU_SAMPLE, threads, args.warmup, args.steps)
+    line = {
+        "impl": "reference", "metric": "unknowns/s per source iteration", "value": value,
+        "unit": "unknowns/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded generator, no external data)",
+        "config": {"workload": WORKLOAD_NAME, "sample": sample_name},
+        "cpu_baseline": {"value": value, "unit": "unknowns/s", "cores": threads, "kind": "port",
+                         "sample": sample_name},
+        "e2e": {"value": value, "unit": "unknowns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local):
+    import ctypes
+    import numpy as np
+    import torch
+    from kripke_gb300 import abi
+
+    torch.cuda.set_device(local)
+    precision = abi.MIXED if args.precision == "mixed" else abi.FP64
+    w = dict(WORKLOAD)
+    ctx = abi.Context(local)
+    inp = ctx.generate(precision=precision, **w)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    U = unknowns(w)
+
+    # warm-up (the solve starts from psi = 0, like SteadyStateSolver)
+    ctx.fill("psi", 0.0)
+    for _ in range(args.warmup):
+        ctx.iterate(want_population=False)
+    ctx.sync()
+
+    # timed region: K source iterations, CUDA events on the stream the kernels run on
+    clocks = ClockSampler(local)
+    ctx.reset_timers()
+    ctx.set_timing(True)
+    launches0 = ctx.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.iterate(want_population=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = ctx.launch_count() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    fam = {f: ctx.kernel_time(f) for f in ("sweep", "ltimes", "lplustimes", "scattering", "source", "population")}
+    ctx.set_timing(False)
+    part = ctx.population()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # end to end through the public API with host buffers: upload every generated input from
+    # pinned host memory, run a 10-iteration solve (psi reset, populations read back each solve)
+    names = [n for n in ("ell", "ell_plus", "sigt_zonal", "data/sigs", "quadrature/xcos", "quadrature/ycos",
+                         "quadrature/zcos", "quadrature/w", "quadrature/id", "quadrature/jd", "quadrature/kd", "dx",
+                         "dy", "dz", "volume", "zone_to_num_mixelem", "zone_to_mixelem", "mixelem_to_zone",
+                         "mixelem_to_material", "mixelem_to_fraction", "moment_to_legendre")]
+    host = {}
+    for n in names:
+        a = ctx.download(n)
+        pinned = torch.empty(a.size, dtype=torch.int32 if a.dtype == np.int32 else torch.float64).pin_memory()
+        pinned.numpy()[:] = a
+        host[n] = pinned
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    niter = 10
+    e2e_times = []
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for n in names:
+            ctx.upload(n, host[n].numpy())
+        ctx.solve(niter)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value = U * niter / e2e_times[-1] * world
+
+    # roofline of the dominant kernel family
+    pk = peaks()
+    tbytes = 8 if precision == abi.FP64 else 4
+    alg = algorithmic(w, tbytes)
+    shares = {f: fam[f][0] for f in fam}
+    total = sum(shares.values()) or 1.0
+    dom = max(shares, key=shares.get)
+    dom_ms = fam[dom][0] / args.steps
+    flops, nbytes = alg[dom]["flops"], alg[dom]["bytes"]
+    if precision == abi.FP64:
+        achieved = flops / (dom_ms * 1e-3) / 1e9
+        roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
+                "frac": achieved / FP64_PEAK_GFLOPS, "traffic": None, "kernel": dom,
+                "peak_source": "measured FP64 FMA rate (MEASURED_PEAKS.json has no FP64 figure)",
+                "hbm": {"achieved": nbytes / (dom_ms * 1e-3) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                        "frac": nbytes / (dom_ms * 1e-3) / 1e9 / pk["hbm_gbs"]}}
+    else:
+        achieved = nbytes / (dom_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": None, "kernel": dom}
+    traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_file):
+        tr = json.load(open(traffic_file)).get("%s/%s" % (args.precision, dom))
+        if tr:
+            roof["traffic"] = tr
+
+    line = {
+        "metric": "unknowns/s per source iteration", "value": U * world / (ms * 1e-3), "unit": "unknowns/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if precision == abi.FP64 else "f32 (FP64 reductions)",
+        "data": "synthetic (seeded generator, no external data)",
+        "config": {"workload": WORKLOAD_NAME, "precision": args.precision, "unknowns": U,
+                   "l2": "inputs larger than L2 (psi, rhs 17.2 GB each); no flush",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "roofline": roof,
+        "kernel_ms_per_step": {f: fam[f][0] / args.steps for f in fam},
+        "kernel_share": {f: shares[f] / total for f in shares},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": "unknowns/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * niter,
+                "step": "upload all inputs from pinned host memory + %d-iteration solve + populations to host" % niter},
+        "population_after_timed_steps": part,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, dt = cpu_run(CPU_SAMPLE, threads, 1, 2)
+        line["cpu_baseline"] = {"value": v, "unit": "unknowns/s", "cores": threads, "kind": "port",
+                                "sample": "oracle (OpenMP restatement) on the 32^3-zone sample, 2 iterations"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,188 @@
+/*
+ * kgb.h -- C ABI of kripke_gb300, the GB300 (sm_103a) implementation of
+ * Kripke's source-iteration hot path.
+ *
+ * One context = one GPU, one CUDA stream, and the device-resident fields of
+ * one Kripke problem.  Fields are named exactly as in Kripke's DataStore and
+ * move across the ABI in Kripke's own host layout: the concatenation of the
+ * field's per-subdomain chunks, in chunk order, each chunk in the nesting
+ * (DGZ..ZGD) given to kgb_setup.  On the device every field lives in one
+ * GPU-chosen nesting (zone-major, direction fastest: "ZGD" over the whole
+ * problem) and is transposed on upload and download.
+ *
+ * Every entry point returns a kgb_status (KGB_OK = 0) and never throws or
+ * aborts; kgb_last_error() describes the most recent failure on a context.
+ * All work is queued on the context's stream; only the calls that hand a
+ * host value back (population, balance, solve, download, sync) wait for it.
+ *
+ * Reference interfaces replaced (paths relative to the Kripke source tree):
+ *   Kripke::Kernel::LTimes          src/Kripke/Kernel.h:22   -> kgb_ltimes
+ *   Kripke::Kernel::LPlusTimes      src/Kripke/Kernel.h:19   -> kgb_lplustimes
+ *   Kripke::Kernel::scattering      src/Kripke/Kernel.h:28   -> kgb_scattering
+ *   Kripke::Kernel::source          src/Kripke/Kernel.h:31   -> kgb_source
+ *   Kripke::Kernel::sweepSubdomain  src/Kripke/Kernel.h:34   -> kgb_sweep_subdomain
+ *   Kripke::Kernel::population      src/Kripke/Kernel.h:25   -> kgb_population
+ *   Kripke::Kernel::kConst          src/Kripke/Kernel.h:37-55 -> kgb_field_fill
+ *   Kripke::SweepSolver             src/Kripke/SweepSolver.h:20-22 -> kgb_sweep_solver
+ *   Kripke::SteadyStateSolver       src/Kripke/SteadyStateSolver.h:18 -> kgb_solve
+ *   Core::Field chunk storage       src/Kripke/Core/Field.h:53-104 -> kgb_field_upload/download
+ *   Kripke::generateProblem         src/Kripke/Generate.h:20-21 -> kgb_generate
+ *   Kripke::Core::Set sizes / PartitionSpace (one rank)
+ *                                   src/Kripke/Core/Set.h:23-202, Core/PartitionSpace.h:35-88 -> kgb_setup
+ */
+#ifndef KGB_H
+#define KGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum kgb_status {
+  KGB_OK = 0,
+  KGB_ERR_ARG = 1,      /* bad argument, size or name */
+  KGB_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+  KGB_ERR_OOM = 3,      /* device or host allocation failed */
+  KGB_ERR_TIMEOUT = 4,  /* a bounded device-side wait gave up */
+  KGB_ERR_LAYOUT = 5,   /* unknown nesting */
+  KGB_ERR_STATE = 6     /* call out of order (e.g. kernel before kgb_setup) */
+} kgb_status;
+
+/* Nestings, longest stride first (src/Kripke/ArchLayout.h:92-101). */
+typedef enum kgb_layout {
+  KGB_LAYOUT_DGZ = 0, KGB_LAYOUT_DZG = 1, KGB_LAYOUT_GDZ = 2,
+  KGB_LAYOUT_GZD = 3, KGB_LAYOUT_ZDG = 4, KGB_LAYOUT_ZGD = 5
+} kgb_layout;
+
+/* Precision forms. */
+typedef enum kgb_precision {
+  KGB_FP64 = 0,   /* plain form: every kernel in FP64 (the drop-in) */
+  KGB_MIXED = 1   /* FP32 state and sweep, FP32 GEMM-shaped kernels, FP64 reductions */
+} kgb_precision;
+
+typedef struct kgb_ctx kgb_ctx;
+
+/* Problem shape: InputVariables sizes and the on-rank decomposition
+ * (src/Kripke/InputVariables.h:18-49, Generate/Decomp.cpp:35-48). */
+typedef struct kgb_dims {
+  int32_t nx, ny, nz;            /* global zones */
+  int32_t num_groups;
+  int32_t num_directions;
+  int32_t legendre_order;
+  int32_t num_groupsets;         /* --gset */
+  int32_t num_dirsets;           /* --dset */
+  int32_t num_zonesets[3];       /* --zset */
+  int32_t layout;                /* kgb_layout of the host-side chunks */
+  int32_t precision;             /* kgb_precision */
+} kgb_dims;
+
+/* --- lifecycle --------------------------------------------------------- */
+int kgb_ctx_create(int device, kgb_ctx **out);
+int kgb_ctx_destroy(kgb_ctx *ctx);
+const char *kgb_last_error(const kgb_ctx *ctx);
+/* Library version string, e.g. "kripke_gb300 0.1 sm_103a". */
+const char *kgb_version(void);
+
+/* Allocates every device field for this shape (contents zero). */
+int kgb_setup(kgb_ctx *ctx, const kgb_dims *dims);
+/* Number of PQR subdomains (= gset * dset * zset_x * zset_y * zset_z). */
+int kgb_num_subdomains(const kgb_ctx *ctx, int32_t *out);
+
+/* --- problem generation (Kripke::generateProblem) ---------------------
+ * InputVariables (src/Kripke/InputVariables.h:18-49) plus the generator
+ * options of the benchmark problems.  kgb_generate calls kgb_setup with the
+ * matching dims and uploads every input field the hot path reads, generated
+ * as src/Kripke/Generate/{Quadrature,Space,Data,Energy}.cpp do. */
+typedef struct kgb_input {
+  int32_t nx, ny, nz;
+  int32_t num_directions;
+  int32_t num_groups;
+  int32_t legendre_order;
+  int32_t quad_num_polar;        /* 0: the reference's dummy S2 set (--quad N) */
+  int32_t quad_num_azimuthal;    /* >0 with quad_num_polar: Gauss-Legendre product set */
+  int32_t num_groupsets;
+  int32_t num_dirsets;
+  int32_t num_zonesets[3];
+  int32_t layout;
+  int32_t precision;
+  int32_t num_material_subsamples;
+  int32_t geometry;              /* 0: Kobayashi 3i (reference); 1: 100 cm cube, first duct leg only */
+  int32_t scatter;               /* 0: diagonal P0 (reference); 1: seeded lower-triangular downscatter */
+  int32_t perturb;               /* 1: seeded uniform +-20% per (material, group) on sigma_t, sigma_s */
+  int32_t pad_;
+  uint64_t seed;
+  double sigt[3];
+  double sigs[3];
+} kgb_input;
+/* The reference defaults (src/Kripke/InputVariables.cpp:17-47). */
+void kgb_default_input(kgb_input *in);
+int kgb_generate(kgb_ctx *ctx, const kgb_input *in);
+
+/* --- fields (Core::Field chunks, Kripke DataStore names) ---------------
+ * Names: psi rhs phi phi_out i_plane j_plane k_plane ell ell_plus sigt_zonal
+ * data/sigs quadrature/{xcos,ycos,zcos,w,id,jd,kd} dx dy dz volume
+ * zone_to_mixelem zone_to_num_mixelem mixelem_to_zone mixelem_to_material
+ * mixelem_to_fraction moment_to_legendre.
+ * Element type: int32 for the id/jd/kd, zone/mixelem/material and
+ * moment_to_legendre maps, double for everything else.  nbytes must equal
+ * the field's full size; kgb_field_bytes reports it (mixed-element fields are
+ * sized by the uploaded zone_to_num_mixelem, so upload that map first). */
+int kgb_field_bytes(kgb_ctx *ctx, const char *name, int64_t *nbytes);
+int kgb_field_upload(kgb_ctx *ctx, const char *name, const void *host, int64_t nbytes);
+int kgb_field_download(kgb_ctx *ctx, const char *name, void *host, int64_t nbytes);
+/* Kripke::Kernel::kConst over every chunk of a state field. */
+int kgb_field_fill(kgb_ctx *ctx, const char *name, double value);
+
+/* --- the hot path (Kripke::Kernel::*) ----------------------------------
+ * Same semantics as the reference: LTimes accumulates into phi, LPlusTimes
+ * into rhs, scattering into phi_out, source adds the isotropic source of
+ * material 0 to moment 0 of phi_out.  The caller zeroes targets with
+ * kgb_field_fill exactly as SteadyStateSolver does. */
+int kgb_ltimes(kgb_ctx *ctx);
+int kgb_lplustimes(kgb_ctx *ctx);
+int kgb_scattering(kgb_ctx *ctx);
+int kgb_source(kgb_ctx *ctx, double source_strength);
+/* Sweeps one subdomain: reads its incoming i/j/k planes and overwrites them
+ * with the outgoing ones, like Kernel::sweepSubdomain. */
+int kgb_sweep_subdomain(kgb_ctx *ctx, int32_t sdom_id);
+/* SweepSolver over all subdomains: zeroes the planes, clears vacuum
+ * boundaries, sweeps every subdomain in upwind order (all octants at once)
+ * and hands planes to downwind zone sets. */
+int kgb_sweep_solver(kgb_ctx *ctx);
+/* Kernel::population: sum over d,g,z of w(d) psi(d,g,z) volume(z), in FP64. */
+int kgb_population(kgb_ctx *ctx, double *out);
+/* FP64 particle balance after a sweep: out[0] emission (sum w rhs vol),
+ * out[1] collision (sum w sigt psi vol), out[2] leakage through the domain
+ * boundary, out[3] population, out[4] = out[0]-out[1]-out[2]. */
+int kgb_balance(kgb_ctx *ctx, double out[5]);
+
+/* SteadyStateSolver: niter source iterations from psi = 0.  part[i] gets the
+ * particle count after iteration i (may be NULL).  source_strength is the
+ * reference's 1.0 unless a caller scales the source. */
+int kgb_solve(kgb_ctx *ctx, int32_t niter, double source_strength, double *part);
+/* One source iteration on the current psi (no psi reset).  The particle
+ * count is always computed on the device; it is copied to *part (and the
+ * call waits) only when part is not NULL. */
+int kgb_iterate(kgb_ctx *ctx, double source_strength, double *part);
+/* Blocks until the context's stream is idle. */
+int kgb_sync(kgb_ctx *ctx);
+/* Run on a caller-owned CUDA stream (a cudaStream_t passed as a pointer)
+ * instead of the context's own; NULL restores the context's stream. */
+int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
+/* Tuning knobs: "sweep_tile_z" (tile depth in k, default 4). */
+int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
+/* Device time in milliseconds of the named kernel family accumulated since the
+ * last reset ("sweep", "ltimes", "lplustimes", "scattering", "population");
+ * timing is off unless kgb_set_timing(ctx, 1). */
+int kgb_set_timing(kgb_ctx *ctx, int on);
+int kgb_kernel_time(kgb_ctx *ctx, const char *family, double *ms, int64_t *launches);
+int kgb_reset_timers(kgb_ctx *ctx);
+/* Number of kernels this context has launched since it was created. */
+int kgb_launch_count(kgb_ctx *ctx, int64_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1333 @@
+// kgb_api.cu -- the C ABI of kripke_gb300 (include/kgb.h).
+//
+// Owns one GPU context: the device fields of one Kripke problem in the
+// device nesting (kgb_internal.h), the host copies of the small inputs, the
+// sweep schedule, and the source-iteration loop.  Kernels live in sweep.cu,
+// moments.cu, scatter.cu, reduce.cu and xpose.cu.
+//
+// Host-side conventions mirrored from the reference (paths relative to the
+// Kripke source tree):
+//   nesting strides ......... VarTypes.h:67-101 + Core/VarLayout.h:118-170 (the
+//                             field's index types sorted by their position in
+//                             the nesting's order list; ties keep argument order)
+//   subdomain numbering ..... Core/PartitionSpace.cpp:82-92,246-273 (row-major
+//                             over P, Q, Rx, Ry, Rz; spaces project coordinates out)
+//   chunk of a field ........ Core/DomainVar.cpp:15-39 (one chunk per subdomain
+//                             of the field's space, in space-index order)
+//   zone numbering .......... Generate/Space.cpp:92-93 (zone = (k*nj + j)*ni + i)
+//   sweep scheduling ........ SweepSolver.cpp:23-87, ParallelComm.cpp:61-185
+//   iteration ............... SteadyStateSolver.cpp:39-108
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "kgb_internal.h"
+#include "kgb_layout.h"
+
+using namespace kgb;
+
+namespace {
+
+enum Kind { K_FLUX, K_MOM, K_PLANE, K_SIGT, K_ELL, K_ELLP, K_SIGS, K_QD, K_QI, K_DXYZ, K_VOL, K_ZI, K_MI, K_MD, K_M2L };
+
+struct FieldInfo {
+  const char *name;
+  Kind kind;
+  int which;
+};
+
+const FieldInfo kFields[] = {
+    {"psi", K_FLUX, 0}, {"rhs", K_FLUX, 1}, {"phi", K_MOM, 0}, {"phi_out", K_MOM, 1},
+    {"i_plane", K_PLANE, 0}, {"j_plane", K_PLANE, 1}, {"k_plane", K_PLANE, 2},
+    {"sigt_zonal", K_SIGT, 0}, {"ell", K_ELL, 0}, {"ell_plus", K_ELLP, 0}, {"data/sigs", K_SIGS, 0},
+    {"quadrature/xcos", K_QD, 0}, {"quadrature/ycos", K_QD, 1}, {"quadrature/zcos", K_QD, 2},
+    {"quadrature/w", K_QD, 3}, {"quadrature/id", K_QI, 0}, {"quadrature/jd", K_QI, 1},
+    {"quadrature/kd", K_QI, 2}, {"dx", K_DXYZ, 0}, {"dy", K_DXYZ, 1}, {"dz", K_DXYZ, 2},
+    {"volume", K_VOL, 0}, {"zone_to_mixelem", K_ZI, 0}, {"zone_to_num_mixelem", K_ZI, 1},
+    {"mixelem_to_zone", K_MI, 0}, {"mixelem_to_material", K_MI, 1}, {"mixelem_to_fraction", K_MD, 0},
+    {"moment_to_legendre", K_M2L, 0},
+};
+
+const FieldInfo *findField(const char *name) {
+  if (!name) return nullptr;
+  for (const auto &f : kFields)
+    if (!std::strcmp(f.name, name)) return &f;
+  return nullptr;
+}
+
+// One chunk of a field in Kripke's host layout.
+struct ChunkGeom {
+  int nd;
+  Idx types[4];
+  int64_t dims[4];
+  Space space;
+};
+
+struct TimerFam {
+  double ms = 0.0;
+  int64_t launches = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+};
+
+}  // namespace
+
+struct kgb_ctx {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool ready = false;
+  kgb_dims dims{};
+  Decomp dc;
+  int G = 0, D = 0, M = 0, L = 0, Gs = 0, Ds = 0;
+  int nx = 0, ny = 0, nz = 0, nxs = 0, nys = 0, nzs = 0;
+  int64_t Z = 0, Zs = 0;
+  int prec = KGB_FP64;
+  size_t tsz = 8;
+  int tz = 4;
+
+  // device state (element type T = double or float by precision)
+  void *psi = nullptr, *rhs = nullptr, *phi = nullptr, *phi_out = nullptr, *sigt = nullptr;
+  void *plane[3] = {nullptr, nullptr, nullptr};
+  int64_t plane_chunk[3] = {0, 0, 0};
+  void *ell = nullptr, *ellp = nullptr, *sigsT = nullptr, *cx = nullptr, *cy = nullptr, *cz = nullptr;
+  double *w_d = nullptr, *cos_d[3] = {nullptr, nullptr, nullptr}, *vol_d = nullptr, *dxyz_d[3] = {nullptr, nullptr, nullptr};
+  int *zmix_start = nullptr, *zmix_count = nullptr, *mix_mat = nullptr, *mix_zone = nullptr;
+  double *mix_frac = nullptr;
+  int64_t nmix = 0, nmix_cap = 0;
+  int *gp_lo = nullptr, *gp_hi = nullptr;
+  SdomDesc *sdoms_d = nullptr;
+  int *ident_d = nullptr, *levels_d = nullptr;
+  int4 *tiles_d = nullptr;
+  double *partials = nullptr;
+  int npart = 0;
+  double *results = nullptr;   // small device result slots
+  double *parts_dev = nullptr; // per-iteration population
+  int parts_cap = 0;
+  double *staging = nullptr;
+  size_t staging_bytes = 0;
+
+  // host copies of the small inputs (global indexing)
+  std::vector<double> q[4];          // xcos, ycos, zcos, w  [D]
+  std::vector<int> qi[3];            // id, jd, kd           [D]
+  std::vector<double> dxyz[3];       // dx [nx], dy [ny], dz [nz]
+  std::vector<double> ell_h, ellp_h; // [D][M]
+  std::vector<double> sigs_h;        // [3][L+1][G][G]
+  std::vector<double> vol_h;         // [Z]
+  std::vector<std::vector<int>> zmap[2];  // per R chunk: zone_to_mixelem, zone_to_num_mixelem
+  std::vector<std::vector<int>> mimap[2]; // per R chunk: mixelem_to_zone, mixelem_to_material
+  std::vector<std::vector<double>> mfrac; // per R chunk
+  std::vector<int> m2l;
+  bool have[32] = {};
+  bool dirty_quad = true, dirty_geom = true, dirty_ell = true, dirty_sigs = true, dirty_mix = true, dirty_vol = true;
+
+  // sweep schedule
+  std::vector<SdomDesc> sdoms_h;
+  std::vector<int> tile_off;  // step -> first tile, size nsteps+1
+  int nsteps = 0;
+  std::vector<int> level_off;  // wave level -> offset into levels_d
+  std::vector<int> level_sdoms;
+
+  bool timing = false;
+  std::map<std::string, TimerFam> fams;
+  int64_t launches = 0;  // kernels launched by this context
+};
+
+namespace {
+
+int fail(kgb_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) return fail(ctx, KGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define CKL() CK(cudaGetLastError())
+// record `n` kernel launches, then check the launch status
+#define CKN(n)              \
+  do {                      \
+    ctx->launches += (n);   \
+    CKL();                  \
+  } while (0)
+
+int fieldIndex(const FieldInfo *f) { return (int)(f - kFields); }
+
+// Host-layout geometry of chunk `ch` of a field.
+ChunkGeom chunkGeom(const kgb_ctx *c, const FieldInfo *f, int ch) {
+  ChunkGeom g{};
+  switch (f->kind) {
+    case K_FLUX: g = {3, {I_DIR, I_GRP, I_ZONE}, {c->Ds, c->Gs, c->Zs}, S_PQR}; break;
+    case K_MOM: g = {3, {I_MOM, I_GRP, I_ZONE}, {c->M, c->Gs, c->Zs}, S_PR}; break;
+    case K_PLANE:
+      if (f->which == 0) g = {4, {I_DIR, I_GRP, I_ZJ, I_ZK}, {c->Ds, c->Gs, c->nys, c->nzs}, S_PQR};
+      else if (f->which == 1) g = {4, {I_DIR, I_GRP, I_ZI, I_ZK}, {c->Ds, c->Gs, c->nxs, c->nzs}, S_PQR};
+      else g = {4, {I_DIR, I_GRP, I_ZI, I_ZJ}, {c->Ds, c->Gs, c->nxs, c->nys}, S_PQR};
+      break;
+    case K_SIGT: g = {2, {I_GRP, I_ZONE}, {c->Gs, c->Zs}, S_PR}; break;
+    case K_ELL: g = {2, {I_MOM, I_DIR}, {c->M, c->Ds}, S_Q}; break;
+    case K_ELLP: g = {2, {I_DIR, I_MOM}, {c->Ds, c->M}, S_Q}; break;
+    case K_SIGS: g = {4, {I_MAT, I_LEG, I_GGRP, I_GGRP}, {3, c->L + 1, c->G, c->G}, S_NULL}; break;
+    case K_QD:
+    case K_QI: g = {1, {I_DIR}, {c->Ds}, S_Q}; break;
+    case K_DXYZ:
+      if (f->which == 0) g = {1, {I_ZI}, {c->nxs}, S_RX};
+      else if (f->which == 1) g = {1, {I_ZJ}, {c->nys}, S_RY};
+      else g = {1, {I_ZK}, {c->nzs}, S_RZ};
+      break;
+    case K_VOL:
+    case K_ZI: g = {1, {I_ZONE}, {c->Zs}, S_R}; break;
+    case K_MI:
+    case K_MD: {
+      int64_t n = 0;
+      if (ch < (int)c->zmap[1].size())
+        for (int v : c->zmap[1][ch]) n += v;
+      g = {1, {I_MIX}, {n}, S_R};
+      break;
+    }
+    case K_M2L: g = {1, {I_MOM}, {c->M}, S_NULL}; break;
+  }
+  return g;
+}
+
+bool isIntKind(Kind k) { return k == K_QI || k == K_ZI || k == K_MI || k == K_M2L; }
+
+int64_t chunkElems(const ChunkGeom &g) {
+  int64_t n = 1;
+  for (int k = 0; k < g.nd; ++k) n *= g.dims[k];
+  return n;
+}
+
+int numChunks(const kgb_ctx *c, const FieldInfo *f) { return c->dc.chunks(chunkGeom(c, f, 0).space); }
+
+int64_t fieldBytes(const kgb_ctx *c, const FieldInfo *f) {
+  int64_t n = 0;
+  const int nch = numChunks(c, f);
+  for (int ch = 0; ch < nch; ++ch) n += chunkElems(chunkGeom(c, f, ch));
+  return n * (isIntKind(f->kind) ? 4 : 8);
+}
+
+template <typename T>
+T *as(void *p) {
+  return reinterpret_cast<T *>(p);
+}
+
+int ensureStaging(kgb_ctx *ctx, size_t bytes) {
+  if (bytes <= ctx->staging_bytes) return KGB_OK;
+  if (ctx->staging) cudaFree(ctx->staging);
+  ctx->staging = nullptr;
+  ctx->staging_bytes = 0;
+  cudaError_t e = cudaMalloc(&ctx->staging, bytes);
+  if (e != cudaSuccess) return fail(ctx, KGB_ERR_OOM, "staging allocation failed");
+  ctx->staging_bytes = bytes;
+  return KGB_OK;
+}
+
+// Device descriptor of one chunk of a device-transposed field.
+XposeDesc chunkXpose(const kgb_ctx *c, const FieldInfo *f, int ch) {
+  ChunkGeom g = chunkGeom(c, f, ch);
+  XposeDesc x{};
+  x.nd = g.nd;
+  for (int k = 0; k < g.nd; ++k) x.n[k] = g.dims[k];
+  nestStrides(c->dims.layout, g.nd, g.types, g.dims, x.hs);
+  int co[5];
+  c->dc.chunkCoord(g.space, ch, co);
+  const int glo = co[0] * c->Gs, dlo = co[1] * c->Ds;
+  x.nxs = c->nxs;
+  x.nys = c->nys;
+  x.io = co[2] * c->nxs;
+  x.jo = co[3] * c->nys;
+  x.ko = co[4] * c->nzs;
+  x.nx = c->nx;
+  x.ny = c->ny;
+  x.zdim = -1;
+  switch (f->kind) {
+    case K_FLUX:  // (d, g, z) -> ((zg*G + glo+g)*D + dlo+d)
+      x.os[0] = 1; x.os[1] = c->D; x.os[2] = (int64_t)c->G * c->D; x.zdim = 2;
+      x.obase = (int64_t)glo * c->D + dlo;
+      x.iter[0] = 2; x.iter[1] = 1; x.iter[2] = 0;
+      break;
+    case K_MOM:  // (m, g, z) -> ((zg*G + glo+g)*M + m)
+      x.os[0] = 1; x.os[1] = c->M; x.os[2] = (int64_t)c->G * c->M; x.zdim = 2;
+      x.obase = (int64_t)glo * c->M;
+      x.iter[0] = 2; x.iter[1] = 1; x.iter[2] = 0;
+      break;
+    case K_SIGT:  // (g, z) -> zg*G + glo+g
+      x.os[0] = 1; x.os[1] = c->G; x.zdim = 1;
+      x.obase = glo;
+      x.iter[0] = 1; x.iter[1] = 0;
+      break;
+    case K_PLANE: {  // (d, g, a, b) -> ((b*na + a)*Gs + g)*Ds + d within the subdomain's chunk
+      const int64_t na = g.dims[2];
+      x.os[0] = 1; x.os[1] = c->Ds; x.os[2] = (int64_t)c->Gs * c->Ds; x.os[3] = na * c->Gs * c->Ds;
+      x.obase = (int64_t)ch * c->plane_chunk[f->which];
+      x.iter[0] = 3; x.iter[1] = 2; x.iter[2] = 1; x.iter[3] = 0;
+      break;
+    }
+    default: break;
+  }
+  return x;
+}
+
+bool deviceKind(Kind k) { return k == K_FLUX || k == K_MOM || k == K_PLANE || k == K_SIGT; }
+
+void *deviceArray(kgb_ctx *c, const FieldInfo *f) {
+  switch (f->kind) {
+    case K_FLUX: return f->which == 0 ? c->psi : c->rhs;
+    case K_MOM: return f->which == 0 ? c->phi : c->phi_out;
+    case K_PLANE: return c->plane[f->which];
+    case K_SIGT: return c->sigt;
+    default: return nullptr;
+  }
+}
+
+int64_t deviceElems(const kgb_ctx *c, const FieldInfo *f) {
+  switch (f->kind) {
+    case K_FLUX: return c->Z * c->G * c->D;
+    case K_MOM: return c->Z * c->G * c->M;
+    case K_PLANE: return c->plane_chunk[f->which] * c->dc.num();
+    case K_SIGT: return c->Z * c->G;
+    default: return 0;
+  }
+}
+
+template <typename T>
+int dmalloc(kgb_ctx *ctx, T **p, size_t n) {
+  cudaError_t e = cudaMalloc((void **)p, std::max<size_t>(n, 1) * sizeof(T));
+  if (e != cudaSuccess) return fail(ctx, KGB_ERR_OOM, "device allocation failed");
+  return KGB_OK;
+}
+
+int dalloc(kgb_ctx *ctx, void **p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 1));
+  if (e != cudaSuccess) return fail(ctx, KGB_ERR_OOM, "device allocation failed (" + std::to_string(bytes) + " bytes)");
+  e = cudaMemsetAsync(*p, 0, std::max<size_t>(bytes, 1), ctx->stream);
+  if (e != cudaSuccess) return fail(ctx, KGB_ERR_CUDA, "memset failed");
+  return KGB_OK;
+}
+
+void freeAll(kgb_ctx *c) {
+  void *ptrs[] = {c->psi, c->rhs, c->phi, c->phi_out, c->sigt, c->plane[0], c->plane[1], c->plane[2], c->ell, c->ellp,
+                  c->sigsT, c->cx, c->cy, c->cz, c->w_d, c->cos_d[0], c->cos_d[1], c->cos_d[2], c->vol_d,
+                  c->dxyz_d[0], c->dxyz_d[1], c->dxyz_d[2], c->zmix_start, c->zmix_count, c->mix_mat, c->mix_zone,
+                  c->mix_frac, c->gp_lo, c->gp_hi, c->sdoms_d, c->ident_d, c->levels_d, c->tiles_d, c->partials,
+                  c->results, c->parts_dev, c->staging};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  c->psi = c->rhs = c->phi = c->phi_out = c->sigt = nullptr;
+  c->plane[0] = c->plane[1] = c->plane[2] = nullptr;
+  c->ell = c->ellp = c->sigsT = c->cx = c->cy = c->cz = nullptr;
+  c->w_d = c->vol_d = nullptr;
+  for (int k = 0; k < 3; ++k) c->cos_d[k] = c->dxyz_d[k] = nullptr;
+  c->zmix_start = c->zmix_count = c->mix_mat = c->mix_zone = nullptr;
+  c->mix_frac = nullptr;
+  c->gp_lo = c->gp_hi = nullptr;
+  c->sdoms_d = nullptr;
+  c->ident_d = c->levels_d = nullptr;
+  c->tiles_d = nullptr;
+  c->partials = c->results = c->parts_dev = c->staging = nullptr;
+  c->staging_bytes = 0;
+  c->nmix_cap = 0;
+  c->parts_cap = 0;
+  c->ready = false;
+}
+
+// ---------------------------------------------------------------------------
+// Timers (CUDA events on the context's stream)
+// ---------------------------------------------------------------------------
+struct FamScope {
+  kgb_ctx *c;
+  TimerFam *fam = nullptr;
+  cudaEvent_t b = nullptr;
+  FamScope(kgb_ctx *ctx, const char *name) : c(ctx) {
+    if (!c->timing) return;
+    fam = &c->fams[name];
+    cudaEventCreate(&b);
+    cudaEventRecord(b, c->stream);
+  }
+  ~FamScope() {
+    if (!fam) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, c->stream);
+    fam->pending.push_back({b, e});
+    fam->launches++;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Derived device tables (built lazily when inputs change)
+// ---------------------------------------------------------------------------
+template <typename T>
+int uploadVec(kgb_ctx *ctx, void *dst, const std::vector<double> &src) {
+  std::vector<T> tmp(src.begin(), src.end());
+  CK(cudaMemcpyAsync(dst, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));  // tmp goes out of scope
+  return KGB_OK;
+}
+
+int need(kgb_ctx *ctx, std::initializer_list<const char *> names) {
+  for (const char *n : names) {
+    const FieldInfo *f = findField(n);
+    if (!ctx->have[fieldIndex(f)]) return fail(ctx, KGB_ERR_STATE, std::string("input field '") + n + "' has not been uploaded");
+  }
+  return KGB_OK;
+}
+
+template <typename T>
+int prepareT(kgb_ctx *ctx) {
+  int rc;
+  if (ctx->dirty_quad) {
+    if ((rc = need(ctx, {"quadrature/xcos", "quadrature/ycos", "quadrature/zcos", "quadrature/w", "quadrature/id",
+                         "quadrature/jd", "quadrature/kd"})))
+      return rc;
+    CK(cudaMemcpyAsync(ctx->w_d, ctx->q[3].data(), ctx->D * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    for (int k = 0; k < 3; ++k)
+      CK(cudaMemcpyAsync(ctx->cos_d[k], ctx->q[k].data(), ctx->D * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    // sweep descriptors: every direction of a subdomain follows its first direction's traversal
+    ctx->sdoms_h.resize(ctx->dc.num());
+    for (int s = 0; s < ctx->dc.num(); ++s) {
+      int co[5];
+      ctx->dc.coord(s, co);
+      SdomDesc &d = ctx->sdoms_h[s];
+      d.p = co[0]; d.q = co[1]; d.xs = co[2]; d.ys = co[3]; d.zs = co[4];
+      d.glo = co[0] * ctx->Gs;
+      d.dlo = co[1] * ctx->Ds;
+      d.io = co[2] * ctx->nxs; d.jo = co[3] * ctx->nys; d.ko = co[4] * ctx->nzs;
+      d.id = ctx->qi[0][d.dlo]; d.jd = ctx->qi[1][d.dlo]; d.kd = ctx->qi[2][d.dlo];
+      d.ip = (int64_t)s * ctx->plane_chunk[0];
+      d.jp = (int64_t)s * ctx->plane_chunk[1];
+      d.kp = (int64_t)s * ctx->plane_chunk[2];
+    }
+    CK(cudaMemcpyAsync(ctx->sdoms_d, ctx->sdoms_h.data(), ctx->sdoms_h.size() * sizeof(SdomDesc), cudaMemcpyHostToDevice, ctx->stream));
+    // zone-set waves in upwind order (level = oriented zone-set coordinate sum)
+    const int S[3] = {ctx->dc.Sx, ctx->dc.Sy, ctx->dc.Sz};
+    int nlev = S[0] + S[1] + S[2] - 2;
+    std::vector<std::vector<int>> lv(nlev);
+    for (int s = 0; s < ctx->dc.num(); ++s) {
+      const SdomDesc &d = ctx->sdoms_h[s];
+      int ox = d.id > 0 ? d.xs : S[0] - 1 - d.xs;
+      int oy = d.jd > 0 ? d.ys : S[1] - 1 - d.ys;
+      int oz = d.kd > 0 ? d.zs : S[2] - 1 - d.zs;
+      lv[ox + oy + oz].push_back(s);
+    }
+    ctx->level_off.assign(1, 0);
+    ctx->level_sdoms.clear();
+    for (auto &v : lv) {
+      for (int s : v) ctx->level_sdoms.push_back(s);
+      ctx->level_off.push_back((int)ctx->level_sdoms.size());
+    }
+    CK(cudaMemcpyAsync(ctx->levels_d, ctx->level_sdoms.data(), ctx->level_sdoms.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->dirty_quad = false;
+    ctx->dirty_geom = true;
+  }
+  if (ctx->dirty_geom) {
+    if ((rc = need(ctx, {"dx", "dy", "dz"}))) return rc;
+    const int n[3] = {ctx->nx, ctx->ny, ctx->nz};
+    void *dst[3] = {ctx->cx, ctx->cy, ctx->cz};
+    for (int k = 0; k < 3; ++k) {
+      // 2*cos/delta exactly as the reference forms it per cell (SweepSubdomain.cpp:174-176)
+      std::vector<double> t((size_t)ctx->D * n[k]);
+      for (int d = 0; d < ctx->D; ++d)
+        for (int i = 0; i < n[k]; ++i) t[(size_t)d * n[k] + i] = 2.0 * ctx->q[k][d] / ctx->dxyz[k][i];
+      if ((rc = uploadVec<T>(ctx, dst[k], t))) return rc;
+      CK(cudaMemcpyAsync(ctx->dxyz_d[k], ctx->dxyz[k].data(), n[k] * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->dirty_geom = false;
+  }
+  if (ctx->dirty_ell) {
+    if ((rc = need(ctx, {"ell", "ell_plus"}))) return rc;
+    if ((rc = uploadVec<T>(ctx, ctx->ell, ctx->ell_h))) return rc;
+    if ((rc = uploadVec<T>(ctx, ctx->ellp, ctx->ellp_h))) return rc;
+    ctx->dirty_ell = false;
+  }
+  if (ctx->dirty_sigs) {
+    if ((rc = need(ctx, {"data/sigs"}))) return rc;
+    const int G = ctx->G, L1 = ctx->L + 1;
+    std::vector<double> t((size_t)3 * L1 * G * G);
+    std::vector<int> lo(G, G), hi(G, -1);
+    for (int m = 0; m < 3; ++m)
+      for (int l = 0; l < L1; ++l)
+        for (int g = 0; g < G; ++g)
+          for (int gp = 0; gp < G; ++gp) {
+            double v = ctx->sigs_h[(((size_t)m * L1 + l) * G + g) * G + gp];
+            t[(((size_t)m * L1 + l) * G + gp) * G + g] = v;
+            if (v != 0.0) {
+              lo[g] = std::min(lo[g], gp);
+              hi[g] = std::max(hi[g], gp);
+            }
+          }
+    if ((rc = uploadVec<T>(ctx, ctx->sigsT, t))) return rc;
+    CK(cudaMemcpyAsync(ctx->gp_lo, lo.data(), G * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->gp_hi, hi.data(), G * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->dirty_sigs = false;
+  }
+  if (ctx->dirty_vol) {
+    if ((rc = need(ctx, {"volume"}))) return rc;
+    CK(cudaMemcpyAsync(ctx->vol_d, ctx->vol_h.data(), ctx->Z * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->dirty_vol = false;
+  }
+  if (ctx->dirty_mix) {
+    if ((rc = need(ctx, {"zone_to_mixelem", "zone_to_num_mixelem", "mixelem_to_zone", "mixelem_to_material",
+                         "mixelem_to_fraction"})))
+      return rc;
+    const int nr = ctx->dc.chunks(S_R);
+    int64_t total = 0;
+    for (int r = 0; r < nr; ++r) total += (int64_t)ctx->mfrac[r].size();
+    if (total > ctx->nmix_cap) {
+      for (void *p : {(void *)ctx->mix_mat, (void *)ctx->mix_zone, (void *)ctx->mix_frac})
+        if (p) cudaFree(p);
+      ctx->mix_mat = ctx->mix_zone = nullptr;
+      ctx->mix_frac = nullptr;
+      if ((rc = dmalloc(ctx, &ctx->mix_mat, total)) || (rc = dmalloc(ctx, &ctx->mix_zone, total)) ||
+          (rc = dmalloc(ctx, &ctx->mix_frac, total)))
+        return rc;
+      ctx->nmix_cap = total;
+    }
+    std::vector<int> zstart(ctx->Z, 0), zcount(ctx->Z, 0), mmat(total), mzone(total);
+    std::vector<double> mfr(total);
+    int64_t off = 0;
+    for (int r = 0; r < nr; ++r) {
+      int co[5];
+      ctx->dc.chunkCoord(S_R, r, co);
+      const int io = co[2] * ctx->nxs, jo = co[3] * ctx->nys, ko = co[4] * ctx->nzs;
+      auto glob = [&](int64_t zl) {
+        int64_t i = zl % ctx->nxs, j = (zl / ctx->nxs) % ctx->nys, k = zl / ((int64_t)ctx->nxs * ctx->nys);
+        return ((k + ko) * ctx->ny + (j + jo)) * ctx->nx + (i + io);
+      };
+      const int64_t nm = (int64_t)ctx->mfrac[r].size();
+      for (int64_t zl = 0; zl < ctx->Zs; ++zl) {
+        const int64_t zg = glob(zl);
+        const int st = ctx->zmap[0][r][zl], cn = ctx->zmap[1][r][zl];
+        if (st < 0 || cn < 0 || st + cn > nm) return fail(ctx, KGB_ERR_ARG, "zone_to_mixelem out of range");
+        zstart[zg] = (int)(off + st);
+        zcount[zg] = cn;
+      }
+      for (int64_t m = 0; m < nm; ++m) {
+        const int zl = ctx->mimap[0][r][m], mat = ctx->mimap[1][r][m];
+        if (zl < 0 || zl >= ctx->Zs || mat < 0 || mat > 2) return fail(ctx, KGB_ERR_ARG, "mixelem map out of range");
+        mzone[off + m] = (int)glob(zl);
+        mmat[off + m] = mat;
+        mfr[off + m] = ctx->mfrac[r][m];
+      }
+      off += nm;
+    }
+    ctx->nmix = total;
+    CK(cudaMemcpyAsync(ctx->zmix_start, zstart.data(), ctx->Z * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->zmix_count, zcount.data(), ctx->Z * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->mix_mat, mmat.data(), total * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->mix_zone, mzone.data(), total * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->mix_frac, mfr.data(), total * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->dirty_mix = false;
+  }
+  return KGB_OK;
+}
+
+int prepare(kgb_ctx *ctx) {
+  if (!ctx) return KGB_ERR_ARG;
+  if (!ctx->ready) return fail(ctx, KGB_ERR_STATE, "kgb_setup has not been called");
+  CK(cudaSetDevice(ctx->device));
+  return ctx->prec == KGB_FP64 ? prepareT<double>(ctx) : prepareT<float>(ctx);
+}
+
+int buildTiles(kgb_ctx *ctx) {
+  const int ntx = (ctx->nxs + kTileX - 1) / kTileX;
+  const int nty = (ctx->nys + kTileY - 1) / kTileY;
+  const int ntz = (ctx->nzs + ctx->tz - 1) / ctx->tz;
+  ctx->nsteps = ntx + nty + ntz - 2;
+  std::vector<int4> tiles;
+  ctx->tile_off.assign(1, 0);
+  for (int s = 0; s < ctx->nsteps; ++s) {
+    for (int c = 0; c < ntz; ++c)
+      for (int b = 0; b < nty; ++b) {
+        int a = s - b - c;
+        if (a >= 0 && a < ntx) tiles.push_back(make_int4(a, b, c, 0));
+      }
+    ctx->tile_off.push_back((int)tiles.size());
+  }
+  if (ctx->tiles_d) cudaFree(ctx->tiles_d);
+  ctx->tiles_d = nullptr;
+  int rc = dmalloc(ctx, &ctx->tiles_d, tiles.size());
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(ctx->tiles_d, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return KGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel drivers
+// ---------------------------------------------------------------------------
+template <typename T>
+int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave) {
+  SweepArgs<T> a{};
+  a.rhs = as<T>(ctx->rhs);
+  a.psi = as<T>(ctx->psi);
+  a.sigt = as<T>(ctx->sigt);
+  a.iplane = as<T>(ctx->plane[0]);
+  a.jplane = as<T>(ctx->plane[1]);
+  a.kplane = as<T>(ctx->plane[2]);
+  a.cx = as<T>(ctx->cx);
+  a.cy = as<T>(ctx->cy);
+  a.cz = as<T>(ctx->cz);
+  a.sdoms = ctx->sdoms_d;
+  a.wave = wave_dev;
+  a.tiles = ctx->tiles_d;
+  a.nx = ctx->nx; a.ny = ctx->ny; a.nz = ctx->nz;
+  a.G = ctx->G; a.D = ctx->D; a.Gs = ctx->Gs; a.Ds = ctx->Ds;
+  a.nxs = ctx->nxs; a.nys = ctx->nys; a.nzs = ctx->nzs;
+  a.tz = ctx->tz;
+  FamScope fs(ctx, "sweep");
+  for (int s = 0; s < ctx->nsteps; ++s) {
+    a.tile_off = ctx->tile_off[s];
+    const int nt = ctx->tile_off[s + 1] - ctx->tile_off[s];
+    if (nt == 0) continue;
+    launch_sweep_step<T>(a, nt, nwave, ctx->stream);
+    CKN(1);
+  }
+  return KGB_OK;
+}
+
+int sweepWaveAny(kgb_ctx *ctx, const int *wave_dev, int nwave) {
+  return ctx->prec == KGB_FP64 ? sweepWave<double>(ctx, wave_dev, nwave) : sweepWave<float>(ctx, wave_dev, nwave);
+}
+
+int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
+  void *p = deviceArray(ctx, f);
+  const int64_t n = deviceElems(ctx, f);
+  if (!p) return fail(ctx, KGB_ERR_ARG, std::string("field '") + f->name + "' cannot be filled");
+  if (v == 0.0) {
+    CK(cudaMemsetAsync(p, 0, n * ctx->tsz, ctx->stream));
+  } else if (ctx->prec == KGB_FP64) {
+    launch_fill<double>(as<double>(p), n, v, ctx->stream);
+    CKN(1);
+  } else {
+    launch_fill<float>(as<float>(p), n, v, ctx->stream);
+    CKN(1);
+  }
+  return KGB_OK;
+}
+
+int sweepSolver(kgb_ctx *ctx) {
+  for (int k = 0; k < 3; ++k) CK(cudaMemsetAsync(ctx->plane[k], 0, ctx->plane_chunk[k] * ctx->dc.num() * ctx->tsz, ctx->stream));
+  const int nlev = (int)ctx->level_off.size() - 1;
+  const int S[3] = {ctx->dc.Sx, ctx->dc.Sy, ctx->dc.Sz};
+  for (int lv = 0; lv < nlev; ++lv) {
+    const int b = ctx->level_off[lv], e = ctx->level_off[lv + 1];
+    if (e == b) continue;
+    int rc = sweepWaveAny(ctx, ctx->levels_d + b, e - b);
+    if (rc) return rc;
+    // hand the outgoing planes to downwind zone sets (ParallelComm.cpp:146-162)
+    for (int x = b; x < e; ++x) {
+      const int s = ctx->level_sdoms[x];
+      const SdomDesc &d = ctx->sdoms_h[s];
+      int co[5] = {d.p, d.q, d.xs, d.ys, d.zs};
+      const int dirv[3] = {d.id, d.jd, d.kd};
+      for (int dim = 0; dim < 3; ++dim) {
+        int dn[5] = {co[0], co[1], co[2], co[3], co[4]};
+        dn[2 + dim] += dirv[dim];
+        if (dn[2 + dim] < 0 || dn[2 + dim] >= S[dim]) continue;
+        const int t = ctx->dc.sdomOf(dn);
+        const size_t bytes = ctx->plane_chunk[dim] * ctx->tsz;
+        char *base = (char *)ctx->plane[dim];
+        CK(cudaMemcpyAsync(base + (size_t)t * bytes, base + (size_t)s * bytes, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+      }
+    }
+  }
+  return KGB_OK;
+}
+
+ScatterArgsBase scatterArgs(kgb_ctx *ctx) {
+  ScatterArgsBase a{};
+  a.Z = ctx->Z;
+  a.G = ctx->G;
+  a.M = ctx->M;
+  a.L = ctx->L;
+  a.zmix_start = ctx->zmix_start;
+  a.zmix_count = ctx->zmix_count;
+  a.mix_mat = ctx->mix_mat;
+  a.mix_frac = ctx->mix_frac;
+  a.gp_lo = ctx->gp_lo;
+  a.gp_hi = ctx->gp_hi;
+  a.src_glo = 0;
+  a.src_ghi = ctx->G;
+  a.dst_glo = 0;
+  a.dst_ghi = ctx->G;
+  return a;
+}
+
+int doLTimes(kgb_ctx *ctx, bool acc) {
+  FamScope fs(ctx, "ltimes");
+  const int64_t rows = ctx->Z * ctx->G;
+  if (ctx->prec == KGB_FP64)
+    launch_ltimes<double>(as<double>(ctx->psi), as<double>(ctx->phi), as<double>(ctx->ell), rows, ctx->D, ctx->M, acc, ctx->stream);
+  else
+    launch_ltimes<float>(as<float>(ctx->psi), as<float>(ctx->phi), as<float>(ctx->ell), rows, ctx->D, ctx->M, acc, ctx->stream);
+  CKN((ctx->M + 31) / 32);
+  return KGB_OK;
+}
+
+int doLPlusTimes(kgb_ctx *ctx, bool acc) {
+  FamScope fs(ctx, "lplustimes");
+  const int64_t rows = ctx->Z * ctx->G;
+  if (ctx->prec == KGB_FP64)
+    launch_lplustimes<double>(as<double>(ctx->phi_out), as<double>(ctx->rhs), as<double>(ctx->ellp), rows, ctx->D, ctx->M, acc, ctx->stream);
+  else
+    launch_lplustimes<float>(as<float>(ctx->phi_out), as<float>(ctx->rhs), as<float>(ctx->ellp), rows, ctx->D, ctx->M, acc, ctx->stream);
+  CKN(1);
+  return KGB_OK;
+}
+
+int doScattering(kgb_ctx *ctx, bool acc) {
+  FamScope fs(ctx, "scattering");
+  ScatterArgsBase a = scatterArgs(ctx);
+  if (ctx->prec == KGB_FP64)
+    launch_scattering<double>(as<double>(ctx->phi), as<double>(ctx->phi_out), as<double>(ctx->sigsT), a, acc, ctx->stream);
+  else
+    launch_scattering<float>(as<float>(ctx->phi), as<float>(ctx->phi_out), as<float>(ctx->sigsT), a, acc, ctx->stream);
+  CKN(1);
+  return KGB_OK;
+}
+
+int doSource(kgb_ctx *ctx, double q) {
+  FamScope fs(ctx, "source");
+  if (ctx->prec == KGB_FP64)
+    launch_source<double>(as<double>(ctx->phi_out), ctx->nmix, ctx->mix_zone, ctx->mix_mat, ctx->mix_frac, ctx->G, ctx->M, q, ctx->stream);
+  else
+    launch_source<float>(as<float>(ctx->phi_out), ctx->nmix, ctx->mix_zone, ctx->mix_mat, ctx->mix_frac, ctx->G, ctx->M, q, ctx->stream);
+  CKN((ctx->nmix * ctx->G > 0 ? 1 : 0));
+  return KGB_OK;
+}
+
+// population into device slot `out` (no host synchronisation)
+int doPopulation(kgb_ctx *ctx, double *out) {
+  FamScope fs(ctx, "population");
+  const int64_t rows = ctx->Z * ctx->G;
+  if (ctx->prec == KGB_FP64)
+    launch_population<double>(as<double>(ctx->psi), ctx->w_d, ctx->vol_d, rows, ctx->G, ctx->D, ctx->partials, ctx->npart, out, ctx->stream);
+  else
+    launch_population<float>(as<float>(ctx->psi), ctx->w_d, ctx->vol_d, rows, ctx->G, ctx->D, ctx->partials, ctx->npart, out, ctx->stream);
+  CKN(2);
+  return KGB_OK;
+}
+
+int iterateDevice(kgb_ctx *ctx, double q, double *part_slot) {
+  int rc;
+  if ((rc = doLTimes(ctx, false))) return rc;          // phi = L psi        (kConst + LTimes)
+  if ((rc = doScattering(ctx, false))) return rc;      // phi_out = S phi    (kConst + scattering)
+  if ((rc = doSource(ctx, q))) return rc;              // phi_out += Q
+  if ((rc = doLPlusTimes(ctx, false))) return rc;      // rhs = L+ phi_out   (kConst + LPlusTimes)
+  if ((rc = sweepSolver(ctx))) return rc;              // psi = H^-1 rhs
+  if (part_slot && (rc = doPopulation(ctx, part_slot))) return rc;
+  return KGB_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char *kgb_version(void) { return "kripke_gb300 0.1 sm_103a"; }
+
+int kgb_ctx_create(int device, kgb_ctx **out) {
+  if (!out) return KGB_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    cudaGetLastError();
+    return KGB_ERR_CUDA;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return KGB_ERR_CUDA;
+  kgb_ctx *c = new (std::nothrow) kgb_ctx();
+  if (!c) return KGB_ERR_OOM;
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return KGB_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  *out = c;
+  return KGB_OK;
+}
+
+int kgb_ctx_destroy(kgb_ctx *ctx) {
+  if (!ctx) return KGB_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto &kv : ctx->fams)
+    for (auto &pr : kv.second.pending) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  freeAll(ctx);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return KGB_OK;
+}
+
+const char *kgb_last_error(const kgb_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int kgb_setup(kgb_ctx *ctx, const kgb_dims *d) {
+  if (!ctx || !d) return KGB_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  if (d->layout < 0 || d->layout > 5) return fail(ctx, KGB_ERR_LAYOUT, "unknown layout");
+  if (d->precision != KGB_FP64 && d->precision != KGB_MIXED) return fail(ctx, KGB_ERR_ARG, "unknown precision");
+  if (d->nx < 1 || d->ny < 1 || d->nz < 1 || d->num_groups < 1 || d->num_directions < 8 || d->legendre_order < 0 ||
+      d->legendre_order > 7)
+    return fail(ctx, KGB_ERR_ARG, "bad problem size (zones >= 1, groups >= 1, directions >= 8, 0 <= legendre <= 7)");
+  if (d->num_groupsets < 1 || d->num_groups % d->num_groupsets)
+    return fail(ctx, KGB_ERR_ARG, "number of groups must be divisible by the number of group sets");
+  if (d->num_dirsets < 1 || (d->num_dirsets % 8 && d->num_dirsets < 8) || d->num_directions % d->num_dirsets)
+    return fail(ctx, KGB_ERR_ARG, "direction sets must be a multiple of 8 (or >= 8) and divide the directions");
+  for (int k = 0; k < 3; ++k)
+    if (d->num_zonesets[k] < 1) return fail(ctx, KGB_ERR_ARG, "zone sets must be >= 1");
+  if (d->nx % d->num_zonesets[0] || d->ny % d->num_zonesets[1] || d->nz % d->num_zonesets[2])
+    return fail(ctx, KGB_ERR_ARG, "zone sets must divide the zones");
+  cudaStreamSynchronize(ctx->stream);
+  freeAll(ctx);
+  ctx->dims = *d;
+  ctx->prec = d->precision;
+  ctx->tsz = ctx->prec == KGB_FP64 ? 8 : 4;
+  ctx->dc.SP = d->num_groupsets;
+  ctx->dc.SQ = d->num_dirsets;
+  ctx->dc.Sx = d->num_zonesets[0];
+  ctx->dc.Sy = d->num_zonesets[1];
+  ctx->dc.Sz = d->num_zonesets[2];
+  ctx->G = d->num_groups;
+  ctx->D = d->num_directions;
+  ctx->L = d->legendre_order;
+  ctx->M = (ctx->L + 1) * (ctx->L + 1);
+  ctx->Gs = ctx->G / ctx->dc.SP;
+  ctx->Ds = ctx->D / ctx->dc.SQ;
+  ctx->nx = d->nx; ctx->ny = d->ny; ctx->nz = d->nz;
+  ctx->nxs = d->nx / ctx->dc.Sx; ctx->nys = d->ny / ctx->dc.Sy; ctx->nzs = d->nz / ctx->dc.Sz;
+  ctx->Z = (int64_t)d->nx * d->ny * d->nz;
+  ctx->Zs = (int64_t)ctx->nxs * ctx->nys * ctx->nzs;
+  const int64_t nch = (int64_t)ctx->Gs * ctx->Ds;
+  ctx->plane_chunk[0] = nch * ctx->nys * ctx->nzs;
+  ctx->plane_chunk[1] = nch * ctx->nxs * ctx->nzs;
+  ctx->plane_chunk[2] = nch * ctx->nxs * ctx->nys;
+  const size_t T = ctx->tsz;
+  int rc;
+  const int64_t flux = ctx->Z * ctx->G * ctx->D, mom = ctx->Z * ctx->G * ctx->M;
+  if ((rc = dalloc(ctx, &ctx->psi, flux * T)) || (rc = dalloc(ctx, &ctx->rhs, flux * T)) ||
+      (rc = dalloc(ctx, &ctx->phi, mom * T)) || (rc = dalloc(ctx, &ctx->phi_out, mom * T)) ||
+      (rc = dalloc(ctx, &ctx->sigt, ctx->Z * ctx->G * T)))
+    goto oom;
+  for (int k = 0; k < 3; ++k)
+    if ((rc = dalloc(ctx, &ctx->plane[k], ctx->plane_chunk[k] * ctx->dc.num() * T))) goto oom;
+  if ((rc = dalloc(ctx, &ctx->ell, (size_t)ctx->D * ctx->M * T)) || (rc = dalloc(ctx, &ctx->ellp, (size_t)ctx->D * ctx->M * T)) ||
+      (rc = dalloc(ctx, &ctx->sigsT, (size_t)3 * (ctx->L + 1) * ctx->G * ctx->G * T)) ||
+      (rc = dalloc(ctx, &ctx->cx, (size_t)ctx->D * ctx->nx * T)) || (rc = dalloc(ctx, &ctx->cy, (size_t)ctx->D * ctx->ny * T)) ||
+      (rc = dalloc(ctx, &ctx->cz, (size_t)ctx->D * ctx->nz * T)))
+    goto oom;
+  if ((rc = dmalloc(ctx, &ctx->w_d, ctx->D)) || (rc = dmalloc(ctx, &ctx->cos_d[0], ctx->D)) ||
+      (rc = dmalloc(ctx, &ctx->cos_d[1], ctx->D)) || (rc = dmalloc(ctx, &ctx->cos_d[2], ctx->D)) ||
+      (rc = dmalloc(ctx, &ctx->vol_d, ctx->Z)) || (rc = dmalloc(ctx, &ctx->dxyz_d[0], ctx->nx)) ||
+      (rc = dmalloc(ctx, &ctx->dxyz_d[1], ctx->ny)) || (rc = dmalloc(ctx, &ctx->dxyz_d[2], ctx->nz)) ||
+      (rc = dmalloc(ctx, &ctx->zmix_start, ctx->Z)) || (rc = dmalloc(ctx, &ctx->zmix_count, ctx->Z)) ||
+      (rc = dmalloc(ctx, &ctx->gp_lo, ctx->G)) || (rc = dmalloc(ctx, &ctx->gp_hi, ctx->G)) ||
+      (rc = dmalloc(ctx, &ctx->sdoms_d, ctx->dc.num())) || (rc = dmalloc(ctx, &ctx->ident_d, ctx->dc.num())) ||
+      (rc = dmalloc(ctx, &ctx->levels_d, ctx->dc.num())))
+    goto oom;
+  ctx->npart = 152 * 4;
+  if ((rc = dmalloc(ctx, &ctx->partials, 2 * ctx->npart)) || (rc = dmalloc(ctx, &ctx->results, 16))) goto oom;
+  {
+    std::vector<int> ident(ctx->dc.num());
+    for (int s = 0; s < ctx->dc.num(); ++s) ident[s] = s;
+    CK(cudaMemcpyAsync(ctx->ident_d, ident.data(), ident.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  for (auto &v : ctx->q) v.assign(ctx->D, 0.0);
+  for (auto &v : ctx->qi) v.assign(ctx->D, 1);
+  ctx->dxyz[0].assign(ctx->nx, 1.0);
+  ctx->dxyz[1].assign(ctx->ny, 1.0);
+  ctx->dxyz[2].assign(ctx->nz, 1.0);
+  ctx->ell_h.assign((size_t)ctx->D * ctx->M, 0.0);
+  ctx->ellp_h.assign((size_t)ctx->D * ctx->M, 0.0);
+  ctx->sigs_h.assign((size_t)3 * (ctx->L + 1) * ctx->G * ctx->G, 0.0);
+  ctx->vol_h.assign(ctx->Z, 0.0);
+  for (int k = 0; k < 2; ++k) {
+    ctx->zmap[k].assign(ctx->dc.chunks(S_R), std::vector<int>(ctx->Zs, 0));
+    ctx->mimap[k].assign(ctx->dc.chunks(S_R), std::vector<int>());
+  }
+  ctx->mfrac.assign(ctx->dc.chunks(S_R), std::vector<double>());
+  ctx->m2l.resize(ctx->M);
+  for (int n = 0, nm = 0; n <= ctx->L; ++n)
+    for (int m = -n; m <= n; ++m) ctx->m2l[nm++] = n;
+  for (bool &h : ctx->have) h = false;
+  ctx->have[fieldIndex(findField("moment_to_legendre"))] = true;
+  ctx->dirty_quad = ctx->dirty_geom = ctx->dirty_ell = ctx->dirty_sigs = ctx->dirty_mix = ctx->dirty_vol = true;
+  ctx->ready = true;
+  if ((rc = buildTiles(ctx))) goto oom;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return KGB_OK;
+oom:
+  {
+    std::string msg = ctx->err;
+    freeAll(ctx);
+    ctx->err = msg;
+  }
+  return rc;
+}
+
+int kgb_num_subdomains(const kgb_ctx *ctx, int32_t *out) {
+  if (!ctx || !out) return KGB_ERR_ARG;
+  if (!ctx->ready) return KGB_ERR_STATE;
+  *out = ctx->dc.num();
+  return KGB_OK;
+}
+
+int kgb_field_bytes(kgb_ctx *ctx, const char *name, int64_t *nbytes) {
+  if (!ctx || !nbytes) return KGB_ERR_ARG;
+  if (!ctx->ready) return fail(ctx, KGB_ERR_STATE, "kgb_setup has not been called");
+  const FieldInfo *f = findField(name);
+  if (!f) return fail(ctx, KGB_ERR_ARG, std::string("unknown field '") + (name ? name : "(null)") + "'");
+  *nbytes = fieldBytes(ctx, f);
+  return KGB_OK;
+}
+
+int kgb_field_upload(kgb_ctx *ctx, const char *name, const void *host, int64_t nbytes) {
+  if (!ctx) return KGB_ERR_ARG;
+  if (!ctx->ready) return fail(ctx, KGB_ERR_STATE, "kgb_setup has not been called");
+  const FieldInfo *f = findField(name);
+  if (!f) return fail(ctx, KGB_ERR_ARG, std::string("unknown field '") + (name ? name : "(null)") + "'");
+  if (!host && nbytes > 0) return fail(ctx, KGB_ERR_ARG, "null host pointer");
+  const int64_t want = fieldBytes(ctx, f);
+  if (nbytes != want)
+    return fail(ctx, KGB_ERR_ARG, std::string("field '") + name + "' expects " + std::to_string(want) + " bytes, got " + std::to_string(nbytes));
+  CK(cudaSetDevice(ctx->device));
+  const int nch = numChunks(ctx, f);
+  const int layout = ctx->dims.layout;
+  if (deviceKind(f->kind)) {
+    size_t maxc = 0;
+    for (int ch = 0; ch < nch; ++ch) maxc = std::max<size_t>(maxc, chunkElems(chunkGeom(ctx, f, ch)) * 8);
+    int rc = ensureStaging(ctx, maxc);
+    if (rc) return rc;
+    const char *src = (const char *)host;
+    void *dev = deviceArray(ctx, f);
+    for (int ch = 0; ch < nch; ++ch) {
+      const int64_t ne = chunkElems(chunkGeom(ctx, f, ch));
+      CK(cudaMemcpyAsync(ctx->staging, src, ne * 8, cudaMemcpyHostToDevice, ctx->stream));
+      XposeDesc x = chunkXpose(ctx, f, ch);
+      if (ctx->prec == KGB_FP64) launch_upload_xpose<double>(ctx->staging, as<double>(dev), x, ctx->stream);
+      else launch_upload_xpose<float>(ctx->staging, as<float>(dev), x, ctx->stream);
+      CKN(1);
+      src += ne * 8;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->have[fieldIndex(f)] = true;
+    return KGB_OK;
+  }
+  // host-side inputs: convert the chunks into global host tables
+  const double *hd = (const double *)host;
+  const int32_t *hi = (const int32_t *)host;
+  int64_t off = 0;
+  for (int ch = 0; ch < nch; ++ch) {
+    ChunkGeom g = chunkGeom(ctx, f, ch);
+    int64_t st[4] = {1, 1, 1, 1};
+    nestStrides(layout, g.nd, g.types, g.dims, st);
+    int co[5];
+    ctx->dc.chunkCoord(g.space, ch, co);
+    const int dlo = co[1] * ctx->Ds;
+    switch (f->kind) {
+      case K_ELL:
+        for (int m = 0; m < ctx->M; ++m)
+          for (int d = 0; d < ctx->Ds; ++d) ctx->ell_h[(size_t)(dlo + d) * ctx->M + m] = hd[off + m * st[0] + d * st[1]];
+        break;
+      case K_ELLP:
+        for (int d = 0; d < ctx->Ds; ++d)
+          for (int m = 0; m < ctx->M; ++m) ctx->ellp_h[(size_t)(dlo + d) * ctx->M + m] = hd[off + d * st[0] + m * st[1]];
+        break;
+      case K_SIGS: {
+        const int L1 = ctx->L + 1, G = ctx->G;
+        for (int m = 0; m < 3; ++m)
+          for (int l = 0; l < L1; ++l)
+            for (int g2 = 0; g2 < G; ++g2)
+              for (int gp = 0; gp < G; ++gp)
+                ctx->sigs_h[(((size_t)m * L1 + l) * G + g2) * G + gp] = hd[off + m * st[0] + l * st[1] + g2 * st[2] + gp * st[3]];
+        break;
+      }
+      case K_QD:
+        for (int d = 0; d < ctx->Ds; ++d) ctx->q[f->which][dlo + d] = hd[off + d];
+        break;
+      case K_QI:
+        for (int d = 0; d < ctx->Ds; ++d) {
+          const int v = hi[off + d];
+          if (v != 1 && v != -1) return fail(ctx, KGB_ERR_ARG, "direction flags must be +1 or -1");
+          ctx->qi[f->which][dlo + d] = v;
+        }
+        break;
+      case K_DXYZ: {
+        const int n = (int)g.dims[0], o = co[2 + f->which] * n;
+        for (int i = 0; i < n; ++i) {
+          if (!(hd[off + i] > 0.0)) return fail(ctx, KGB_ERR_ARG, "zone widths must be positive");
+          ctx->dxyz[f->which][o + i] = hd[off + i];
+        }
+        break;
+      }
+      case K_VOL: {
+        const int io = co[2] * ctx->nxs, jo = co[3] * ctx->nys, ko = co[4] * ctx->nzs;
+        for (int64_t zl = 0; zl < ctx->Zs; ++zl) {
+          int64_t i = zl % ctx->nxs, j = (zl / ctx->nxs) % ctx->nys, k = zl / ((int64_t)ctx->nxs * ctx->nys);
+          ctx->vol_h[((k + ko) * ctx->ny + (j + jo)) * ctx->nx + (i + io)] = hd[off + zl];
+        }
+        break;
+      }
+      case K_ZI: {
+        const int r = ctx->dc.rIndex(co);
+        ctx->zmap[f->which][r].assign(hi + off, hi + off + ctx->Zs);
+        break;
+      }
+      case K_MI: {
+        const int r = ctx->dc.rIndex(co);
+        ctx->mimap[f->which][r].assign(hi + off, hi + off + g.dims[0]);
+        break;
+      }
+      case K_MD: {
+        const int r = ctx->dc.rIndex(co);
+        ctx->mfrac[r].assign(hd + off, hd + off + g.dims[0]);
+        break;
+      }
+      case K_M2L:
+        for (int m = 0; m < ctx->M; ++m)
+          if (hi[off + m] != ctx->m2l[m]) return fail(ctx, KGB_ERR_ARG, "moment_to_legendre must list n=0..L with 2n+1 moments each");
+        break;
+      default: break;
+    }
+    off += chunkElems(g);
+  }
+  switch (f->kind) {
+    case K_ELL: case K_ELLP: ctx->dirty_ell = true; break;
+    case K_SIGS: ctx->dirty_sigs = true; break;
+    case K_QD: case K_QI: ctx->dirty_quad = true; ctx->dirty_geom = true; break;
+    case K_DXYZ: ctx->dirty_geom = true; break;
+    case K_VOL: ctx->dirty_vol = true; break;
+    case K_ZI: case K_MI: case K_MD: ctx->dirty_mix = true; break;
+    default: break;
+  }
+  if (f->kind == K_ZI && f->which == 1) {
+    // counts changed: mixed-element fields must be uploaded again
+    for (const char *n : {"mixelem_to_zone", "mixelem_to_material", "mixelem_to_fraction"}) ctx->have[fieldIndex(findField(n))] = false;
+  }
+  ctx->have[fieldIndex(f)] = true;
+  return KGB_OK;
+}
+
+int kgb_field_download(kgb_ctx *ctx, const char *name, void *host, int64_t nbytes) {
+  if (!ctx) return KGB_ERR_ARG;
+  if (!ctx->ready) return fail(ctx, KGB_ERR_STATE, "kgb_setup has not been called");
+  const FieldInfo *f = findField(name);
+  if (!f) return fail(ctx, KGB_ERR_ARG, std::string("unknown field '") + (name ? name : "(null)") + "'");
+  if (!host && nbytes > 0) return fail(ctx, KGB_ERR_ARG, "null host pointer");
+  const int64_t want = fieldBytes(ctx, f);
+  if (nbytes != want)
+    return fail(ctx, KGB_ERR_ARG, std::string("field '") + name + "' holds " + std::to_string(want) + " bytes, got " + std::to_string(nbytes));
+  CK(cudaSetDevice(ctx->device));
+  const int nch = numChunks(ctx, f);
+  if (deviceKind(f->kind)) {
+    size_t maxc = 0;
+    for (int ch = 0; ch < nch; ++ch) maxc = std::max<size_t>(maxc, chunkElems(chunkGeom(ctx, f, ch)) * 8);
+    int rc = ensureStaging(ctx, maxc);
+    if (rc) return rc;
+    char *dst = (char *)host;
+    const void *dev = deviceArray(ctx, f);
+    for (int ch = 0; ch < nch; ++ch) {
+      const int64_t ne = chunkElems(chunkGeom(ctx, f, ch));
+      XposeDesc x = chunkXpose(ctx, f, ch);
+      if (ctx->prec == KGB_FP64) launch_download_xpose<double>(as<const double>(const_cast<void *>(dev)), ctx->staging, x, ctx->stream);
+      else launch_download_xpose<float>(as<const float>(const_cast<void *>(dev)), ctx->staging, x, ctx->stream);
+      CKN(1);
+      CK(cudaMemcpyAsync(dst, ctx->staging, ne * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+      dst += ne * 8;
+    }
+    return KGB_OK;
+  }
+  // host-side inputs: rebuild Kripke's chunks from the global tables
+  double *hd = (double *)host;
+  int32_t *hi = (int32_t *)host;
+  int64_t off = 0;
+  for (int ch = 0; ch < nch; ++ch) {
+    ChunkGeom g = chunkGeom(ctx, f, ch);
+    int64_t st[4] = {1, 1, 1, 1};
+    nestStrides(ctx->dims.layout, g.nd, g.types, g.dims, st);
+    int co[5];
+    ctx->dc.chunkCoord(g.space, ch, co);
+    const int dlo = co[1] * ctx->Ds;
+    switch (f->kind) {
+      case K_ELL:
+        for (int m = 0; m < ctx->M; ++m)
+          for (int d = 0; d < ctx->Ds; ++d) hd[off + m * st[0] + d * st[1]] = ctx->ell_h[(size_t)(dlo + d) * ctx->M + m];
+        break;
+      case K_ELLP:
+        for (int d = 0; d < ctx->Ds; ++d)
+          for (int m = 0; m < ctx->M; ++m) hd[off + d * st[0] + m * st[1]] = ctx->ellp_h[(size_t)(dlo + d) * ctx->M + m];
+        break;
+      case K_SIGS: {
+        const int L1 = ctx->L + 1, G = ctx->G;
+        for (int m = 0; m < 3; ++m)
+          for (int l = 0; l < L1; ++l)
+            for (int g2 = 0; g2 < G; ++g2)
+              for (int gp = 0; gp < G; ++gp)
+                hd[off + m * st[0] + l * st[1] + g2 * st[2] + gp * st[3]] = ctx->sigs_h[(((size_t)m * L1 + l) * G + g2) * G + gp];
+        break;
+      }
+      case K_QD:
+        for (int d = 0; d < ctx->Ds; ++d) hd[off + d] = ctx->q[f->which][dlo + d];
+        break;
+      case K_QI:
+        for (int d = 0; d < ctx->Ds; ++d) hi[off + d] = ctx->qi[f->which][dlo + d];
+        break;
+      case K_DXYZ: {
+        const int n = (int)g.dims[0], o = co[2 + f->which] * n;
+        for (int i = 0; i < n; ++i) hd[off + i] = ctx->dxyz[f->which][o + i];
+        break;
+      }
+      case K_VOL: {
+        const int io = co[2] * ctx->nxs, jo = co[3] * ctx->nys, ko = co[4] * ctx->nzs;
+        for (int64_t zl = 0; zl < ctx->Zs; ++zl) {
+          int64_t i = zl % ctx->nxs, j = (zl / ctx->nxs) % ctx->nys, k = zl / ((int64_t)ctx->nxs * ctx->nys);
+          hd[off + zl] = ctx->vol_h[((k + ko) * ctx->ny + (j + jo)) * ctx->nx + (i + io)];
+        }
+        break;
+      }
+      case K_ZI: {
+        const int r = ctx->dc.rIndex(co);
+        std::copy(ctx->zmap[f->which][r].begin(), ctx->zmap[f->which][r].end(), hi + off);
+        break;
+      }
+      case K_MI: {
+        const int r = ctx->dc.rIndex(co);
+        std::copy(ctx->mimap[f->which][r].begin(), ctx->mimap[f->which][r].end(), hi + off);
+        break;
+      }
+      case K_MD: {
+        const int r = ctx->dc.rIndex(co);
+        std::copy(ctx->mfrac[r].begin(), ctx->mfrac[r].end(), hd + off);
+        break;
+      }
+      case K_M2L:
+        for (int m = 0; m < ctx->M; ++m) hi[off + m] = ctx->m2l[m];
+        break;
+      default: break;
+    }
+    off += chunkElems(g);
+  }
+  return KGB_OK;
+}
+
+int kgb_field_fill(kgb_ctx *ctx, const char *name, double value) {
+  if (!ctx) return KGB_ERR_ARG;
+  if (!ctx->ready) return fail(ctx, KGB_ERR_STATE, "kgb_setup has not been called");
+  const FieldInfo *f = findField(name);
+  if (!f) return fail(ctx, KGB_ERR_ARG, std::string("unknown field '") + (name ? name : "(null)") + "'");
+  CK(cudaSetDevice(ctx->device));
+  return fillField(ctx, f, value);
+}
+
+int kgb_ltimes(kgb_ctx *ctx) {
+  int rc = prepare(ctx);
+  return rc ? rc : doLTimes(ctx, true);
+}
+
+int kgb_lplustimes(kgb_ctx *ctx) {
+  int rc = prepare(ctx);
+  return rc ? rc : doLPlusTimes(ctx, true);
+}
+
+int kgb_scattering(kgb_ctx *ctx) {
+  int rc = prepare(ctx);
+  return rc ? rc : doScattering(ctx, true);
+}
+
+int kgb_source(kgb_ctx *ctx, double q) {
+  int rc = prepare(ctx);
+  return rc ? rc : doSource(ctx, q);
+}
+
+int kgb_sweep_subdomain(kgb_ctx *ctx, int32_t sdom) {
+  int rc = prepare(ctx);
+  if (rc) return rc;
+  if (sdom < 0 || sdom >= ctx->dc.num()) return fail(ctx, KGB_ERR_ARG, "subdomain id out of range");
+  return sweepWaveAny(ctx, ctx->ident_d + sdom, 1);
+}
+
+int kgb_sweep_solver(kgb_ctx *ctx) {
+  int rc = prepare(ctx);
+  return rc ? rc : sweepSolver(ctx);
+}
+
+int kgb_population(kgb_ctx *ctx, double *out) {
+  if (!out) return fail(ctx, KGB_ERR_ARG, "null output");
+  int rc = prepare(ctx);
+  if (rc) return rc;
+  if ((rc = doPopulation(ctx, ctx->results))) return rc;
+  CK(cudaMemcpyAsync(out, ctx->results, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return KGB_OK;
+}
+
+int kgb_balance(kgb_ctx *ctx, double out[5]) {
+  if (!out) return fail(ctx, KGB_ERR_ARG, "null output");
+  int rc = prepare(ctx);
+  if (rc) return rc;
+  const int64_t rows = ctx->Z * ctx->G;
+  CK(cudaMemsetAsync(ctx->results, 0, 8 * sizeof(double), ctx->stream));
+  if (ctx->prec == KGB_FP64)
+    launch_balance_terms<double>(as<double>(ctx->psi), as<double>(ctx->rhs), as<double>(ctx->sigt), ctx->w_d, ctx->vol_d, rows, ctx->G, ctx->D, ctx->partials, ctx->npart, ctx->results, ctx->stream);
+  else
+    launch_balance_terms<float>(as<float>(ctx->psi), as<float>(ctx->rhs), as<float>(ctx->sigt), ctx->w_d, ctx->vol_d, rows, ctx->G, ctx->D, ctx->partials, ctx->npart, ctx->results, ctx->stream);
+  CKN(3);
+  // leakage through the planes of subdomains whose downwind face is the domain boundary
+  const int S[3] = {ctx->dc.Sx, ctx->dc.Sy, ctx->dc.Sz};
+  for (int s = 0; s < ctx->dc.num(); ++s) {
+    const SdomDesc &d = ctx->sdoms_h[s];
+    const int co[5] = {d.p, d.q, d.xs, d.ys, d.zs};
+    const int dirv[3] = {d.id, d.jd, d.kd};
+    for (int dim = 0; dim < 3; ++dim) {
+      const int dn = co[2 + dim] + dirv[dim];
+      if (dn >= 0 && dn < S[dim]) continue;
+      // plane chunk [nb][na][Gs][Ds]; face area = wa(a) * wb(b) in global zone widths
+      const double *wa, *wb;
+      int na;
+      if (dim == 0) { wa = ctx->dxyz_d[1] + d.jo; wb = ctx->dxyz_d[2] + d.ko; na = ctx->nys; }
+      else if (dim == 1) { wa = ctx->dxyz_d[0] + d.io; wb = ctx->dxyz_d[2] + d.ko; na = ctx->nxs; }
+      else { wa = ctx->dxyz_d[0] + d.io; wb = ctx->dxyz_d[1] + d.jo; na = ctx->nxs; }
+      const int64_t ne = ctx->plane_chunk[dim];
+      const int64_t off = (int64_t)s * ne;
+      if (ctx->prec == KGB_FP64)
+        launch_leakage<double>(as<double>(ctx->plane[dim]) + off, ne, ctx->Gs, ctx->Ds, d.dlo, na, ctx->w_d, ctx->cos_d[dim], wa, wb, ctx->partials, ctx->npart, ctx->results + 2, ctx->stream);
+      else
+        launch_leakage<float>(as<float>(ctx->plane[dim]) + off, ne, ctx->Gs, ctx->Ds, d.dlo, na, ctx->w_d, ctx->cos_d[dim], wa, wb, ctx->partials, ctx->npart, ctx->results + 2, ctx->stream);
+      CKN(2);
+    }
+  }
+  if ((rc = doPopulation(ctx, ctx->results + 3))) return rc;
+  double h[4];
+  CK(cudaMemcpyAsync(h, ctx->results, 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  out[0] = h[0];
+  out[1] = h[1];
+  out[2] = h[2];
+  out[3] = h[3];
+  out[4] = h[0] - h[1] - h[2];
+  return KGB_OK;
+}
+
+int kgb_iterate(kgb_ctx *ctx, double q, double *part) {
+  int rc = prepare(ctx);
+  if (rc) return rc;
+  if ((rc = iterateDevice(ctx, q, ctx->results))) return rc;
+  if (part) {
+    CK(cudaMemcpyAsync(part, ctx->results, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return KGB_OK;
+}
+
+int kgb_solve(kgb_ctx *ctx, int32_t niter, double q, double *part) {
+  int rc = prepare(ctx);
+  if (rc) return rc;
+  if (niter < 1) return fail(ctx, KGB_ERR_ARG, "niter must be >= 1");
+  if (niter > ctx->parts_cap) {
+    if (ctx->parts_dev) cudaFree(ctx->parts_dev);
+    ctx->parts_dev = nullptr;
+    ctx->parts_cap = 0;
+    if ((rc = dmalloc(ctx, &ctx->parts_dev, niter))) return rc;
+    ctx->parts_cap = niter;
+  }
+  CK(cudaMemsetAsync(ctx->psi, 0, ctx->Z * ctx->G * ctx->D * ctx->tsz, ctx->stream));  // kConst(psi, 0)
+  for (int it = 0; it < niter; ++it)
+    if ((rc = iterateDevice(ctx, q, ctx->parts_dev + it))) return rc;
+  if (part) CK(cudaMemcpyAsync(part, ctx->parts_dev, niter * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return KGB_OK;
+}
+
+int kgb_sync(kgb_ctx *ctx) {
+  if (!ctx) return KGB_ERR_ARG;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return KGB_OK;
+}
+
+int kgb_set_stream(kgb_ctx *ctx, void *s) {
+  if (!ctx) return KGB_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->stream = s ? (cudaStream_t)s : ctx->own_stream;
+  return KGB_OK;
+}
+
+int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
+  if (!ctx || !key) return KGB_ERR_ARG;
+  if (!std::strcmp(key, "sweep_tile_z")) {
+    if (value < 1 || value > 1024) return fail(ctx, KGB_ERR_ARG, "sweep_tile_z must be in [1, 1024]");
+    ctx->tz = (int)value;
+    if (ctx->ready) return buildTiles(ctx);
+    return KGB_OK;
+  }
+  return fail(ctx, KGB_ERR_ARG, std::string("unknown option '") + key + "'");
+}
+
+int kgb_set_timing(kgb_ctx *ctx, int on) {
+  if (!ctx) return KGB_ERR_ARG;
+  ctx->timing = on != 0;
+  return KGB_OK;
+}
+
+int kgb_kernel_time(kgb_ctx *ctx, const char *family, double *ms, int64_t *launches) {
+  if (!ctx || !family || !ms || !launches) return KGB_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  auto it = ctx->fams.find(family);
+  if (it == ctx->fams.end()) {
+    *ms = 0.0;
+    *launches = 0;
+    return KGB_OK;
+  }
+  TimerFam &f = it->second;
+  for (auto &pr : f.pending) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, pr.first, pr.second);
+    f.ms += t;
+    cudaEventDestroy(pr.first);
+    cudaEventDestroy(pr.second);
+  }
+  f.pending.clear();
+  *ms = f.ms;
+  *launches = f.launches;
+  return KGB_OK;
+}
+
+int kgb_launch_count(kgb_ctx *ctx, int64_t *out) {
+  if (!ctx || !out) return KGB_ERR_ARG;
+  *out = ctx->launches;
+  return KGB_OK;
+}
+
+int kgb_reset_timers(kgb_ctx *ctx) {
+  if (!ctx) return KGB_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (auto &kv : ctx->fams)
+    for (auto &pr : kv.second.pending) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  ctx->fams.clear();
+  return KGB_OK;
+}
+
+}  // extern "C"

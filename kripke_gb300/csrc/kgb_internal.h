@@ -1,0 +1,108 @@
+// kgb_internal.h -- device data model and kernel launchers of kripke_gb300.
+//
+// Device nesting (chosen for the GPU, independent of the host nesting):
+//   psi, rhs       [Z][G][D]   zone-major over the whole problem, direction fastest
+//   phi, phi_out   [Z][G][M]   moment fastest
+//   sigt_zonal     [Z][G]
+//   planes         per subdomain chunk: i_plane [nzs][nys][Gs][Ds],
+//                  j_plane [nzs][nxs][Gs][Ds], k_plane [nys][nxs][Gs][Ds]
+// with Z = global zone index (k*ny + j)*nx + i.  A subdomain's (group,
+// direction) pairs are "chains" c = g_local*Ds + d_local; chains are the
+// fastest index everywhere the sweep touches memory, so one warp reads and
+// writes contiguous runs.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/kgb.h"
+
+namespace kgb {
+
+// Per-subdomain sweep descriptor (device copy).
+struct SdomDesc {
+  int p, q, xs, ys, zs;   // coordinates in (P, Q, Rx, Ry, Rz)
+  int glo, dlo;           // first global group / direction
+  int io, jo, ko;         // zone-set origin in global zones
+  int id, jd, kd;         // traversal of the subdomain's first direction
+  int64_t ip, jp, kp;     // element offsets of its plane chunks
+};
+
+template <typename T>
+struct SweepArgs {
+  const T *rhs;
+  T *psi;
+  const T *sigt;
+  T *iplane, *jplane, *kplane;
+  const T *cx, *cy, *cz;      // 2*cos/delta per (direction, zone index): [D][nx], [D][ny], [D][nz]
+  const SdomDesc *sdoms;
+  const int *wave;            // subdomains swept by this launch
+  const int4 *tiles;          // oriented tile coordinates of every step, concatenated
+  int tile_off;               // first tile of this step
+  int nx, ny, nz, G, D, Gs, Ds, nxs, nys, nzs;
+  int tz;                     // tile depth in k
+};
+
+// Sweep tile footprint in i and j (compile-time); depth in k is runtime.
+constexpr int kTileX = 4;
+constexpr int kTileY = 4;
+constexpr int kSweepThreads = 128;
+
+template <typename T>
+void launch_sweep_step(const SweepArgs<T> &a, int ntiles, int nwave, cudaStream_t s);
+
+template <typename T>
+void launch_ltimes(const T *psi, T *phi, const T *ell_dm, int64_t rows, int D, int M, bool accumulate, cudaStream_t s);
+template <typename T>
+void launch_lplustimes(const T *phi_out, T *rhs, const T *ellp_dm, int64_t rows, int D, int M, bool accumulate, cudaStream_t s);
+
+struct ScatterArgsBase {
+  int64_t Z;
+  int G, M, L;
+  const int *zmix_start, *zmix_count, *mix_mat;
+  const double *mix_frac;
+  const int *gp_lo, *gp_hi;   // nonzero source-group range per destination group
+  int src_glo, src_ghi;       // source groups [lo, hi) taken (group-set pairs)
+  int dst_glo, dst_ghi;       // destination groups updated
+};
+template <typename T>
+void launch_scattering(const T *phi, T *phi_out, const T *sigsT, const ScatterArgsBase &a, bool accumulate, cudaStream_t s);
+template <typename T>
+void launch_source(T *phi_out, int64_t nmix, const int *mix_zone, const int *mix_mat, const double *mix_frac,
+                   int G, int M, double strength, cudaStream_t s);
+
+// FP64 reductions, two passes with a fixed order: per-block partials then one block.
+template <typename T>
+void launch_population(const T *psi, const double *w, const double *vol, int64_t rows, int G, int D,
+                       double *partials, int nblocks, double *out, cudaStream_t s);
+template <typename T>
+void launch_balance_terms(const T *psi, const T *rhs, const T *sigt, const double *w, const double *vol,
+                          int64_t rows, int G, int D, double *partials, int nblocks, double *out2, cudaStream_t s);
+template <typename T>
+void launch_leakage(const T *plane, int64_t nelem, int Gs, int Ds, int dlo, int na, const double *w,
+                    const double *cosv, const double *wa, const double *wb, double *partials, int nblocks,
+                    double *out, cudaStream_t s);
+
+// Layout transfer between a host-nested chunk and the device nesting.
+struct XposeDesc {
+  int nd;                 // logical dims (<= 4)
+  int64_t n[4];           // logical sizes
+  int64_t hs[4];          // host strides (elements)
+  int64_t os[4];          // device strides (elements); the zone dim uses os for the global zone
+  int zdim;               // logical dim that is a zone index (-1: none)
+  int nxs, nys;           // zone-set shape for local->global zone mapping
+  int io, jo, ko, nx, ny; // zone-set origin and global shape
+  int iter[4];            // iteration order, fastest last (matches the device-fastest dim)
+  int64_t obase;
+};
+template <typename Td>
+void launch_upload_xpose(const double *staging, Td *dev, const XposeDesc &x, cudaStream_t s);
+template <typename Td>
+void launch_download_xpose(const Td *dev, double *staging, const XposeDesc &x, cudaStream_t s);
+template <typename T>
+void launch_fill(T *p, int64_t n, double v, cudaStream_t s);
+
+}  // namespace kgb

@@ -1,0 +1,109 @@
+// scatter.cu -- group-to-group scattering and the isotropic source on GB300.
+//
+// Replaces Kernel::scattering (src/Kripke/Kernel/Scattering.cpp:59-100,
+// 137-145) and Kernel::source (src/Kripke/Kernel/Source.cpp:57-76).
+//   phi_out(nm,g,z) += sum_g' [sum_mix f * sigs(mat, l(nm), g, g')] * phi(nm,g',z)
+// One thread owns a (zone, destination group) row and loops over Legendre
+// orders l; the 2l+1 moments of order l share one coefficient per source
+// group.  The coefficient is built exactly as the reference does (sum over the
+// zone's mix elements of sigs*fraction, starting from 0).  Source groups are
+// visited in ascending order and only over the range where any material's
+// matrix row is nonzero (adding an exact zero term leaves the sum unchanged).
+// sigs is stored transposed, [mat][l][g'][g], so a warp's coefficient loads
+// are contiguous.
+#include "kgb_internal.h"
+
+namespace kgb {
+
+namespace {
+constexpr int kScatThreads = 128;
+
+template <typename T, int LMAX>
+__global__ void __launch_bounds__(kScatThreads) scattering_kernel(const T *__restrict__ phi, T *__restrict__ phi_out,
+                                                                 const T *__restrict__ sigsT, const ScatterArgsBase a,
+                                                                 bool accumulate) {
+  const int Gd = a.dst_ghi - a.dst_glo;
+  const int64_t rows = a.Z * Gd;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t z = r / Gd;
+    const int g = a.dst_glo + (int)(r - z * Gd);
+    const int ms = a.zmix_start[z], mcnt = a.zmix_count[z];
+    const int lo = max(a.gp_lo[g], a.src_glo);
+    const int hi = min(a.gp_hi[g] + 1, a.src_ghi);
+    for (int l = 0; l <= a.L; ++l) {
+      const int mb = l * l, na = 2 * l + 1;
+      T acc[2 * LMAX + 1];
+#pragma unroll
+      for (int x = 0; x < 2 * LMAX + 1; ++x) acc[x] = T(0);
+      for (int gp = lo; gp < hi; ++gp) {
+        T s = T(0);
+        for (int x = 0; x < mcnt; ++x) {
+          const int mat = a.mix_mat[ms + x];
+          s += sigsT[(((int64_t)mat * (a.L + 1) + l) * a.G + gp) * a.G + g] * (T)a.mix_frac[ms + x];
+        }
+        const T *ph = phi + (z * a.G + gp) * a.M + mb;
+#pragma unroll
+        for (int x = 0; x < 2 * LMAX + 1; ++x)
+          if (x < na) acc[x] += s * ph[x];
+      }
+      T *o = phi_out + (z * a.G + g) * a.M + mb;
+#pragma unroll
+      for (int x = 0; x < 2 * LMAX + 1; ++x)
+        if (x < na) o[x] = accumulate ? o[x] + acc[x] : acc[x];
+    }
+  }
+}
+
+template <typename T>
+__global__ void source_kernel(T *__restrict__ phi_out, int64_t nmix, const int *__restrict__ mix_zone,
+                              const int *__restrict__ mix_mat, const double *__restrict__ mix_frac, int G, int M,
+                              double strength) {
+  const int64_t n = nmix * G;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t mix = t / G;
+    const int g = (int)(t - mix * G);
+    if (mix_mat[mix] == 0) {
+      T *o = phi_out + ((int64_t)mix_zone[mix] * G + g) * M;  // moment 0
+      *o += (T)(strength * mix_frac[mix]);
+    }
+  }
+}
+
+int gridFor(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  const int64_t cap = 152 * 16;
+  return (int)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+}  // namespace
+
+template <typename T>
+void launch_scattering(const T *phi, T *phi_out, const T *sigsT, const ScatterArgsBase &a, bool accumulate,
+                       cudaStream_t s) {
+  const int64_t rows = a.Z * (a.dst_ghi - a.dst_glo);
+  const int grid = gridFor(rows, kScatThreads);
+  switch (a.L) {
+    case 0: scattering_kernel<T, 0><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
+    case 1: scattering_kernel<T, 1><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
+    case 2: scattering_kernel<T, 2><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
+    case 3: scattering_kernel<T, 3><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
+    case 4: scattering_kernel<T, 4><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
+    case 5: scattering_kernel<T, 5><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
+    case 6: scattering_kernel<T, 6><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
+    default: scattering_kernel<T, 7><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
+  }
+}
+
+template <typename T>
+void launch_source(T *phi_out, int64_t nmix, const int *mix_zone, const int *mix_mat, const double *mix_frac, int G,
+                   int M, double strength, cudaStream_t s) {
+  const int64_t n = nmix * G;
+  if (n == 0) return;
+  source_kernel<T><<<gridFor(n, 256), 256, 0, s>>>(phi_out, nmix, mix_zone, mix_mat, mix_frac, G, M, strength);
+}
+
+template void launch_scattering<double>(const double *, double *, const double *, const ScatterArgsBase &, bool, cudaStream_t);
+template void launch_scattering<float>(const float *, float *, const float *, const ScatterArgsBase &, bool, cudaStream_t);
+template void launch_source<double>(double *, int64_t, const int *, const int *, const double *, int, int, double, cudaStream_t);
+template void launch_source<float>(float *, int64_t, const int *, const int *, const double *, int, int, double, cudaStream_t);
+
+}  // namespace kgb

@@ -1,0 +1,191 @@
+"""GPU parity: every hot-path kernel through the C ABI against the CPU oracle.
+
+Inputs come from the oracle's generator (a restatement of Kripke's), are moved
+across the ABI in Kripke's chunked host layout, and the outputs are compared
+in the same layout.  Tolerances: the plain form is FP64 and must match to
+1e-12 relative (fused multiply-adds and sum order are the only differences);
+the mixed form is checked against the FP64 oracle at 1e-5 on single kernels
+and 1e-6 norm-wise on phi after a solve.
+"""
+import numpy as np
+import pytest
+
+from tests.nesting import LAYOUTS
+
+pytestmark = pytest.mark.gpu
+
+INPUTS = ("ell", "ell_plus", "sigt_zonal", "data/sigs", "quadrature/xcos", "quadrature/ycos", "quadrature/zcos",
+          "quadrature/w", "quadrature/id", "quadrature/jd", "quadrature/kd", "dx", "dy", "dz", "volume",
+          "zone_to_num_mixelem", "zone_to_mixelem", "mixelem_to_zone", "mixelem_to_material",
+          "mixelem_to_fraction", "moment_to_legendre")
+
+
+def pair(oracle, kgb, precision=0, **kw):
+    base = dict(zones=(6, 5, 7), groups=4, quad=16, legendre=2, gset=1, dset=8, niter=3)
+    base.update(kw)
+    p = oracle.Problem(**base)
+    ctx = kgb.Context(0)
+    ctx.setup_like(p.inp, precision=precision)
+    for n in INPUTS:
+        ctx.upload(n, p.get(n))
+    return p, ctx
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def maxrel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def check(a, b, tol):
+    assert rel(a, b) <= tol and maxrel(a, b) <= tol, (rel(a, b), maxrel(a, b))
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_field_roundtrip_all_layouts(oracle, kgb, layout):
+    p, ctx = pair(oracle, kgb, layout=layout, gset=2, dset=16, zsets=(2, 1, 1), zones=(6, 5, 4))
+    rng = np.random.default_rng(1)
+    for n in ("psi", "rhs", "phi", "phi_out", "i_plane", "j_plane", "k_plane", "sigt_zonal"):
+        x = rng.standard_normal(ctx.field_bytes(n) // 8)
+        ctx.upload(n, x)
+        np.testing.assert_array_equal(ctx.download(n), x, err_msg=n)
+    for n in INPUTS:
+        np.testing.assert_array_equal(ctx.download(n), p.get(n), err_msg=n)
+
+
+@pytest.mark.parametrize("layout", ["DGZ", "ZGD", "GZD"])
+def test_ltimes_lplustimes(oracle, kgb, layout):
+    p, ctx = pair(oracle, kgb, layout=layout, quad=(4, 8), legendre=4, gset=2, dset=8, zones=(5, 4, 6))
+    rng = np.random.default_rng(2)
+    psi = rng.standard_normal(ctx.field_bytes("psi") // 8)
+    p.set("psi", psi); ctx.upload("psi", psi)
+    p.kconst("phi", 0.0); ctx.fill("phi", 0.0)
+    p.ltimes(); ctx.ltimes()
+    check(ctx.download("phi"), p.get("phi"), 1e-13)
+    phi_out = rng.standard_normal(ctx.field_bytes("phi_out") // 8)
+    p.set("phi_out", phi_out); ctx.upload("phi_out", phi_out)
+    rhs0 = rng.standard_normal(ctx.field_bytes("rhs") // 8)
+    p.set("rhs", rhs0); ctx.upload("rhs", rhs0)  # accumulate semantics
+    p.lplustimes(); ctx.lplustimes()
+    check(ctx.download("rhs"), p.get("rhs"), 1e-13)
+
+
+@pytest.mark.parametrize("scatter,gset", [(0, 1), (1, 1), (1, 4)])
+def test_scattering_and_source(oracle, kgb, scatter, gset):
+    p, ctx = pair(oracle, kgb, scatter=scatter, gset=gset, groups=8, legendre=3, geometry=1, zones=(8, 6, 7))
+    rng = np.random.default_rng(3)
+    phi = rng.uniform(0.0, 1.0, ctx.field_bytes("phi") // 8)
+    p.set("phi", phi); ctx.upload("phi", phi)
+    p.kconst("phi_out", 0.0); ctx.fill("phi_out", 0.0)
+    p.scattering(); ctx.scattering()
+    check(ctx.download("phi_out"), p.get("phi_out"), 1e-13)
+    p.source(); ctx.source(1.0)
+    check(ctx.download("phi_out"), p.get("phi_out"), 1e-13)
+
+
+@pytest.mark.parametrize("zones,zsets,dset,layout", [
+    ((6, 5, 7), (1, 1, 1), 8, "DGZ"),
+    ((9, 4, 5), (1, 1, 1), 16, "ZDG"),
+    ((8, 6, 4), (2, 3, 2), 8, "GDZ"),
+    ((13, 11, 9), (1, 1, 1), 8, "DZG"),
+])
+def test_sweep_solver(oracle, kgb, zones, zsets, dset, layout):
+    p, ctx = pair(oracle, kgb, zones=zones, zsets=zsets, dset=dset, layout=layout, quad=(4, 8), groups=3)
+    rng = np.random.default_rng(4)
+    rhs = rng.uniform(0.0, 2.0, ctx.field_bytes("rhs") // 8)
+    p.set("rhs", rhs); ctx.upload("rhs", rhs)
+    p.sweep_solver(); ctx.sweep_solver()
+    check(ctx.download("psi"), p.get("psi"), 1e-12)
+    for n in ("i_plane", "j_plane", "k_plane"):
+        check(ctx.download(n), p.get(n), 1e-12)
+
+
+def test_sweep_subdomain_reads_incoming_planes(oracle, kgb):
+    p, ctx = pair(oracle, kgb, zones=(5, 6, 7), quad=16, groups=2)
+    rng = np.random.default_rng(5)
+    for n in ("rhs", "i_plane", "j_plane", "k_plane"):
+        x = rng.uniform(0.0, 1.0, ctx.field_bytes(n) // 8)
+        p.set(n, x); ctx.upload(n, x)
+    for s in (0, 3, 7):
+        p.sweep_subdomain(s); ctx.sweep_subdomain(s)
+    check(ctx.download("psi"), p.get("psi"), 1e-12)
+    check(ctx.download("k_plane"), p.get("k_plane"), 1e-12)
+
+
+@pytest.mark.parametrize("tz", [1, 3, 4, 16])
+def test_sweep_tile_depth(oracle, kgb, tz):
+    p, ctx = pair(oracle, kgb, zones=(7, 9, 10), quad=16, groups=2)
+    ctx.set_option("sweep_tile_z", tz)
+    rhs = np.random.default_rng(6).uniform(0.0, 1.0, ctx.field_bytes("rhs") // 8)
+    p.set("rhs", rhs); ctx.upload("rhs", rhs)
+    p.sweep_solver(); ctx.sweep_solver()
+    check(ctx.download("psi"), p.get("psi"), 1e-12)
+
+
+def test_population_and_balance(oracle, kgb):
+    p, ctx = pair(oracle, kgb, scatter=1, quad=(4, 8), zones=(8, 8, 8), geometry=1)
+    p.solve(2)
+    ctx.solve(2)
+    check(ctx.download("psi"), p.get("psi"), 1e-12)
+    assert ctx.population() == pytest.approx(p.population(), rel=1e-12)
+    gb, ob = ctx.balance(), p.balance()
+    for k in range(4):
+        assert gb[k] == pytest.approx(ob[k], rel=1e-12), k
+    assert abs(gb[4]) <= 1e-11 * gb[0]
+
+
+@pytest.mark.parametrize("quad", [96, (8, 12)])
+def test_solve_config0(oracle, kgb, quad):
+    """The 16^3 / 32-group / 96-direction / P4 / DGZ problem, 10 iterations."""
+    p, ctx = pair(oracle, kgb, zones=(16, 16, 16), groups=32, quad=quad, legendre=4, gset=1, dset=8, geometry=1,
+                  layout="DGZ")
+    want = p.solve(10)
+    got = ctx.solve(10)
+    np.testing.assert_allclose(got, want, rtol=1e-12)
+    ctx.fill("phi", 0.0); ctx.ltimes()
+    p.kconst("phi", 0.0); p.ltimes()
+    check(ctx.download("phi"), p.get("phi"), 1e-12)
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_solve_downscatter_all_layouts(oracle, kgb, layout):
+    """Config-1 physics (GL quadrature, seeded downscatter) at a size the oracle finishes quickly."""
+    p, ctx = pair(oracle, kgb, zones=(8, 8, 8), groups=16, quad=(4, 8), legendre=4, scatter=1, geometry=1,
+                  layout=layout)
+    want = p.solve(4)
+    got = ctx.solve(4)
+    np.testing.assert_allclose(got, want, rtol=1e-12)
+    check(ctx.download("psi"), p.get("psi"), 1e-12)
+    check(ctx.download("phi"), p.get("phi"), 1e-12)
+
+
+def test_mixed_precision_phi_error(oracle, kgb):
+    p, ctx = pair(oracle, kgb, precision=1, zones=(12, 12, 12), groups=16, quad=(4, 8), legendre=4, scatter=1,
+                  geometry=1)
+    want = p.solve(10)
+    got = ctx.solve(10)
+    np.testing.assert_allclose(got, want, rtol=1e-5)
+    assert rel(ctx.download("phi"), p.get("phi")) <= 1e-6
+
+
+def test_errors_are_reported(oracle, kgb):
+    ctx = kgb.Context(0)
+    with pytest.raises(kgb.KgbError) as e:
+        ctx.ltimes()
+    assert e.value.code == 6  # not set up
+    ctx.setup(4, 4, 4, 2, 16, 1)
+    with pytest.raises(kgb.KgbError) as e:
+        ctx.ltimes()
+    assert e.value.code == 6  # inputs missing
+    with pytest.raises(kgb.KgbError) as e:
+        ctx.upload("psi", np.zeros(3))
+    assert e.value.code == 1
+    with pytest.raises(kgb.KgbError) as e:
+        ctx.upload("no_such_field", np.zeros(3))
+    assert e.value.code == 1
+    with pytest.raises(kgb.KgbError):
+        ctx.setup(4, 4, 4, 3, 16, 1, gset=2)
