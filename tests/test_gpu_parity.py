@@ -48,13 +48,13 @@ def check(a, b, tol):
 @pytest.mark.parametrize("layout", LAYOUTS)
 def test_field_roundtrip_all_layouts(oracle, kgb, layout):
     p, ctx = pair(oracle, kgb, layout=layout, gset=2, dset=16, zsets=(2, 1, 1), zones=(6, 5, 4))
+    for n in INPUTS:
+        np.testing.assert_array_equal(ctx.download(n), p.get(n), err_msg=n)
     rng = np.random.default_rng(1)
     for n in ("psi", "rhs", "phi", "phi_out", "i_plane", "j_plane", "k_plane", "sigt_zonal"):
         x = rng.standard_normal(ctx.field_bytes(n) // 8)
         ctx.upload(n, x)
         np.testing.assert_array_equal(ctx.download(n), x, err_msg=n)
-    for n in INPUTS:
-        np.testing.assert_array_equal(ctx.download(n), p.get(n), err_msg=n)
 
 
 @pytest.mark.parametrize("layout", ["DGZ", "ZGD", "GZD"])
@@ -170,6 +170,22 @@ def test_mixed_precision_phi_error(oracle, kgb):
     got = ctx.solve(10)
     np.testing.assert_allclose(got, want, rtol=1e-5)
     assert rel(ctx.download("phi"), p.get("phi")) <= 1e-6
+
+
+@pytest.mark.parametrize("kw", [
+    dict(zones=(16, 16, 16), groups=32, quad=96, legendre=4, geometry=1),
+    dict(zones=(12, 10, 8), groups=16, quad=(8, 12), legendre=4, scatter=1, geometry=1, layout="GZD"),
+    dict(zones=(8, 6, 10), groups=8, quad=(4, 8), legendre=3, scatter=1, perturb=1, geometry=0, gset=2,
+         zsets=(2, 3, 1), layout="ZDG"),
+    dict(zones=(6, 6, 6), groups=6, quad=32, legendre=2, perturb=1, dset=16, layout="DZG"),
+])
+def test_generator_matches_oracle(oracle, kgb, kw):
+    """kgb_generate reproduces the oracle's restatement of Kripke's generator bit for bit."""
+    p = oracle.Problem(**kw)
+    ctx = kgb.Context(0)
+    ctx.generate(**kw)
+    for n in INPUTS:
+        np.testing.assert_array_equal(ctx.download(n), p.get(n), err_msg=n)
 
 
 def test_errors_are_reported(oracle, kgb):
