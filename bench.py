@@ -177,6 +177,8 @@ def run_gpu(args, world, rank, local):
     torch.cuda.set_device(local)
     precision = abi.MIXED if args.precision == "mixed" else abi.FP64
     w = dict(WORKLOAD)
+    if args.zones:
+        w["zones"] = (args.zones, args.zones, args.zones)
     ctx = abi.Context(local)
     inp = ctx.generate(precision=precision, **w)
     stream = torch.cuda.Stream(device=local)
@@ -224,6 +226,8 @@ def run_gpu(args, world, rank, local):
                          "dy", "dz", "volume", "zone_to_num_mixelem", "zone_to_mixelem", "mixelem_to_zone",
                          "mixelem_to_material", "mixelem_to_fraction", "moment_to_legendre")]
     host = {}
+    if args.no_e2e:
+        names = []
     for n in names:
         a = ctx.download(n)
         pinned = torch.empty(a.size, dtype=torch.int32 if a.dtype == np.int32 else torch.float64).pin_memory()
@@ -232,14 +236,14 @@ def run_gpu(args, world, rank, local):
     h2d = sum(t.numel() * t.element_size() for t in host.values())
     niter = 10
     e2e_times = []
-    for rep in range(2):
+    for rep in range(2 if names else 0):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for n in names:
             ctx.upload(n, host[n].numpy())
         ctx.solve(niter)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_value = U * niter / e2e_times[-1] * world
+    e2e_value = U * niter / e2e_times[-1] * world if e2e_times else None
 
     # roofline of the dominant kernel family
     pk = peaks()
@@ -273,7 +277,8 @@ def run_gpu(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if precision == abi.FP64 else "f32 (FP64 reductions)",
         "data": "synthetic (seeded generator, no external data)",
-        "config": {"workload": WORKLOAD_NAME, "precision": args.precision, "unknowns": U,
+        "config": {"workload": WORKLOAD_NAME if not args.zones else WORKLOAD_NAME.replace("64^3", "%d^3" % args.zones),
+                   "precision": args.precision, "unknowns": U,
                    "l2": "inputs larger than L2 (psi, rhs 17.2 GB each); no flush",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "roofline": roof,
@@ -303,6 +308,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--zones", type=int, default=0, help="override zones per axis (profiling on a smaller case)")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":
