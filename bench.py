@@ -36,7 +36,18 @@ WORKLOAD = dict(zones=(64, 64, 64), groups=64, quad=(8, 16), legendre=4, gset=1,
 WORKLOAD_NAME = "kripke 64^3 zones x 64 groups x 128 GL directions, P4, cube100, downscatter, DGZ, dset 8"
 # bounded CPU sample: same physics and per-zone work, 32^3 zones (1/8 of the unknowns)
 CPU_SAMPLE = dict(WORKLOAD, zones=(32, 32, 32))
-FP64_PEAK_GFLOPS = 1196.0  # measured DFMA rate on this machine's GB300 (profiles/fp64_peak_gb300.md)
+FP64_PEAK_GFLOPS = 1196.0  # DFMA rate measured on this machine's GB300 (profiles/fp64_peak_gb300.md)
+
+
+def fp64_peak():
+    """FP64 FMA rate of this GPU from kripke_gb300/bin/peak_probe; the recorded figure if it cannot run."""
+    probe = os.path.join(ROOT, "kripke_gb300", "bin", "peak_probe")
+    try:
+        out = subprocess.run([probe], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=60)
+        v = json.loads(out.stdout.strip().splitlines()[-1])["fp64_fma_gflops"]
+        return float(v), "measured live by kripke_gb300/bin/peak_probe (MEASURED_PEAKS.json has no FP64 figure)"
+    except Exception:
+        return FP64_PEAK_GFLOPS, "recorded probe figure (profiles/fp64_peak_gb300.md)"
 
 
 def unknowns(w):
@@ -256,9 +267,9 @@ def run_gpu(args, world, rank, local):
     flops, nbytes = alg[dom]["flops"], alg[dom]["bytes"]
     if precision == abi.FP64:
         achieved = flops / (dom_ms * 1e-3) / 1e9
-        roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s",
-                "frac": achieved / FP64_PEAK_GFLOPS, "traffic": None, "kernel": dom,
-                "peak_source": "measured FP64 FMA rate (MEASURED_PEAKS.json has no FP64 figure)",
+        p64, p64_src = fp64_peak()
+        roof = {"bound": "fp64", "achieved": achieved, "peak": p64, "unit": "GFLOP/s",
+                "frac": achieved / p64, "traffic": None, "kernel": dom, "peak_source": p64_src,
                 "hbm": {"achieved": nbytes / (dom_ms * 1e-3) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
                         "frac": nbytes / (dom_ms * 1e-3) / 1e9 / pk["hbm_gbs"]}}
     else:

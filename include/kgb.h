@@ -182,6 +182,7 @@ int kgb_reset_timers(kgb_ctx *ctx);
 /* Number of kernels this context has launched since it was created. */
 int kgb_launch_count(kgb_ctx *ctx, int64_t *out);
 
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,6 +22,7 @@ LIBDIR = os.path.join(HERE, "lib")
 BINDIR = os.path.join(HERE, "bin")
 LIB = os.path.join(LIBDIR, "libkgb.so")
 CLI = os.path.join(BINDIR, "kripke")
+PROBE = os.path.join(BINDIR, "peak_probe")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
@@ -88,6 +89,10 @@ def build(force=False, verbose=False):
                 print(o)
     if force or jobs or _stale(LIB, objs):
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    os.makedirs(BINDIR, exist_ok=True)
+    probe_src = os.path.join(CSRC, "tools", "peak_probe.cu")
+    if force or _stale(PROBE, [probe_src]):
+        _run([nvcc] + ARCH + ["-O3", "-std=c++17", "-o", PROBE, probe_src])
     host = _host_sources()
     if host:
         os.makedirs(BINDIR, exist_ok=True)
