@@ -182,6 +182,22 @@ int kgb_reset_timers(kgb_ctx *ctx);
 /* Number of kernels this context has launched since it was created. */
 int kgb_launch_count(kgb_ctx *ctx, int64_t *out);
 
+/* Allocation-free population edit.  No counterpart in the reference: it
+ * exists for callers that cannot allocate device memory at the point they
+ * need the particle count -- code recorded into a CUDA graph, frameworks that
+ * own all device memory through their own pool, latency-bound loops.  Same
+ * sum as kgb_population, over caller-owned device arrays: psi in the device
+ * nesting [zone][group][direction] (FP64), w [directions], volume [zones];
+ * *out (device memory) receives the FP64 result.  Allocates nothing: its
+ * scratch is a static 128 KiB device array, which limits zones*groups to
+ * 33,554,432 rows (larger sizes return KGB_ERR_ARG).  Launches on `stream`
+ * (a cudaStream_t, NULL = legacy default stream) on the current device; the
+ * first call on each device looks up the scratch address and should come
+ * before any stream capture.  Calls share the scratch: calls that overlap on
+ * the GPU race.  err/err_len (optional) receive a message on failure. */
+int kgb_population_noalloc(const double *psi, const double *w, const double *volume, int64_t zones,
+                           int32_t groups, int32_t directions, double *out, void *stream, char *err,
+                           int32_t err_len);
 
 #ifdef __cplusplus
 }

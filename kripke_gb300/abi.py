@@ -25,7 +25,7 @@ EXPORTS = (
     "kgb_lplustimes", "kgb_scattering", "kgb_source", "kgb_sweep_subdomain", "kgb_sweep_solver",
     "kgb_population", "kgb_balance", "kgb_solve", "kgb_iterate", "kgb_sync", "kgb_set_stream",
     "kgb_set_option", "kgb_set_timing", "kgb_kernel_time", "kgb_reset_timers", "kgb_default_input",
-    "kgb_generate", "kgb_launch_count",
+    "kgb_generate", "kgb_launch_count", "kgb_population_noalloc",
 )
 
 INT_FIELDS = ("quadrature/id", "quadrature/jd", "quadrature/kd", "zone_to_mixelem", "zone_to_num_mixelem",
@@ -143,6 +143,8 @@ def load():
         "kgb_default_input": ([ctypes.POINTER(KgbInput)], None),
         "kgb_generate": ([P, ctypes.POINTER(KgbInput)], I),
         "kgb_launch_count": ([P, ctypes.POINTER(I64)], I),
+        "kgb_population_noalloc": ([P, P, P, I64, ctypes.c_int32, ctypes.c_int32, P, P, ctypes.c_char_p,
+                                    ctypes.c_int32], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
