@@ -171,8 +171,16 @@ int kgb_sync(kgb_ctx *ctx);
 /* Run on a caller-owned CUDA stream (a cudaStream_t passed as a pointer)
  * instead of the context's own; NULL restores the context's stream. */
 int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
-/* Tuning knobs: "sweep_tile_z" (tile depth in k, default 4). */
+/* Tuning knobs: "sweep_tile_z" (tile depth in k, default 4); "sweep_tile_xy"
+ * (tile footprint in i and j: 44, 42 or 22, default 44); "sweep_reciprocals"
+ * (FP64 on a uniform mesh: 1 = tabulate 1/denominator per (sigt value,
+ * direction), the default; 0 = divide in every cell). */
 int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
+/* Sweep autotuner: times every tile shape (footprint 4x4, 4x2, 2x2 x depth
+ * 2, 4, 8, 16 zones) on this problem with CUDA events, keeps the fastest and
+ * returns its sweep time (best_ms), footprint (as 44/42/22) and depth.  It
+ * sweeps the current rhs, so psi and the planes are overwritten. */
+int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_z);
 /* Device time in milliseconds of the named kernel family accumulated since the
  * last reset ("sweep", "ltimes", "lplustimes", "scattering", "population");
  * timing is off unless kgb_set_timing(ctx, 1). */

@@ -25,7 +25,7 @@ EXPORTS = (
     "kgb_lplustimes", "kgb_scattering", "kgb_source", "kgb_sweep_subdomain", "kgb_sweep_solver",
     "kgb_population", "kgb_balance", "kgb_solve", "kgb_iterate", "kgb_sync", "kgb_set_stream",
     "kgb_set_option", "kgb_set_timing", "kgb_kernel_time", "kgb_reset_timers", "kgb_default_input",
-    "kgb_generate", "kgb_launch_count", "kgb_population_noalloc",
+    "kgb_generate", "kgb_launch_count", "kgb_population_noalloc", "kgb_autotune",
 )
 
 INT_FIELDS = ("quadrature/id", "quadrature/jd", "quadrature/kd", "zone_to_mixelem", "zone_to_num_mixelem",
@@ -143,6 +143,7 @@ def load():
         "kgb_default_input": ([ctypes.POINTER(KgbInput)], None),
         "kgb_generate": ([P, ctypes.POINTER(KgbInput)], I),
         "kgb_launch_count": ([P, ctypes.POINTER(I64)], I),
+        "kgb_autotune": ([P, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], I),
         "kgb_population_noalloc": ([P, P, P, I64, ctypes.c_int32, ctypes.c_int32, P, P, ctypes.c_char_p,
                                     ctypes.c_int32], I),
     }
@@ -295,6 +296,13 @@ class Context:
         self._check(self.lib.kgb_kernel_time(self.h, family.encode(), ctypes.byref(ms), ctypes.byref(n)),
                     "kgb_kernel_time")
         return ms.value, n.value
+
+    def autotune(self):
+        """Pick the fastest sweep tile shape for this problem (overwrites psi and the planes)."""
+        ms, xy, tz = ctypes.c_double(), ctypes.c_int32(), ctypes.c_int32()
+        self._check(self.lib.kgb_autotune(self.h, ctypes.byref(ms), ctypes.byref(xy), ctypes.byref(tz)),
+                    "kgb_autotune")
+        return {"sweep_ms": ms.value, "sweep_tile_xy": xy.value, "sweep_tile_z": tz.value}
 
     def launch_count(self):
         n = ctypes.c_int64()

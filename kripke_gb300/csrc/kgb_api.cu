@@ -89,6 +89,7 @@ struct kgb_ctx {
   int prec = KGB_FP64;
   size_t tsz = 8;
   int tz = 4;
+  int tx = 4, ty = 4;  // sweep tile footprint
 
   // device state (element type T = double or float by precision)
   void *psi = nullptr, *rhs = nullptr, *phi = nullptr, *phi_out = nullptr, *sigt = nullptr;
@@ -135,6 +136,18 @@ struct kgb_ctx {
   bool timing = false;
   std::map<std::string, TimerFam> fams;
   int64_t launches = 0;  // kernels launched by this context
+
+  // tabulated sweep reciprocals (FP64, uniform mesh)
+  bool dirty_sigt = true;
+  bool use_recip = false;
+  bool allow_recip = true;
+  uint16_t *cls_d = nullptr;
+  double *inv_d = nullptr;
+  int64_t ncls = 0;
+  // fused population partials, one per (tile, subdomain, chain block)
+  double *pop_slots = nullptr;
+  int64_t npop_slots = 0;
+  double vol_uniform = 0.0;
 };
 
 namespace {
@@ -318,7 +331,7 @@ void freeAll(kgb_ctx *c) {
                   c->sigsT, c->cx, c->cy, c->cz, c->w_d, c->cos_d[0], c->cos_d[1], c->cos_d[2], c->vol_d,
                   c->dxyz_d[0], c->dxyz_d[1], c->dxyz_d[2], c->zmix_start, c->zmix_count, c->mix_mat, c->mix_zone,
                   c->mix_frac, c->gp_lo, c->gp_hi, c->sdoms_d, c->ident_d, c->levels_d, c->tiles_d, c->partials,
-                  c->results, c->parts_dev, c->staging};
+                  c->results, c->parts_dev, c->staging, c->cls_d, c->inv_d, c->pop_slots};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->psi = c->rhs = c->phi = c->phi_out = c->sigt = nullptr;
@@ -333,6 +346,11 @@ void freeAll(kgb_ctx *c) {
   c->ident_d = c->levels_d = nullptr;
   c->tiles_d = nullptr;
   c->partials = c->results = c->parts_dev = c->staging = nullptr;
+  c->cls_d = nullptr;
+  c->inv_d = nullptr;
+  c->pop_slots = nullptr;
+  c->npop_slots = 0;
+  c->use_recip = false;
   c->staging_bytes = 0;
   c->nmix_cap = 0;
   c->parts_cap = 0;
@@ -378,6 +396,52 @@ int need(kgb_ctx *ctx, std::initializer_list<const char *> names) {
     const FieldInfo *f = findField(n);
     if (!ctx->have[fieldIndex(f)]) return fail(ctx, KGB_ERR_STATE, std::string("input field '") + n + "' has not been uploaded");
   }
+  return KGB_OK;
+}
+
+// Tabulated sweep reciprocals (FP64 only).  On a uniform mesh the per-cell
+// denominator ((2mu/dx + 2eta/dy) + 2xi/dz) + sigt depends on the direction and
+// on the zone's sigt value alone; the distinct sigt values are few (mixtures of
+// three materials), so 1/den is tabulated per (class, direction) and each
+// (zone, group) stores its class.  Falls back to a per-cell divide when the mesh
+// is not uniform or the classes do not fit 16 bits.
+int buildReciprocals(kgb_ctx *ctx) {
+  ctx->use_recip = false;
+  if (ctx->prec != KGB_FP64 || !ctx->allow_recip) return KGB_OK;
+  for (int k = 0; k < 3; ++k)
+    for (double v : ctx->dxyz[k])
+      if (v != ctx->dxyz[k][0]) return KGB_OK;
+  const int64_t n = ctx->Z * ctx->G;
+  std::vector<double> sig(n);
+  CK(cudaMemcpyAsync(sig.data(), ctx->sigt, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::vector<double> uniq(sig);
+  std::sort(uniq.begin(), uniq.end());
+  uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+  const int64_t ncls = (int64_t)uniq.size();
+  if (ncls > 65535 || ncls * ctx->D > (int64_t)16 << 20) return KGB_OK;
+  std::vector<uint16_t> cls(n);
+  for (int64_t e = 0; e < n; ++e)
+    cls[e] = (uint16_t)(std::lower_bound(uniq.begin(), uniq.end(), sig[e]) - uniq.begin());
+  std::vector<double> inv((size_t)ncls * ctx->D);
+  for (int64_t c = 0; c < ncls; ++c)
+    for (int d = 0; d < ctx->D; ++d) {
+      const double cx = 2.0 * ctx->q[0][d] / ctx->dxyz[0][0];
+      const double cy = 2.0 * ctx->q[1][d] / ctx->dxyz[1][0];
+      const double cz = 2.0 * ctx->q[2][d] / ctx->dxyz[2][0];
+      inv[(size_t)c * ctx->D + d] = 1.0 / (cx + cy + cz + uniq[c]);
+    }
+  if (ctx->cls_d) cudaFree(ctx->cls_d);
+  if (ctx->inv_d) cudaFree(ctx->inv_d);
+  ctx->cls_d = nullptr;
+  ctx->inv_d = nullptr;
+  int rc;
+  if ((rc = dmalloc(ctx, &ctx->cls_d, n)) || (rc = dmalloc(ctx, &ctx->inv_d, inv.size()))) return rc;
+  CK(cudaMemcpyAsync(ctx->cls_d, cls.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->inv_d, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->ncls = ncls;
+  ctx->use_recip = true;
   return KGB_OK;
 }
 
@@ -443,6 +507,7 @@ int prepareT(kgb_ctx *ctx) {
     }
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_geom = false;
+    ctx->dirty_sigt = true;  // the tabulated reciprocals depend on 2*cos/delta
   }
   if (ctx->dirty_ell) {
     if ((rc = need(ctx, {"ell", "ell_plus"}))) return rc;
@@ -476,6 +541,9 @@ int prepareT(kgb_ctx *ctx) {
     if ((rc = need(ctx, {"volume"}))) return rc;
     CK(cudaMemcpyAsync(ctx->vol_d, ctx->vol_h.data(), ctx->Z * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    ctx->vol_uniform = ctx->vol_h[0];
+    for (double v : ctx->vol_h)
+      if (v != ctx->vol_uniform || !(v > 0.0)) { ctx->vol_uniform = 0.0; break; }
     ctx->dirty_vol = false;
   }
   if (ctx->dirty_mix) {
@@ -532,6 +600,11 @@ int prepareT(kgb_ctx *ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_mix = false;
   }
+  if (ctx->dirty_sigt) {
+    if ((rc = need(ctx, {"sigt_zonal"}))) return rc;
+    if ((rc = buildReciprocals(ctx))) return rc;
+    ctx->dirty_sigt = false;
+  }
   return KGB_OK;
 }
 
@@ -543,8 +616,8 @@ int prepare(kgb_ctx *ctx) {
 }
 
 int buildTiles(kgb_ctx *ctx) {
-  const int ntx = (ctx->nxs + kTileX - 1) / kTileX;
-  const int nty = (ctx->nys + kTileY - 1) / kTileY;
+  const int ntx = (ctx->nxs + ctx->tx - 1) / ctx->tx;
+  const int nty = (ctx->nys + ctx->ty - 1) / ctx->ty;
   const int ntz = (ctx->nzs + ctx->tz - 1) / ctx->tz;
   ctx->nsteps = ntx + nty + ntz - 2;
   std::vector<int4> tiles;
@@ -561,6 +634,12 @@ int buildTiles(kgb_ctx *ctx) {
   ctx->tiles_d = nullptr;
   int rc = dmalloc(ctx, &ctx->tiles_d, tiles.size());
   if (rc) return rc;
+  const int64_t nchain = (int64_t)ctx->Gs * ctx->Ds;
+  const int64_t nslots = (int64_t)tiles.size() * ctx->dc.num() * ((nchain + kSweepThreads - 1) / kSweepThreads);
+  if (ctx->pop_slots) cudaFree(ctx->pop_slots);
+  ctx->pop_slots = nullptr;
+  if ((rc = dmalloc(ctx, &ctx->pop_slots, nslots))) return rc;
+  ctx->npop_slots = nslots;
   CK(cudaMemcpyAsync(ctx->tiles_d, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return KGB_OK;
@@ -570,7 +649,7 @@ int buildTiles(kgb_ctx *ctx) {
 // Kernel drivers
 // ---------------------------------------------------------------------------
 template <typename T>
-int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave) {
+int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop) {
   SweepArgs<T> a{};
   a.rhs = as<T>(ctx->rhs);
   a.psi = as<T>(ctx->psi);
@@ -588,6 +667,19 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave) {
   a.G = ctx->G; a.D = ctx->D; a.Gs = ctx->Gs; a.Ds = ctx->Ds;
   a.nxs = ctx->nxs; a.nys = ctx->nys; a.nzs = ctx->nzs;
   a.tz = ctx->tz;
+  a.tx = ctx->tx;
+  a.ty = ctx->ty;
+  if (ctx->use_recip) {
+    a.cls = ctx->cls_d;
+    a.inv = ctx->inv_d;
+  }
+  if (fused_pop) {
+    a.pop = ctx->pop_slots;
+    a.nsdom = ctx->dc.num();
+    a.w = ctx->w_d;
+    a.vol = ctx->vol_d;
+    a.vol_uniform = ctx->vol_uniform;
+  }
   FamScope fs(ctx, "sweep");
   for (int s = 0; s < ctx->nsteps; ++s) {
     a.tile_off = ctx->tile_off[s];
@@ -599,8 +691,9 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave) {
   return KGB_OK;
 }
 
-int sweepWaveAny(kgb_ctx *ctx, const int *wave_dev, int nwave) {
-  return ctx->prec == KGB_FP64 ? sweepWave<double>(ctx, wave_dev, nwave) : sweepWave<float>(ctx, wave_dev, nwave);
+int sweepWaveAny(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop = false) {
+  return ctx->prec == KGB_FP64 ? sweepWave<double>(ctx, wave_dev, nwave, fused_pop)
+                               : sweepWave<float>(ctx, wave_dev, nwave, fused_pop);
 }
 
 int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
@@ -619,14 +712,14 @@ int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
   return KGB_OK;
 }
 
-int sweepSolver(kgb_ctx *ctx) {
+int sweepSolver(kgb_ctx *ctx, bool fused_pop = false) {
   for (int k = 0; k < 3; ++k) CK(cudaMemsetAsync(ctx->plane[k], 0, ctx->plane_chunk[k] * ctx->dc.num() * ctx->tsz, ctx->stream));
   const int nlev = (int)ctx->level_off.size() - 1;
   const int S[3] = {ctx->dc.Sx, ctx->dc.Sy, ctx->dc.Sz};
   for (int lv = 0; lv < nlev; ++lv) {
     const int b = ctx->level_off[lv], e = ctx->level_off[lv + 1];
     if (e == b) continue;
-    int rc = sweepWaveAny(ctx, ctx->levels_d + b, e - b);
+    int rc = sweepWaveAny(ctx, ctx->levels_d + b, e - b, fused_pop);
     if (rc) return rc;
     // hand the outgoing planes to downwind zone sets (ParallelComm.cpp:146-162)
     for (int x = b; x < e; ++x) {
@@ -728,8 +821,12 @@ int iterateDevice(kgb_ctx *ctx, double q, double *part_slot) {
   if ((rc = doScattering(ctx, false))) return rc;      // phi_out = S phi    (kConst + scattering)
   if ((rc = doSource(ctx, q))) return rc;              // phi_out += Q
   if ((rc = doLPlusTimes(ctx, false))) return rc;      // rhs = L+ phi_out   (kConst + LPlusTimes)
-  if ((rc = sweepSolver(ctx))) return rc;              // psi = H^-1 rhs
-  if (part_slot && (rc = doPopulation(ctx, part_slot))) return rc;
+  if ((rc = sweepSolver(ctx, part_slot != nullptr))) return rc;  // psi = H^-1 rhs (+ population partials)
+  if (part_slot) {
+    FamScope fs(ctx, "population");
+    launch_sum_partials(ctx->pop_slots, ctx->npop_slots, part_slot, ctx->stream);
+    CKN(1);
+  }
   return KGB_OK;
 }
 
@@ -930,6 +1027,7 @@ int kgb_field_upload(kgb_ctx *ctx, const char *name, const void *host, int64_t n
     }
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->have[fieldIndex(f)] = true;
+    if (f->kind == K_SIGT) ctx->dirty_sigt = true;
     return KGB_OK;
   }
   // host-side inputs: convert the chunks into global host tables
@@ -1280,7 +1378,67 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     if (ctx->ready) return buildTiles(ctx);
     return KGB_OK;
   }
+  if (!std::strcmp(key, "sweep_tile_xy")) {
+    if (value != 44 && value != 42 && value != 22) return fail(ctx, KGB_ERR_ARG, "sweep_tile_xy must be 44, 42 or 22");
+    ctx->tx = (int)(value / 10);
+    ctx->ty = (int)(value % 10);
+    if (ctx->ready) return buildTiles(ctx);
+    return KGB_OK;
+  }
+  if (!std::strcmp(key, "sweep_reciprocals")) {
+    ctx->allow_recip = value != 0;
+    ctx->dirty_sigt = true;
+    return KGB_OK;
+  }
   return fail(ctx, KGB_ERR_ARG, std::string("unknown option '") + key + "'");
+}
+
+int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_z) {
+  int rc = prepare(ctx);
+  if (rc) return rc;
+  const int xys[3] = {44, 42, 22};
+  const int tzs[4] = {2, 4, 8, 16};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const bool timing = ctx->timing;
+  ctx->timing = false;
+  float best = 1e30f;
+  int bxy = 44, btz = 4;
+  for (int xy : xys)
+    for (int tz : tzs) {
+      if (tz > 2 * ctx->nzs && tz != 2) continue;
+      ctx->tx = xy / 10;
+      ctx->ty = xy % 10;
+      ctx->tz = tz;
+      if ((rc = buildTiles(ctx))) break;
+      if ((rc = sweepSolver(ctx, true))) break;  // warm-up
+      CK(cudaEventRecord(e0, ctx->stream));
+      for (int r = 0; r < 2; ++r)
+        if ((rc = sweepSolver(ctx, true))) break;
+      CK(cudaEventRecord(e1, ctx->stream));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      ms *= 0.5f;
+      if (ms < best) {
+        best = ms;
+        bxy = xy;
+        btz = tz;
+      }
+    }
+  ctx->timing = timing;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  ctx->tx = bxy / 10;
+  ctx->ty = bxy % 10;
+  ctx->tz = btz;
+  if ((rc = buildTiles(ctx))) return rc;
+  if (best_ms) *best_ms = best;
+  if (tile_xy) *tile_xy = bxy;
+  if (tile_z) *tile_z = btz;
+  return KGB_OK;
 }
 
 int kgb_set_timing(kgb_ctx *ctx, int on) {

@@ -44,11 +44,20 @@ struct SweepArgs {
   int tile_off;               // first tile of this step
   int nx, ny, nz, G, D, Gs, Ds, nxs, nys, nzs;
   int tz;                     // tile depth in k
+  int tx, ty;                 // tile footprint in i and j: 4x4, 4x2 or 2x2
+  // tabulated reciprocals (uniform mesh): 1/((cx+cy+cz)[d] + sigt) per (sigt class, direction)
+  const uint16_t *cls;        // [Z][G] class of sigt_zonal, or null: divide per cell
+  const double *inv;          // [nclass][D]
+  // fused population: per-block partial sums of w(d)*psi*volume(z), or null
+  double *pop;                // slot = ((tile index)*nsdom + sdom)*gridDim.x + blockIdx.x
+  int nsdom;
+  const double *w;            // [D]
+  const double *vol;          // [Z]; unused when vol_uniform > 0
+  double vol_uniform;
 };
 
-// Sweep tile footprint in i and j (compile-time); depth in k is runtime.
-constexpr int kTileX = 4;
-constexpr int kTileY = 4;
+// Sweep tiles: footprint in i and j is a compile-time instance (4x4, 4x2 or
+// 2x2), depth in k is runtime.
 constexpr int kSweepThreads = 128;
 
 template <typename T>
@@ -85,6 +94,9 @@ template <typename T>
 void launch_leakage(const T *plane, int64_t nelem, int Gs, int Ds, int dlo, int na, const double *w,
                     const double *cosv, const double *wa, const double *wb, double *partials, int nblocks,
                     double *out, cudaStream_t s);
+
+// One block sums n partials in a fixed order into *out.
+void launch_sum_partials(const double *partials, int64_t n, double *out, cudaStream_t s);
 
 // Layout transfer between a host-nested chunk and the device nesting.
 struct XposeDesc {

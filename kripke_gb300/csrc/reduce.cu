@@ -122,6 +122,10 @@ void launch_leakage(const T *plane, int64_t nelem, int Gs, int Ds, int dlo, int 
   finish_kernel<<<1, kRedThreads, 0, s>>>(partials, nblocks, 1, 0, out, true);
 }
 
+void launch_sum_partials(const double *partials, int64_t n, double *out, cudaStream_t s) {
+  finish_kernel<<<1, kRedThreads, 0, s>>>(partials, (int)n, 1, 0, out, false);
+}
+
 template void launch_population<double>(const double *, const double *, const double *, int64_t, int, int, double *, int, double *, cudaStream_t);
 template void launch_population<float>(const float *, const double *, const double *, int64_t, int, int, double *, int, double *, cudaStream_t);
 template void launch_balance_terms<double>(const double *, const double *, const double *, const double *, const double *, int64_t, int, int, double *, int, double *, cudaStream_t);

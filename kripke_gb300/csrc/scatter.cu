@@ -3,12 +3,13 @@
 // Replaces Kernel::scattering (src/Kripke/Kernel/Scattering.cpp:59-100,
 // 137-145) and Kernel::source (src/Kripke/Kernel/Source.cpp:57-76).
 //   phi_out(nm,g,z) += sum_g' [sum_mix f * sigs(mat, l(nm), g, g')] * phi(nm,g',z)
-// One thread owns a (zone, destination group) row and loops over Legendre
-// orders l; the 2l+1 moments of order l share one coefficient per source
-// group.  The coefficient is built exactly as the reference does (sum over the
-// zone's mix elements of sigs*fraction, starting from 0).  Source groups are
-// visited in ascending order and only over the range where any material's
-// matrix row is nonzero (adding an exact zero term leaves the sum unchanged).
+// One thread owns a (zone, destination group) row and keeps all (L+1)^2 moment
+// sums in registers; for each source group it forms the L+1 coefficients
+// (one per Legendre order, shared by the 2l+1 moments of that order) exactly
+// as the reference does -- the sum over the zone's mix elements of
+// sigs*fraction, from 0 -- and applies them.  Source groups are visited in
+// ascending order and only over the range where any material's matrix row is
+// nonzero (adding an exact zero term leaves the sum unchanged).
 // sigs is stored transposed, [mat][l][g'][g], so a warp's coefficient loads
 // are contiguous.
 #include "kgb_internal.h"
@@ -18,39 +19,54 @@ namespace kgb {
 namespace {
 constexpr int kScatThreads = 128;
 
+__host__ __device__ constexpr int legendreOf(int m) {
+  int l = 0;
+  while ((l + 1) * (l + 1) <= m) ++l;
+  return l;
+}
+
 template <typename T, int LMAX>
 __global__ void __launch_bounds__(kScatThreads) scattering_kernel(const T *__restrict__ phi, T *__restrict__ phi_out,
                                                                  const T *__restrict__ sigsT, const ScatterArgsBase a,
                                                                  bool accumulate) {
+  constexpr int MM = (LMAX + 1) * (LMAX + 1);
   const int Gd = a.dst_ghi - a.dst_glo;
   const int64_t rows = a.Z * Gd;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
     const int64_t z = r / Gd;
     const int g = a.dst_glo + (int)(r - z * Gd);
     const int ms = a.zmix_start[z], mcnt = a.zmix_count[z];
+    // a single-material zone has fraction exactly 1, where the reference's
+    // 0 + sigs*fraction is sigs itself
+    const bool pure = mcnt == 1 && a.mix_frac[ms] == 1.0;
+    const int mat0 = a.mix_mat[ms];
     const int lo = max(a.gp_lo[g], a.src_glo);
     const int hi = min(a.gp_hi[g] + 1, a.src_ghi);
-    for (int l = 0; l <= a.L; ++l) {
-      const int mb = l * l, na = 2 * l + 1;
-      T acc[2 * LMAX + 1];
+    T acc[MM];
 #pragma unroll
-      for (int x = 0; x < 2 * LMAX + 1; ++x) acc[x] = T(0);
-      for (int gp = lo; gp < hi; ++gp) {
-        T s = T(0);
+    for (int m = 0; m < MM; ++m) acc[m] = T(0);
+    for (int gp = lo; gp < hi; ++gp) {
+      T sl[LMAX + 1];
+      if (pure) {
+#pragma unroll
+        for (int l = 0; l <= LMAX; ++l) sl[l] = sigsT[(((int64_t)mat0 * (LMAX + 1) + l) * a.G + gp) * a.G + g];
+      } else {
+#pragma unroll
+        for (int l = 0; l <= LMAX; ++l) sl[l] = T(0);
         for (int x = 0; x < mcnt; ++x) {
           const int mat = a.mix_mat[ms + x];
-          s += sigsT[(((int64_t)mat * (a.L + 1) + l) * a.G + gp) * a.G + g] * (T)a.mix_frac[ms + x];
+          const T f = (T)a.mix_frac[ms + x];
+#pragma unroll
+          for (int l = 0; l <= LMAX; ++l) sl[l] += sigsT[(((int64_t)mat * (LMAX + 1) + l) * a.G + gp) * a.G + g] * f;
         }
-        const T *ph = phi + (z * a.G + gp) * a.M + mb;
-#pragma unroll
-        for (int x = 0; x < 2 * LMAX + 1; ++x)
-          if (x < na) acc[x] += s * ph[x];
       }
-      T *o = phi_out + (z * a.G + g) * a.M + mb;
+      const T *ph = phi + (z * a.G + gp) * MM;
 #pragma unroll
-      for (int x = 0; x < 2 * LMAX + 1; ++x)
-        if (x < na) o[x] = accumulate ? o[x] + acc[x] : acc[x];
+      for (int m = 0; m < MM; ++m) acc[m] += sl[legendreOf(m)] * ph[m];
     }
+    T *o = phi_out + (z * a.G + g) * MM;
+#pragma unroll
+    for (int m = 0; m < MM; ++m) o[m] = accumulate ? o[m] + acc[m] : acc[m];
   }
 }
 

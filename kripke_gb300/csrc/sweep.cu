@@ -7,7 +7,7 @@
 //   psi_lf = 2 psi - psi_lf, psi_fr = 2 psi - psi_fr, psi_bo = 2 psi - psi_bo
 // evaluated with the reference's association ((rhs + a)+b)+c and ((x+y)+z)+s.
 //
-// Schedule: a subdomain's zone set is cut into tiles of kTileX x kTileY x tz
+// Schedule: a subdomain's zone set is cut into tiles of tx x ty x tz
 // zones.  In the sweep's own orientation a tile (a,b,c) depends only on
 // (a-1,b,c), (a,b-1,c), (a,b,c-1), so all tiles with a+b+c = step form a
 // hyperplane that runs concurrently; one launch sweeps one tile hyperplane of
@@ -17,103 +17,206 @@
 // one per tile column, psi_bo one per tile column x row).  The reference's
 // i/j/k plane fields are the running face buffers between tiles, with chains
 // fastest, so every global access of a warp is a contiguous run.
+//
+// FP64 on GB300 issues at 1/61 of the FP32 rate and one IEEE divide costs
+// about ten FP64 slots, so on a uniform mesh the denominator's reciprocal is
+// tabulated per (sigt class, direction): den = ((cx+cy)+cz) + sigt is formed
+// exactly as per cell (same operands, same association) and rounded once to
+// 1/den; the cell then multiplies (psi differs from num/den by at most 1.5 ulp).
+//
+// The population edit (Kernel::population) is fused: each thread accumulates
+// volume * psi over its cells (FP64, or compensated FP32 in the mixed form),
+// scales by w(d), and each block writes one partial; a fixed-order reduction
+// over the partials follows the sweep.
 #include "kgb_internal.h"
 
 namespace kgb {
 
-template <typename T, int TX, int TY>
+namespace {
+
+// Compensated FP32 accumulator (Knuth TwoSum): the running error term keeps the
+// sum of a tile's psi values accurate to FP64 level before it is widened.
+struct F32Acc {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = s + x;
+    const float bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+struct F64Acc {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <typename T> struct AccOf;
+template <> struct AccOf<double> { using type = F64Acc; };
+template <> struct AccOf<float> { using type = F32Acc; };
+
+__device__ __forceinline__ double blockSum128(double v) {
+  __shared__ double part[kSweepThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < kSweepThreads / 32; ++i) r += part[i];
+  return r;
+}
+
+}  // namespace
+
+template <typename T, int TX, int TY, bool RECIP, bool POP>
 __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const SweepArgs<T> a) {
-  const SdomDesc sd = a.sdoms[a.wave[blockIdx.z]];
+  const int sdom = a.wave[blockIdx.z];
+  const SdomDesc sd = a.sdoms[sdom];
   const int4 t = a.tiles[a.tile_off + blockIdx.y];
   const int nchain = a.Ds * a.Gs;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nchain) return;  // no block-level synchronisation below
-  const int gl = c / a.Ds;
-  const int dl = c - gl * a.Ds;
-  const int g = sd.glo + gl;
-  const int d = sd.dlo + dl;
+  typename AccOf<T>::type pop;
+  double wd = 0.0;
+  if (c < nchain) {
+    const int gl = c / a.Ds;
+    const int dl = c - gl * a.Ds;
+    const int g = sd.glo + gl;
+    const int d = sd.dlo + dl;
+    if (POP) wd = a.w[d];
 
-  // Oriented coordinates i' run along the sweep; i = id > 0 ? i' : nxs-1-i'.
-  // Partial tiles only occur at the downwind end, so an invalid cell never
-  // precedes a valid one in a row.
-  const int ib = t.x * TX, jb = t.y * TY, kb = t.z * a.tz;
-  int iloc[TX], jloc[TY];
-  bool iv[TX], jv[TY];
-  T cxr[TX], cyr[TY];
+    // Oriented coordinates i' run along the sweep; i = id > 0 ? i' : nxs-1-i'.
+    // Partial tiles only occur at the downwind end, so an invalid cell never
+    // precedes a valid one in a row.
+    const int ib = t.x * TX, jb = t.y * TY, kb = t.z * a.tz;
+    int iloc[TX], jloc[TY];
+    bool iv[TX], jv[TY];
+    T cxr[TX], cyr[TY];
 #pragma unroll
-  for (int ii = 0; ii < TX; ++ii) {
-    const int ip = ib + ii;
-    iv[ii] = ip < a.nxs;
-    iloc[ii] = sd.id > 0 ? ip : a.nxs - 1 - ip;
-    cxr[ii] = iv[ii] ? a.cx[(int64_t)d * a.nx + sd.io + iloc[ii]] : T(0);
-  }
-#pragma unroll
-  for (int jj = 0; jj < TY; ++jj) {
-    const int jp = jb + jj;
-    jv[jj] = jp < a.nys;
-    jloc[jj] = sd.jd > 0 ? jp : a.nys - 1 - jp;
-    cyr[jj] = jv[jj] ? a.cy[(int64_t)d * a.ny + sd.jo + jloc[jj]] : T(0);
-  }
-
-  T *const ipl = a.iplane + sd.ip;  // [nzs][nys][nchain]
-  T *const jpl = a.jplane + sd.jp;  // [nzs][nxs][nchain]
-  T *const kpl = a.kplane + sd.kp;  // [nys][nxs][nchain]
-
-  T bo[TX][TY];
-#pragma unroll
-  for (int ii = 0; ii < TX; ++ii)
-#pragma unroll
-    for (int jj = 0; jj < TY; ++jj)
-      bo[ii][jj] = (iv[ii] && jv[jj]) ? kpl[((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c] : T(0);
-
-  const int kend = min(a.tz, a.nzs - kb);
-  for (int kk = 0; kk < kend; ++kk) {
-    const int kq = kb + kk;
-    const int k = sd.kd > 0 ? kq : a.nzs - 1 - kq;
-    const T czk = a.cz[(int64_t)d * a.nz + sd.ko + k];
-    T fr[TX];
-#pragma unroll
-    for (int ii = 0; ii < TX; ++ii) fr[ii] = iv[ii] ? jpl[((int64_t)k * a.nxs + iloc[ii]) * nchain + c] : T(0);
+    for (int ii = 0; ii < TX; ++ii) {
+      const int ip = ib + ii;
+      iv[ii] = ip < a.nxs;
+      iloc[ii] = sd.id > 0 ? ip : a.nxs - 1 - ip;
+      cxr[ii] = iv[ii] ? a.cx[(int64_t)d * a.nx + sd.io + iloc[ii]] : T(0);
+    }
 #pragma unroll
     for (int jj = 0; jj < TY; ++jj) {
-      if (!jv[jj]) continue;
-      const int j = jloc[jj];
-      T *const lfp = ipl + ((int64_t)k * a.nys + j) * nchain + c;
-      T lf = *lfp;
-      const int64_t zrow = ((int64_t)(sd.ko + k) * a.ny + (sd.jo + j)) * a.nx + sd.io;
+      const int jp = jb + jj;
+      jv[jj] = jp < a.nys;
+      jloc[jj] = sd.jd > 0 ? jp : a.nys - 1 - jp;
+      cyr[jj] = jv[jj] ? a.cy[(int64_t)d * a.ny + sd.jo + jloc[jj]] : T(0);
+    }
+
+    T *const ipl = a.iplane + sd.ip;  // [nzs][nys][nchain]
+    T *const jpl = a.jplane + sd.jp;  // [nzs][nxs][nchain]
+    T *const kpl = a.kplane + sd.kp;  // [nys][nxs][nchain]
+
+    T bo[TX][TY];
 #pragma unroll
-      for (int ii = 0; ii < TX; ++ii) {
-        if (!iv[ii]) continue;
-        const int64_t z = zrow + iloc[ii];
-        const int64_t e = (z * a.G + g) * a.D + d;
-        const T r = a.rhs[e];
-        const T st = a.sigt[z * a.G + g];
-        const T num = r + lf * cxr[ii] + fr[ii] * cyr[jj] + bo[ii][jj] * czk;
-        const T den = cxr[ii] + cyr[jj] + czk + st;
-        const T ps = num / den;
-        a.psi[e] = ps;
-        lf = T(2) * ps - lf;
-        fr[ii] = T(2) * ps - fr[ii];
-        bo[ii][jj] = T(2) * ps - bo[ii][jj];
+    for (int ii = 0; ii < TX; ++ii)
+#pragma unroll
+      for (int jj = 0; jj < TY; ++jj)
+        bo[ii][jj] = (iv[ii] && jv[jj]) ? kpl[((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c] : T(0);
+
+    const T *__restrict__ rhs = a.rhs;
+    T *__restrict__ psi = a.psi;
+    const int kend = min(a.tz, a.nzs - kb);
+    for (int kk = 0; kk < kend; ++kk) {
+      const int kq = kb + kk;
+      const int k = sd.kd > 0 ? kq : a.nzs - 1 - kq;
+      const T czk = a.cz[(int64_t)d * a.nz + sd.ko + k];
+      // The slice's loads do not depend on the upwind chain: issue them all
+      // before the first cell so their latency overlaps.
+      T rv[TY][TX], sv[TY][TX];
+      const int64_t zslice = (int64_t)(sd.ko + k) * a.ny;
+#pragma unroll
+      for (int jj = 0; jj < TY; ++jj) {
+        const int64_t zrow = (zslice + (sd.jo + jloc[jj])) * a.nx + sd.io;
+#pragma unroll
+        for (int ii = 0; ii < TX; ++ii) {
+          const int64_t z = zrow + iloc[ii];
+          if (iv[ii] && jv[jj]) {
+            rv[jj][ii] = rhs[(z * a.G + g) * a.D + d];
+            if (RECIP) sv[jj][ii] = (T)a.inv[(int64_t)a.cls[z * a.G + g] * a.D + d];
+            else sv[jj][ii] = a.sigt[z * a.G + g];
+          } else {
+            rv[jj][ii] = T(0);
+            sv[jj][ii] = T(1);
+          }
+        }
       }
-      *lfp = lf;
+      T fr[TX];
+#pragma unroll
+      for (int ii = 0; ii < TX; ++ii) fr[ii] = iv[ii] ? jpl[((int64_t)k * a.nxs + iloc[ii]) * nchain + c] : T(0);
+#pragma unroll
+      for (int jj = 0; jj < TY; ++jj) {
+        if (!jv[jj]) continue;
+        const int j = jloc[jj];
+        T *const lfp = ipl + ((int64_t)k * a.nys + j) * nchain + c;
+        T lf = *lfp;
+        const int64_t zrow = (zslice + (sd.jo + j)) * a.nx + sd.io;
+#pragma unroll
+        for (int ii = 0; ii < TX; ++ii) {
+          if (!iv[ii]) continue;
+          const int64_t z = zrow + iloc[ii];
+          const int64_t e = (z * a.G + g) * a.D + d;
+          const T num = rv[jj][ii] + lf * cxr[ii] + fr[ii] * cyr[jj] + bo[ii][jj] * czk;
+          T ps;
+          if (RECIP) {
+            ps = num * sv[jj][ii];
+          } else {
+            const T den = cxr[ii] + cyr[jj] + czk + sv[jj][ii];
+            ps = num / den;
+          }
+          psi[e] = ps;
+          lf = T(2) * ps - lf;
+          fr[ii] = T(2) * ps - fr[ii];
+          bo[ii][jj] = T(2) * ps - bo[ii][jj];
+          if (POP) {
+            if (a.vol_uniform > 0.0) pop.add(ps);
+            else pop.add((T)a.vol[z] * ps);
+          }
+        }
+        *lfp = lf;
+      }
+#pragma unroll
+      for (int ii = 0; ii < TX; ++ii)
+        if (iv[ii]) jpl[((int64_t)k * a.nxs + iloc[ii]) * nchain + c] = fr[ii];
     }
 #pragma unroll
     for (int ii = 0; ii < TX; ++ii)
-      if (iv[ii]) jpl[((int64_t)k * a.nxs + iloc[ii]) * nchain + c] = fr[ii];
+#pragma unroll
+      for (int jj = 0; jj < TY; ++jj)
+        if (iv[ii] && jv[jj]) kpl[((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c] = bo[ii][jj];
   }
-#pragma unroll
-  for (int ii = 0; ii < TX; ++ii)
-#pragma unroll
-    for (int jj = 0; jj < TY; ++jj)
-      if (iv[ii] && jv[jj]) kpl[((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c] = bo[ii][jj];
+  if (POP) {
+    double v = pop.value() * wd;
+    if (a.vol_uniform > 0.0) v *= a.vol_uniform;
+    const double b = blockSum128(v);
+    if (threadIdx.x == 0)
+      a.pop[((int64_t)(a.tile_off + blockIdx.y) * a.nsdom + sdom) * gridDim.x + blockIdx.x] = b;
+  }
 }
+
+namespace {
+template <typename T, int TX, int TY>
+void launchTile(const SweepArgs<T> &a, dim3 grid, cudaStream_t s) {
+  const bool recip = a.cls != nullptr && a.inv != nullptr;
+  const bool pop = a.pop != nullptr;
+  if (recip && pop) sweep_step_kernel<T, TX, TY, true, true><<<grid, kSweepThreads, 0, s>>>(a);
+  else if (recip) sweep_step_kernel<T, TX, TY, true, false><<<grid, kSweepThreads, 0, s>>>(a);
+  else if (pop) sweep_step_kernel<T, TX, TY, false, true><<<grid, kSweepThreads, 0, s>>>(a);
+  else sweep_step_kernel<T, TX, TY, false, false><<<grid, kSweepThreads, 0, s>>>(a);
+}
+}  // namespace
 
 template <typename T>
 void launch_sweep_step(const SweepArgs<T> &a, int ntiles, int nwave, cudaStream_t s) {
   const int nchain = a.Ds * a.Gs;
   dim3 grid((nchain + kSweepThreads - 1) / kSweepThreads, ntiles, nwave);
-  sweep_step_kernel<T, kTileX, kTileY><<<grid, kSweepThreads, 0, s>>>(a);
+  if (a.tx == 4 && a.ty == 4) launchTile<T, 4, 4>(a, grid, s);
+  else if (a.tx == 4 && a.ty == 2) launchTile<T, 4, 2>(a, grid, s);
+  else launchTile<T, 2, 2>(a, grid, s);
 }
 
 template void launch_sweep_step<double>(const SweepArgs<double> &, int, int, cudaStream_t);

@@ -116,14 +116,51 @@ def test_sweep_subdomain_reads_incoming_planes(oracle, kgb):
     check(ctx.download("k_plane"), p.get("k_plane"), 1e-12)
 
 
-@pytest.mark.parametrize("tz", [1, 3, 4, 16])
-def test_sweep_tile_depth(oracle, kgb, tz):
+@pytest.mark.parametrize("tz,txy", [(1, 44), (3, 44), (4, 42), (16, 22), (5, 42)])
+def test_sweep_tile_shapes(oracle, kgb, tz, txy):
     p, ctx = pair(oracle, kgb, zones=(7, 9, 10), quad=16, groups=2)
     ctx.set_option("sweep_tile_z", tz)
+    ctx.set_option("sweep_tile_xy", txy)
     rhs = np.random.default_rng(6).uniform(0.0, 1.0, ctx.field_bytes("rhs") // 8)
     p.set("rhs", rhs); ctx.upload("rhs", rhs)
     p.sweep_solver(); ctx.sweep_solver()
     check(ctx.download("psi"), p.get("psi"), 1e-12)
+
+
+@pytest.mark.parametrize("recip", [0, 1])
+def test_sweep_reciprocal_table_and_divide(oracle, kgb, recip):
+    """Both denominator paths of the FP64 sweep (tabulated 1/den on a uniform mesh, or a divide per cell)."""
+    p, ctx = pair(oracle, kgb, zones=(10, 9, 8), quad=(4, 8), groups=4, scatter=1, geometry=0, perturb=1)
+    ctx.set_option("sweep_reciprocals", recip)
+    want = p.solve(3)
+    got = ctx.solve(3)
+    np.testing.assert_allclose(got, want, rtol=1e-12)
+    check(ctx.download("psi"), p.get("psi"), 1e-12)
+
+
+def test_nonuniform_mesh(oracle, kgb):
+    """Zone widths that vary along each axis (the sweep then divides per cell)."""
+    p, ctx = pair(oracle, kgb, zones=(7, 6, 5), quad=16, groups=3, geometry=1)
+    for n, k in (("dx", 7), ("dy", 6), ("dz", 5)):
+        w = p.get(n) * (1.0 + 0.3 * np.sin(np.arange(k)))
+        p.set(n, w); ctx.upload(n, w)
+    rhs = np.random.default_rng(8).uniform(0.0, 1.0, ctx.field_bytes("rhs") // 8)
+    p.set("rhs", rhs); ctx.upload("rhs", rhs)
+    p.sweep_solver(); ctx.sweep_solver()
+    check(ctx.download("psi"), p.get("psi"), 1e-12)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_autotune_then_solve(oracle, kgb, precision):
+    """The autotuner's choice keeps the sweep exact (FP64) / within the mixed tolerance."""
+    p, ctx = pair(oracle, kgb, precision=precision, zones=(12, 10, 9), quad=(4, 8), groups=8, scatter=1, geometry=1)
+    ctx.fill("psi", 0.0)
+    ctx.iterate()
+    tuned = ctx.autotune()
+    assert tuned["sweep_tile_xy"] in (44, 42, 22) and tuned["sweep_ms"] > 0
+    want = p.solve(3)
+    got = ctx.solve(3)
+    np.testing.assert_allclose(got, want, rtol=1e-12 if precision == 0 else 1e-5)
 
 
 def test_population_and_balance(oracle, kgb):
