@@ -174,7 +174,9 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
 /* Tuning knobs: "sweep_tile_z" (tile depth in k, default 4); "sweep_tile_xy"
  * (tile footprint in i and j: 44, 42 or 22, default 44); "sweep_reciprocals"
  * (FP64 on a uniform mesh: 1 = tabulate 1/denominator per (sigt value,
- * direction), the default; 0 = divide in every cell). */
+ * direction), the default; 0 = divide in every cell); "moments_tensor" (1 = LTimes
+ * and LPlusTimes on the tensor cores with exact digit products when the shapes
+ * fit, the default; 0 = SIMT kernels). */
 int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
 /* Sweep autotuner: times every tile shape (footprint 4x4, 4x2, 2x2 x depth
  * 2, 4, 8, 16 zones) on this problem with CUDA events, keeps the fastest and

@@ -144,6 +144,14 @@ struct kgb_ctx {
   uint16_t *cls_d = nullptr;
   double *inv_d = nullptr;
   int64_t ncls = 0;
+  // tensor-core moment transforms (tc_moments.cu)
+  bool allow_tc = true;
+  bool tc_lt = false, tc_lp = false;        // LTimes / LPlusTimes planned for the tensor cores
+  uint16_t *tc_lt_img = nullptr, *tc_lp_img = nullptr;
+  int *tc_lt_exp = nullptr, *tc_lp_exp = nullptr;
+  int tc_lt_kpad = 0, tc_lp_nhalf = 0;
+  int *err_d = nullptr;                     // set by kernels whose bounded waits gave up
+  int nsm = 0;
   // fused population partials, one per (tile, subdomain, chain block)
   double *pop_slots = nullptr;
   int64_t npop_slots = 0;
@@ -331,7 +339,8 @@ void freeAll(kgb_ctx *c) {
                   c->sigsT, c->cx, c->cy, c->cz, c->w_d, c->cos_d[0], c->cos_d[1], c->cos_d[2], c->vol_d,
                   c->dxyz_d[0], c->dxyz_d[1], c->dxyz_d[2], c->zmix_start, c->zmix_count, c->mix_mat, c->mix_zone,
                   c->mix_frac, c->gp_lo, c->gp_hi, c->sdoms_d, c->ident_d, c->levels_d, c->tiles_d, c->partials,
-                  c->results, c->parts_dev, c->staging, c->cls_d, c->inv_d, c->pop_slots};
+                  c->results, c->parts_dev, c->staging, c->cls_d, c->inv_d, c->pop_slots, c->tc_lt_img,
+                  c->tc_lp_img, c->tc_lt_exp, c->tc_lp_exp, c->err_d};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->psi = c->rhs = c->phi = c->phi_out = c->sigt = nullptr;
@@ -349,6 +358,10 @@ void freeAll(kgb_ctx *c) {
   c->cls_d = nullptr;
   c->inv_d = nullptr;
   c->pop_slots = nullptr;
+  c->tc_lt_img = c->tc_lp_img = nullptr;
+  c->tc_lt_exp = c->tc_lp_exp = nullptr;
+  c->tc_lt = c->tc_lp = false;
+  c->err_d = nullptr;
   c->npop_slots = 0;
   c->use_recip = false;
   c->staging_bytes = 0;
@@ -445,6 +458,58 @@ int buildReciprocals(kgb_ctx *ctx) {
   return KGB_OK;
 }
 
+// Plan the tensor-core LTimes / LPlusTimes: digit images of L and L+ and the
+// shapes the kernel supports (exact diagonal sums need K <= 128 directions in
+// FP64 and <= 256 in the mixed form; moments fit one 32-wide K chunk).
+template <typename T>
+int planTensorMoments(kgb_ctx *ctx) {
+  ctx->tc_lt = ctx->tc_lp = false;
+  if (!ctx->allow_tc) return KGB_OK;
+  const bool f64 = sizeof(T) == 8;
+  const int S = f64 ? 8 : 4;
+  const int D = ctx->D, M = ctx->M;
+  auto upload = [&](uint16_t **img_d, int **exp_d, const std::vector<uint16_t> &img, const std::vector<int> &ex) {
+    if (*img_d) cudaFree(*img_d);
+    if (*exp_d) cudaFree(*exp_d);
+    *img_d = nullptr;
+    *exp_d = nullptr;
+    int r;
+    if ((r = dmalloc(ctx, img_d, img.size())) || (r = dmalloc(ctx, exp_d, ex.size()))) return r;
+    if (cudaMemcpyAsync(*img_d, img.data(), img.size() * 2, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        cudaMemcpyAsync(*exp_d, ex.data(), ex.size() * 4, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      return fail(ctx, KGB_ERR_CUDA, "tensor plan upload failed");
+    return (int)KGB_OK;
+  };
+  std::vector<uint16_t> img;
+  std::vector<int> ex;
+  int rc;
+  // LTimes: B[d][m] = ell(m,d), K = D, N = M (one 32-wide block)
+  if (M <= 32 && D <= (f64 ? 128 : 256)) {
+    const int kpad = (D + 31) / 32 * 32;
+    tc_build_b<T>(ctx->ell_h.data(), D, M, kpad, S, 32, 1, img, ex);
+    if ((rc = upload(&ctx->tc_lt_img, &ctx->tc_lt_exp, img, ex))) return rc;
+    ctx->tc_lt_kpad = kpad;
+    ctx->tc_lt = true;
+  }
+  // LPlusTimes: B[m][d] = ell_plus(d,m), K = M (one chunk), N = D in blocks of NB
+  if (M <= 32) {
+    const int NB = f64 ? 64 : 128;
+    const int nhalf = (D + NB - 1) / NB;
+    const size_t smem = (size_t)nhalf * 32 * S * NB * 2 + (size_t)S * 32 * 128 * 2 + 2048 + 4 * nhalf * NB;
+    if (smem <= 227 * 1024) {
+      std::vector<double> bt((size_t)M * D);
+      for (int d = 0; d < D; ++d)
+        for (int m = 0; m < M; ++m) bt[(size_t)m * D + d] = ctx->ellp_h[(size_t)d * M + m];
+      tc_build_b<T>(bt.data(), M, D, 32, S, NB, nhalf, img, ex);
+      if ((rc = upload(&ctx->tc_lp_img, &ctx->tc_lp_exp, img, ex))) return rc;
+      ctx->tc_lp_nhalf = nhalf;
+      ctx->tc_lp = true;
+    }
+  }
+  return KGB_OK;
+}
+
 template <typename T>
 int prepareT(kgb_ctx *ctx) {
   int rc;
@@ -513,6 +578,7 @@ int prepareT(kgb_ctx *ctx) {
     if ((rc = need(ctx, {"ell", "ell_plus"}))) return rc;
     if ((rc = uploadVec<T>(ctx, ctx->ell, ctx->ell_h))) return rc;
     if ((rc = uploadVec<T>(ctx, ctx->ellp, ctx->ellp_h))) return rc;
+    if ((rc = planTensorMoments<T>(ctx))) return rc;
     ctx->dirty_ell = false;
   }
   if (ctx->dirty_sigs) {
@@ -760,9 +826,40 @@ ScatterArgsBase scatterArgs(kgb_ctx *ctx) {
   return a;
 }
 
+template <typename T>
+void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, int N, int nhalf, const uint16_t *img,
+            const int *ex, bool acc, bool multi_n) {
+  TcArgs<T> a{};
+  a.A = A;
+  a.C = C;
+  a.rows = ctx->Z * ctx->G;
+  a.lda = lda;
+  a.ldc = ldc;
+  a.K = K;
+  a.kpad = kpad;
+  a.N = N;
+  a.nhalf = nhalf;
+  a.bimg = img;
+  a.bexp = ex;
+  a.err = ctx->err_d;
+  a.accumulate = acc;
+  a.nsm = ctx->nsm;
+  launch_tc_rows<T>(a, sizeof(T) == 8 ? 8 : 4, 0, multi_n, ctx->stream);
+}
+
 int doLTimes(kgb_ctx *ctx, bool acc) {
   FamScope fs(ctx, "ltimes");
   const int64_t rows = ctx->Z * ctx->G;
+  if (ctx->tc_lt) {
+    if (ctx->prec == KGB_FP64)
+      tcRows<double>(ctx, as<double>(ctx->psi), as<double>(ctx->phi), ctx->D, ctx->M, ctx->D, ctx->tc_lt_kpad, ctx->M, 1,
+                     ctx->tc_lt_img, ctx->tc_lt_exp, acc, false);
+    else
+      tcRows<float>(ctx, as<float>(ctx->psi), as<float>(ctx->phi), ctx->D, ctx->M, ctx->D, ctx->tc_lt_kpad, ctx->M, 1,
+                    ctx->tc_lt_img, ctx->tc_lt_exp, acc, false);
+    CKN(1);
+    return KGB_OK;
+  }
   if (ctx->prec == KGB_FP64)
     launch_ltimes<double>(as<double>(ctx->psi), as<double>(ctx->phi), as<double>(ctx->ell), rows, ctx->D, ctx->M, acc, ctx->stream);
   else
@@ -774,6 +871,16 @@ int doLTimes(kgb_ctx *ctx, bool acc) {
 int doLPlusTimes(kgb_ctx *ctx, bool acc) {
   FamScope fs(ctx, "lplustimes");
   const int64_t rows = ctx->Z * ctx->G;
+  if (ctx->tc_lp) {
+    if (ctx->prec == KGB_FP64)
+      tcRows<double>(ctx, as<double>(ctx->phi_out), as<double>(ctx->rhs), ctx->M, ctx->D, ctx->M, 32, ctx->D,
+                     ctx->tc_lp_nhalf, ctx->tc_lp_img, ctx->tc_lp_exp, acc, true);
+    else
+      tcRows<float>(ctx, as<float>(ctx->phi_out), as<float>(ctx->rhs), ctx->M, ctx->D, ctx->M, 32, ctx->D,
+                    ctx->tc_lp_nhalf, ctx->tc_lp_img, ctx->tc_lp_exp, acc, true);
+    CKN(1);
+    return KGB_OK;
+  }
   if (ctx->prec == KGB_FP64)
     launch_lplustimes<double>(as<double>(ctx->phi_out), as<double>(ctx->rhs), as<double>(ctx->ellp), rows, ctx->D, ctx->M, acc, ctx->stream);
   else
@@ -812,6 +919,18 @@ int doPopulation(kgb_ctx *ctx, double *out) {
   else
     launch_population<float>(as<float>(ctx->psi), ctx->w_d, ctx->vol_d, rows, ctx->G, ctx->D, ctx->partials, ctx->npart, out, ctx->stream);
   CKN(2);
+  return KGB_OK;
+}
+
+// Reports (and clears) a bounded device-side wait that gave up.
+int checkDeviceError(kgb_ctx *ctx) {
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, ctx->err_d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (h) {
+    CK(cudaMemsetAsync(ctx->err_d, 0, sizeof(int), ctx->stream));
+    return fail(ctx, KGB_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
+  }
   return KGB_OK;
 }
 
@@ -940,6 +1059,13 @@ int kgb_setup(kgb_ctx *ctx, const kgb_dims *d) {
       (rc = dmalloc(ctx, &ctx->sdoms_d, ctx->dc.num())) || (rc = dmalloc(ctx, &ctx->ident_d, ctx->dc.num())) ||
       (rc = dmalloc(ctx, &ctx->levels_d, ctx->dc.num())))
     goto oom;
+  {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    ctx->nsm = nsm > 0 ? nsm : 152;
+  }
+  if ((rc = dalloc(ctx, (void **)&ctx->err_d, sizeof(int)))) goto oom;
   ctx->npart = 152 * 4;
   if ((rc = dmalloc(ctx, &ctx->partials, 2 * ctx->npart)) || (rc = dmalloc(ctx, &ctx->results, 16))) goto oom;
   {
@@ -1333,6 +1459,7 @@ int kgb_iterate(kgb_ctx *ctx, double q, double *part) {
   if (part) {
     CK(cudaMemcpyAsync(part, ctx->results, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return checkDeviceError(ctx);
   }
   return KGB_OK;
 }
@@ -1353,14 +1480,14 @@ int kgb_solve(kgb_ctx *ctx, int32_t niter, double q, double *part) {
     if ((rc = iterateDevice(ctx, q, ctx->parts_dev + it))) return rc;
   if (part) CK(cudaMemcpyAsync(part, ctx->parts_dev, niter * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  return KGB_OK;
+  return checkDeviceError(ctx);
 }
 
 int kgb_sync(kgb_ctx *ctx) {
   if (!ctx) return KGB_ERR_ARG;
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
-  return KGB_OK;
+  return ctx->err_d ? checkDeviceError(ctx) : KGB_OK;
 }
 
 int kgb_set_stream(kgb_ctx *ctx, void *s) {
@@ -1383,6 +1510,11 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->tx = (int)(value / 10);
     ctx->ty = (int)(value % 10);
     if (ctx->ready) return buildTiles(ctx);
+    return KGB_OK;
+  }
+  if (!std::strcmp(key, "moments_tensor")) {
+    ctx->allow_tc = value != 0;
+    ctx->dirty_ell = true;
     return KGB_OK;
   }
   if (!std::strcmp(key, "sweep_reciprocals")) {

@@ -83,6 +83,27 @@ template <typename T>
 void launch_source(T *phi_out, int64_t nmix, const int *mix_zone, const int *mix_mat, const double *mix_frac,
                    int G, int M, double strength, cudaStream_t s);
 
+// Tensor-core row products C[r][n] (+)= sum_k A[r][k] B[k][n] (tc_moments.cu).
+template <typename T>
+struct TcArgs {
+  const T *A;            // [rows][lda]
+  T *C;                  // [rows][ldc]
+  int64_t rows;
+  int lda, ldc;
+  int K, kpad, N;        // real K, K padded to a multiple of 32, real N
+  int nhalf;             // N blocks (1 for LTimes; LPlusTimes splits N)
+  const uint16_t *bimg;  // digit image of B, built by tc_build_b
+  const int *bexp;       // per-column exponent of B
+  int *err;              // set to 1 when a bounded wait gives up
+  bool accumulate;
+  int nsm;
+};
+template <typename T>
+void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhalf, std::vector<uint16_t> &img,
+                std::vector<int> &texp);
+template <typename T>
+void launch_tc_rows(const TcArgs<T> &a, int S, int NB, bool multi_n, cudaStream_t s);
+
 // FP64 reductions, two passes with a fixed order: per-block partials then one block.
 template <typename T>
 void launch_population(const T *psi, const double *w, const double *vol, int64_t rows, int G, int D,

@@ -1,0 +1,440 @@
+// tc_moments.cu -- LTimes and LPlusTimes on the GB300 tensor cores (tcgen05).
+//
+// Both transforms are row products C[r][n] = sum_k A[r][k] B[k][n] over the
+// (zone, group) rows of the device nesting: LTimes has A = psi (K = directions)
+// and B[d][m] = ell(m,d); LPlusTimes has A = phi_out (K = moments) and
+// B[m][d] = ell_plus(d,m).  Replaces Kernel::LTimes
+// (src/Kripke/Kernel/LTimes.cpp:54-65) and Kernel::LPlusTimes
+// (src/Kripke/Kernel/LPlusTimes.cpp:49-60) when the shapes fit.
+//
+// Exact products from bf16 digits (the Ozaki splitting, Ozaki et al. 2012,
+// "Error-free transformations of matrix multiplication by using fast
+// routines of matrix multiplication"): every A row is scaled by a power of two
+// taken from its largest element and written as S signed 7-bit digits,
+//   |A[r][k]| = 2^s_r * sum_i a_i * 2^-7i   (truncated after 7*S bits),
+// and every B column likewise with 2^t_n and digits b_j (done on the host).
+// A digit is an integer below 128, exact in bf16; a digit product is an
+// integer below 2^14, and for every anti-diagonal i+j the sum over k of the
+// products stays below 2^24, so tcgen05.mma with FP32 accumulation in tensor
+// memory computes each diagonal sum D_{i+j} exactly.  The diagonals are
+// recombined in integer arithmetic and scaled once:
+//   C = 2^(s_r + t_n) * sum_{k=2..S+1} D_k * 2^-7k.
+// Pairs with i+j > S+1 are dropped: their weight is below 2^-7(S+1) of the
+// leading term.  S = 8 (56 bits) gives the FP64 form, S = 4 (28 bits) the
+// mixed form.
+//
+// Tensor-memory layout: D_k occupies columns [(k-2)*NB, (k-1)*NB).  The B digit
+// slices are stacked along N (slice j in rows [(j-1)*NB, j*NB)), so one MMA of
+// A slice i against the first S+1-i slices of the stack, written at column
+// (i-1)*NB, deposits every product a_i*b_j into diagonal i+j's block.
+//
+// Shared-memory operand layout: K-major, no swizzle ("interleaved" core
+// matrices of 8 rows x 16 bytes; core matrices adjacent in K are LBO bytes
+// apart, adjacent 8-row groups SBO = 128 bytes apart).  One CTA per SM
+// (persistent over 128-row tiles); all 128 threads split rows and run the
+// epilogue (thread t owns row t = TMEM lane t), thread 0 issues the MMAs.  The
+// B image reaches shared memory with one cp.async.bulk.  Every mbarrier wait is
+// bounded; on timeout the CTA records the failure, releases its tensor memory
+// and returns.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "kgb_internal.h"
+
+namespace kgb {
+
+namespace {
+
+constexpr int kTcThreads = 128;
+constexpr int kTcRows = 128;            // rows per tile = MMA M
+constexpr int kTcChunk = 32;            // K elements staged per A buffer
+constexpr uint32_t kWaitLimit = 1u << 24;  // mbarrier polls before giving up
+
+__device__ __forceinline__ uint32_t smemAddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t matDesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo & 0x3FFFF) >> 4) << 16;
+  d |= (uint64_t)((sbo & 0x3FFFF) >> 4) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version for tcgen05; layout bits 61-63 = 0: no swizzle
+  return d;
+}
+
+// kind::f16 instruction descriptor: FP32 accumulate, bf16 A and B, both K-major, M = 128
+__device__ __forceinline__ uint32_t instrDesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+      "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smemAddr(bar)));
+}
+
+// Bounded wait for the phase with the given parity to complete.
+__device__ __forceinline__ bool waitParity(uint64_t *bar, uint32_t parity) {
+  uint32_t done = 0;
+  for (uint32_t it = 0; it < kWaitLimit && !done; ++it) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(smemAddr(bar)), "r"(parity));
+  }
+  return done != 0;
+}
+
+__device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&v)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr));
+}
+
+// bf16 bit pattern of sign * d for an integer 0 <= d < 128 (exact)
+__device__ __forceinline__ uint32_t digitBf16(uint32_t d, uint32_t sign) {
+  const float f = __uint_as_float(0x4B000000u | d) - 8388608.0f;
+  return (__float_as_uint(f) >> 16) | (sign << 15);
+}
+
+// Biased exponent (subnormals count as 1) and significand with the implicit bit.
+__device__ __forceinline__ int expOf(double x) {
+  const int e = (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+  return e > 0 ? e : 1;
+}
+__device__ __forceinline__ int expOf(float x) {
+  const int e = (int)((__float_as_uint(x) >> 23) & 0xFF);
+  return e > 0 ? e : 1;
+}
+
+// Digit source: the 7*S-bit fixed-point magnitude of x relative to the row's
+// largest exponent emax, and its sign.
+template <typename T, int S> struct Fixed;
+template <int S> struct Fixed<double, S> {
+  static __device__ __forceinline__ uint64_t mag(double x, int emax, uint32_t &sign) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    sign = (uint32_t)(b >> 63);
+    const int e = (int)((b >> 52) & 0x7FF);
+    const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
+    const int sh = (e > 0 ? e : 1) - emax + (7 * S - 53);  // left shift; at most 7S-53
+    if (sh >= 0) return m << sh;
+    return -sh >= 64 ? 0ull : m >> (-sh);
+  }
+};
+template <int S> struct Fixed<float, S> {
+  static __device__ __forceinline__ uint64_t mag(float x, int emax, uint32_t &sign) {
+    const uint32_t b = __float_as_uint(x);
+    sign = b >> 31;
+    const int e = (int)((b >> 23) & 0xFF);
+    const uint64_t m = (uint64_t)((b & 0x7FFFFFu) | (e ? (1u << 23) : 0u));
+    const int sh = (e > 0 ? e : 1) - emax + (7 * S - 24);
+    if (sh >= 0) return m << sh;
+    return -sh >= 64 ? 0ull : m >> (-sh);
+  }
+};
+
+// x * 2^e: exponent arithmetic when 2^e is a normal number, ldexp otherwise
+__device__ __forceinline__ double scale2(double x, int e) {
+  return (e >= -1022 && e <= 1023) ? x * __longlong_as_double((long long)(e + 1023) << 52) : ldexp(x, e);
+}
+__device__ __forceinline__ float scale2(float x, int e) {
+  return (e >= -126 && e <= 127) ? x * __uint_as_float((uint32_t)(e + 127) << 23) : ldexpf(x, e);
+}
+
+// Combine the S diagonal sums (FP32, exact integers) into the output value.
+template <typename T, int S> struct Combine;
+template <> struct Combine<double, 8> {
+  // rowexp + colexp = s_r + t_n; value = (H*2^28 + L) * 2^(s_r + t_n - 63)
+  static __device__ __forceinline__ double value(const float (&dk)[8], int e0) {
+    long long h = 0, l = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) h = h * 128 + (long long)__float2int_rn(dk[k]);
+#pragma unroll
+    for (int k = 4; k < 8; ++k) l = l * 128 + (long long)__float2int_rn(dk[k]);
+    // h*2^28 + l is exact in 128 bits; the sum below rounds once
+    const double hs = scale2((double)h, 28);
+    return scale2(hs + (double)l, e0 - 63);
+  }
+};
+template <> struct Combine<float, 4> {
+  static __device__ __forceinline__ float value(const float (&dk)[4], int e0) {
+    long long x = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) x = x * 128 + (long long)__float2int_rn(dk[k]);
+    return scale2((float)x, e0 - 35);
+  }
+};
+
+template <typename T> struct TcBias;
+template <> struct TcBias<double> { static constexpr int v = 1022; };
+template <> struct TcBias<float> { static constexpr int v = 126; };
+
+template <typename T, int S, int NB, bool MULTI_N>
+__global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ uint64_t bars[3];  // 0,1: A buffers (MMA done), 2: B image load / per-half MMA done
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  constexpr int kTmemCols = S * NB;  // power of two: 128, 256 or 512
+  constexpr uint32_t kSliceBytes = kTcChunk * kTcRows * 2;  // one digit slice of one chunk: 8 KB
+  constexpr uint32_t kBufBytes = S * kSliceBytes;
+  constexpr uint32_t kLboA = (kTcRows / 8) * 128;           // 2048: next 8-element K group
+  const uint32_t lboB = (uint32_t)S * NB * 16;               // [kc][S*NB rows] image: next K group
+  const uint32_t halfBytes = (uint32_t)a.kpad * S * NB * 2;  // B image of one N block
+
+  const uint32_t base = smemAddr(smem_raw);
+  unsigned char *al = smem_raw + (((base + 1023u) & ~1023u) - base);
+  unsigned char *sB = al;
+  unsigned char *sA = al + ((halfBytes * a.nhalf + 1023u) & ~1023u);
+  int *sT = reinterpret_cast<int *>(sA + (MULTI_N ? 1 : 2) * kBufBytes);
+
+  // --- set-up: barriers, tensor memory, B image (one bulk copy), column exponents ---
+  if (tid == 0) {
+    for (int i = 0; i < 3; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(&bars[i])), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(&tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  for (int i = tid; i < a.nhalf * NB; i += kTcThreads) sT[i] = a.bexp[i];
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_slot;
+  const uint32_t bbytes = halfBytes * a.nhalf;
+  if (tid == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(&bars[2])), "r"(bbytes));
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smemAddr(sB)),
+                 "l"(a.bimg), "r"(bbytes), "r"(smemAddr(&bars[2])));
+  }
+  bool ok = __syncthreads_and(waitParity(&bars[2], 0));
+  uint32_t parity2 = 1;  // next phase of bars[2]
+  uint32_t uses[2] = {0, 0};
+
+  const int ntiles = (int)((a.rows + kTcRows - 1) / kTcRows);
+  const int nchunks = a.kpad / kTcChunk;
+  uint32_t item = 0;
+  for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+    const int64_t row = (int64_t)tile * kTcRows + tid;
+    const bool valid = row < a.rows;
+    const T *arow = a.A + row * a.lda;
+    // row exponent: largest biased exponent of the row (0 for an all-zero row)
+    int emax = 1;
+    if (valid)
+      for (int k = 0; k < a.K; ++k) emax = max(emax, expOf(arow[k]));
+
+    for (int c = 0; c < nchunks && ok; ++c, ++item) {
+      const int b = MULTI_N ? 0 : (int)(item & 1);
+      if (!MULTI_N && item >= 2) {  // the MMAs that last read this buffer must be done
+        ok = __syncthreads_and(waitParity(&bars[b], (uses[b] - 1) & 1) && ok);
+        if (!ok) break;
+      }
+      unsigned char *buf = sA + b * kBufBytes;
+      // split this chunk of the row into S digit slices (thread = row: 4 core-matrix rows per slice)
+#pragma unroll 1
+      for (int q = 0; q < kTcChunk / 8; ++q) {
+        uint32_t w[S][4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          uint32_t d0[S], d1[S];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int k = c * kTcChunk + q * 8 + e + h;
+            uint32_t sign = 0;
+            uint64_t f = 0;
+            if (valid && k < a.K) f = Fixed<T, S>::mag(arow[k], emax, sign);
+#pragma unroll
+            for (int i = 0; i < S; ++i) {
+              const uint32_t dg = (uint32_t)(f >> (7 * (S - 1 - i))) & 127u;
+              (h ? d1 : d0)[i] = digitBf16(dg, sign);
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < S; ++i) w[i][e >> 1] = d0[i] | (d1[i] << 16);
+        }
+        const uint32_t off = q * kLboA + (tid >> 3) * 128 + (tid & 7) * 16;
+#pragma unroll
+        for (int i = 0; i < S; ++i)
+          *reinterpret_cast<uint4 *>(buf + i * kSliceBytes + off) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;");
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      if (!MULTI_N && tid == 0) {
+        // accumulate this chunk: slice i against B slices 1..S+1-i, at diagonal offset (i-1)*NB
+#pragma unroll 1
+        for (int i = 1; i <= S; ++i) {
+          const int ncols = NB * (S + 1 - i);
+#pragma unroll 1
+          for (int ks = 0; ks < kTcChunk / 16; ++ks) {
+            const int kg = c * (kTcChunk / 16) + ks;  // global 16-element K step
+            const uint64_t da = matDesc(smemAddr(buf + (i - 1) * kSliceBytes + ks * 2 * kLboA), kLboA, 128);
+            for (int n0 = 0; n0 < ncols; n0 += 256) {
+              const int w = min(256, ncols - n0);
+              const uint64_t db = matDesc(smemAddr(sB) + kg * 2 * lboB + (n0 / 8) * 128, lboB, 128);
+              // slice 1's first MMA initialises every diagonal block; all later ones accumulate
+              mma(tmem + (uint32_t)((i - 1) * NB + n0), da, db, instrDesc(w), (c > 0 || ks > 0 || i > 1) ? 1u : 0u);
+            }
+          }
+        }
+        commit(&bars[b]);
+      }
+      if (!MULTI_N) uses[b]++;
+    }
+    if (!ok) break;
+
+    // --- epilogue(s) ---
+    for (int hf = 0; hf < a.nhalf && ok; ++hf) {
+      if (MULTI_N) {
+        if (tid == 0) {
+          const unsigned char *bh = sB + hf * halfBytes;
+#pragma unroll 1
+          for (int i = 1; i <= S; ++i) {
+            const int ncols = NB * (S + 1 - i);
+#pragma unroll 1
+            for (int ks = 0; ks < a.kpad / 16; ++ks) {
+              const uint64_t da = matDesc(smemAddr(sA + (i - 1) * kSliceBytes + ks * 2 * kLboA), kLboA, 128);
+              for (int n0 = 0; n0 < ncols; n0 += 256) {
+                const int w = min(256, ncols - n0);
+                const uint64_t db = matDesc(smemAddr(bh) + ks * 2 * lboB + (n0 / 8) * 128, lboB, 128);
+                mma(tmem + (uint32_t)((i - 1) * NB + n0), da, db, instrDesc(w), (ks > 0 || i > 1) ? 1u : 0u);
+              }
+            }
+          }
+          commit(&bars[2]);
+        }
+        ok = __syncthreads_and(waitParity(&bars[2], parity2) && ok);
+        parity2 ^= 1;
+      } else {
+        const int b = (int)((item - 1) & 1);
+        ok = __syncthreads_and(waitParity(&bars[b], (uses[b] - 1) & 1) && ok);
+      }
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t lane = (uint32_t)(warp * 32) << 16;
+      T *crow = a.C + row * a.ldc;
+#pragma unroll 1
+      for (int c0 = 0; c0 < NB; c0 += 8) {
+        uint32_t v[S][8];
+#pragma unroll
+        for (int k = 0; k < S; ++k) ld8(tmem + lane + (uint32_t)(k * NB + c0), v[k]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int n = hf * NB + c0 + u;
+          float dk[S];
+#pragma unroll
+          for (int k = 0; k < S; ++k) dk[k] = __uint_as_float(v[k][u]);
+          if (valid && n < a.N) {
+            const int e0 = (emax - TcBias<T>::v) + sT[n];
+            const T val = Combine<T, S>::value(dk, e0);
+            crow[n] = a.accumulate ? crow[n] + val : val;
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;");
+    }
+  }
+  if (!ok && tid == 0) atomicExch(a.err, 1);
+  // drain: let any committed MMAs finish (bounded) before the tensor memory is released
+  if (!MULTI_N && tid == 0 && ok) {
+    for (int b = 0; b < 2; ++b)
+      if (uses[b] > 0) waitParity(&bars[b], (uses[b] - 1) & 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+
+template <typename T, int S, int NB, bool MULTI_N>
+void launchRows(const TcArgs<T> &a, cudaStream_t s) {
+  const size_t halfBytes = (size_t)a.kpad * S * NB * 2;
+  const size_t bufBytes = (size_t)S * kTcChunk * kTcRows * 2;
+  const size_t smem = 1024 + ((halfBytes * a.nhalf + 1023) & ~(size_t)1023) + (MULTI_N ? 1 : 2) * bufBytes +
+                      sizeof(int) * a.nhalf * NB;
+  cudaFuncSetAttribute(tc_rows_kernel<T, S, NB, MULTI_N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int64_t ntiles = (a.rows + kTcRows - 1) / kTcRows;
+  const int grid = (int)(ntiles < a.nsm ? ntiles : a.nsm);
+  tc_rows_kernel<T, S, NB, MULTI_N><<<grid, kTcThreads, smem, s>>>(a);
+}
+
+}  // namespace
+
+// Host: digits of B (K x N, row-major in `b`) as the kernel's shared-memory image:
+// per N block of NB columns, [K/8][S*NB][8] bf16 (slice j rows (j-1)*NB..), and
+// the per-column exponent t_n.
+template <typename T>
+void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhalf, std::vector<uint16_t> &img,
+                std::vector<int> &texp) {
+  const int W = 7 * S;
+  const int bias = sizeof(T) == 8 ? 1022 : 126;
+  img.assign((size_t)nhalf * kpad * S * NB, 0);
+  texp.assign((size_t)nhalf * NB, 0);
+  for (int n = 0; n < N; ++n) {
+    int emax = 1;
+    for (int k = 0; k < K; ++k) {
+      const double x = b[(size_t)k * N + n];
+      uint64_t bits;
+      std::memcpy(&bits, &x, 8);
+      const int e = (int)((bits >> 52) & 0x7FF);
+      emax = std::max(emax, e > 0 ? e : 1);
+    }
+    // column exponent in the output precision's convention: |B| < 2^(emax-1022)
+    texp[n] = emax - 1022;
+    (void)bias;
+    const int h = n / NB, nl = n % NB;
+    for (int k = 0; k < K; ++k) {
+      const double x = b[(size_t)k * N + n];
+      uint64_t bits;
+      std::memcpy(&bits, &x, 8);
+      const uint32_t sign = (uint32_t)(bits >> 63);
+      const int e = (int)((bits >> 52) & 0x7FF);
+      const uint64_t m = (bits & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
+      const int sh = (e > 0 ? e : 1) - emax + (W - 53);
+      const uint64_t f = sh >= 0 ? (m << sh) : (-sh >= 64 ? 0ull : (m >> (-sh)));
+      for (int j = 1; j <= S; ++j) {
+        const uint32_t dg = (uint32_t)(f >> (7 * (S - j))) & 127u;
+        float fv = (float)dg;
+        uint32_t fb;
+        std::memcpy(&fb, &fv, 4);
+        const uint16_t bf = (uint16_t)((fb >> 16) | (sign << 15));
+        const int rowi = (j - 1) * NB + nl;
+        const size_t off = (size_t)h * kpad * S * NB + (size_t)(k / 8) * (S * NB * 8) + (size_t)(rowi / 8) * 64 +
+                           (size_t)(rowi % 8) * 8 + (k % 8);
+        img[off] = bf;
+      }
+    }
+  }
+}
+
+template <typename T>
+void launch_tc_rows(const TcArgs<T> &a, int S, int NB, bool multi_n, cudaStream_t s) {
+  if constexpr (sizeof(T) == 8) {
+    if (!multi_n) launchRows<T, 8, 32, false>(a, s);
+    else launchRows<T, 8, 64, true>(a, s);
+  } else {
+    if (!multi_n) launchRows<T, 4, 32, false>(a, s);
+    else launchRows<T, 4, 128, true>(a, s);
+  }
+  (void)S;
+  (void)NB;
+}
+
+template void tc_build_b<double>(const double *, int, int, int, int, int, int, std::vector<uint16_t> &, std::vector<int> &);
+template void tc_build_b<float>(const double *, int, int, int, int, int, int, std::vector<uint16_t> &, std::vector<int> &);
+template void launch_tc_rows<double>(const TcArgs<double> &, int, int, bool, cudaStream_t);
+template void launch_tc_rows<float>(const TcArgs<float> &, int, int, bool, cudaStream_t);
+
+}  // namespace kgb

@@ -74,6 +74,33 @@ def test_ltimes_lplustimes(oracle, kgb, layout):
     check(ctx.download("rhs"), p.get("rhs"), 1e-13)
 
 
+@pytest.mark.parametrize("tensor", [1, 0])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_moment_transforms_wide_range(oracle, kgb, tensor, precision):
+    """LTimes / LPlusTimes on signed values spanning 30 decades, zero rows and partial tiles,
+    through the tensor-core digit path (1) and the SIMT path (0)."""
+    p, ctx = pair(oracle, kgb, precision=precision, quad=(8, 16), legendre=4, zones=(7, 5, 3), groups=5)
+    ctx.set_option("moments_tensor", tensor)
+    rng = np.random.default_rng(11)
+    n = ctx.field_bytes("psi") // 8
+    psi = rng.standard_normal(n) * 10.0 ** rng.uniform(-30 if precision == 0 else -12, 3, n)
+    psi[: n // 7] = 0.0
+    p.set("psi", psi); ctx.upload("psi", psi)
+    p.kconst("phi", 0.0); ctx.fill("phi", 0.0)
+    p.ltimes(); ctx.ltimes()
+    want, got = p.get("phi"), ctx.download("phi")
+    tol = 1e-13 if precision == 0 else 2e-6
+    scale = np.abs(want).max()
+    assert np.max(np.abs(got - want)) <= tol * scale
+    m = ctx.field_bytes("phi_out") // 8
+    phi_out = rng.standard_normal(m) * 10.0 ** rng.uniform(-20 if precision == 0 else -8, 2, m)
+    p.set("phi_out", phi_out); ctx.upload("phi_out", phi_out)
+    p.kconst("rhs", 0.0); ctx.fill("rhs", 0.0)
+    p.lplustimes(); ctx.lplustimes()
+    want, got = p.get("rhs"), ctx.download("rhs")
+    assert np.max(np.abs(got - want)) <= tol * np.abs(want).max()
+
+
 @pytest.mark.parametrize("scatter,gset", [(0, 1), (1, 1), (1, 4)])
 def test_scattering_and_source(oracle, kgb, scatter, gset):
     p, ctx = pair(oracle, kgb, scatter=scatter, gset=gset, groups=8, legendre=3, geometry=1, zones=(8, 6, 7))
