@@ -192,6 +192,9 @@ def run_gpu(args, world, rank, local):
         w["zones"] = (args.zones, args.zones, args.zones)
     ctx = abi.Context(local)
     inp = ctx.generate(precision=precision, **w)
+    for kv in args.option:
+        k, v = kv.split("=")
+        ctx.set_option(k, int(v))
     stream = torch.cuda.Stream(device=local)
     ctx.set_stream(stream.cuda_stream)
     U = unknowns(w)
@@ -200,6 +203,8 @@ def run_gpu(args, world, rank, local):
     ctx.fill("psi", 0.0)
     ctx.iterate(want_population=False)
     tuned = ctx.autotune() if not args.no_autotune else None
+    active = {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "sweep_reciprocals_active",
+                                             "moments_tensor_ltimes", "moments_tensor_lplustimes")}
 
     # warm-up (the solve starts from psi = 0, like SteadyStateSolver)
     ctx.fill("psi", 0.0)
@@ -296,7 +301,8 @@ def run_gpu(args, world, rank, local):
         "config": {"workload": WORKLOAD_NAME if not args.zones else WORKLOAD_NAME.replace("64^3", "%d^3" % args.zones),
                    "precision": args.precision, "unknowns": U,
                    "l2": "inputs larger than L2 (psi, rhs 17.2 GB each); no flush",
-                   "parallelism": "replicas" if world > 1 else "1 GPU", "autotuned": tuned},
+                   "parallelism": "replicas" if world > 1 else "1 GPU", "autotuned": tuned,
+                   "kernels": active},
         "roofline": roof,
         "kernel_ms_per_step": {f: fam[f][0] / args.steps for f in fam},
         "kernel_share": {f: shares[f] / total for f in shares},
@@ -326,6 +332,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default sweep tile shape")
+    ap.add_argument("--option", action="append", default=[], metavar="KEY=VALUE",
+                    help="kgb_set_option knob applied before autotuning (repeatable)")
     ap.add_argument("--zones", type=int, default=0, help="override zones per axis (profiling on a smaller case)")
     args = ap.parse_args()
     world, rank, local = dist_init()

@@ -176,12 +176,18 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * (FP64 on a uniform mesh: 1 = tabulate 1/denominator per (sigt value,
  * direction), the default; 0 = divide in every cell); "moments_tensor" (1 = LTimes
  * and LPlusTimes on the tensor cores with exact digit products when the shapes
- * fit, the default; 0 = SIMT kernels). */
+ * fit; 0 = SIMT kernels; default: tensor for FP64, SIMT for the mixed form). */
 int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
-/* Sweep autotuner: times every tile shape (footprint 4x4, 4x2, 2x2 x depth
- * 2, 4, 8, 16 zones) on this problem with CUDA events, keeps the fastest and
- * returns its sweep time (best_ms), footprint (as 44/42/22) and depth.  It
- * sweeps the current rhs, so psi and the planes are overwritten. */
+/* Current value of a knob: the keys above, plus "moments_tensor_ltimes" and
+ * "moments_tensor_lplustimes" (1 when that transform runs on the tensor cores)
+ * and "sweep_reciprocals_active" (1 when the sweep uses tabulated reciprocals). */
+int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value);
+/* Autotuner: times every sweep tile shape (footprint 4x4, 4x2, 2x2 x depth
+ * 2, 4, 8, 16 zones) and both LTimes / LPlusTimes paths (tensor-core digit
+ * products or SIMT) on this problem with CUDA events, keeps the fastest and
+ * returns the sweep time (best_ms), footprint (as 44/42/22) and depth.  It
+ * sweeps the current rhs and recomputes phi and rhs: psi, phi, rhs and the
+ * planes are overwritten. */
 int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_z);
 /* Device time in milliseconds of the named kernel family accumulated since the
  * last reset ("sweep", "ltimes", "lplustimes", "scattering", "population");

@@ -25,7 +25,7 @@ EXPORTS = (
     "kgb_lplustimes", "kgb_scattering", "kgb_source", "kgb_sweep_subdomain", "kgb_sweep_solver",
     "kgb_population", "kgb_balance", "kgb_solve", "kgb_iterate", "kgb_sync", "kgb_set_stream",
     "kgb_set_option", "kgb_set_timing", "kgb_kernel_time", "kgb_reset_timers", "kgb_default_input",
-    "kgb_generate", "kgb_launch_count", "kgb_population_noalloc", "kgb_autotune",
+    "kgb_generate", "kgb_launch_count", "kgb_population_noalloc", "kgb_autotune", "kgb_get_option",
 )
 
 INT_FIELDS = ("quadrature/id", "quadrature/jd", "quadrature/kd", "zone_to_mixelem", "zone_to_num_mixelem",
@@ -137,6 +137,7 @@ def load():
         "kgb_sync": ([P], I),
         "kgb_set_stream": ([P, P], I),
         "kgb_set_option": ([P, ctypes.c_char_p, I64], I),
+        "kgb_get_option": ([P, ctypes.c_char_p, ctypes.POINTER(I64)], I),
         "kgb_set_timing": ([P, I], I),
         "kgb_kernel_time": ([P, ctypes.c_char_p, ctypes.POINTER(D), ctypes.POINTER(I64)], I),
         "kgb_reset_timers": ([P], I),
@@ -288,6 +289,11 @@ class Context:
     def set_option(self, key, value):
         self._check(self.lib.kgb_set_option(self.h, key.encode(), int(value)), "kgb_set_option(%s)" % key)
 
+    def get_option(self, key):
+        v = ctypes.c_int64()
+        self._check(self.lib.kgb_get_option(self.h, key.encode(), ctypes.byref(v)), "kgb_get_option(%s)" % key)
+        return v.value
+
     def set_timing(self, on=True):
         self._check(self.lib.kgb_set_timing(self.h, 1 if on else 0), "kgb_set_timing")
 
@@ -302,7 +308,9 @@ class Context:
         ms, xy, tz = ctypes.c_double(), ctypes.c_int32(), ctypes.c_int32()
         self._check(self.lib.kgb_autotune(self.h, ctypes.byref(ms), ctypes.byref(xy), ctypes.byref(tz)),
                     "kgb_autotune")
-        return {"sweep_ms": ms.value, "sweep_tile_xy": xy.value, "sweep_tile_z": tz.value}
+        return {"sweep_ms": ms.value, "sweep_tile_xy": xy.value, "sweep_tile_z": tz.value,
+                "ltimes_tensor": self.get_option("moments_tensor_ltimes"),
+                "lplustimes_tensor": self.get_option("moments_tensor_lplustimes")}
 
     def launch_count(self):
         n = ctypes.c_int64()

@@ -147,6 +147,7 @@ struct kgb_ctx {
   // tensor-core moment transforms (tc_moments.cu)
   bool allow_tc = true;
   bool tc_lt = false, tc_lp = false;        // LTimes / LPlusTimes planned for the tensor cores
+  bool use_tc_lt = true, use_tc_lp = true;  // autotuner's choice between tensor and SIMT paths
   uint16_t *tc_lt_img = nullptr, *tc_lp_img = nullptr;
   int *tc_lt_exp = nullptr, *tc_lp_exp = nullptr;
   int tc_lt_kpad = 0, tc_lp_nhalf = 0;
@@ -850,7 +851,7 @@ void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, i
 int doLTimes(kgb_ctx *ctx, bool acc) {
   FamScope fs(ctx, "ltimes");
   const int64_t rows = ctx->Z * ctx->G;
-  if (ctx->tc_lt) {
+  if (ctx->tc_lt && ctx->use_tc_lt) {
     if (ctx->prec == KGB_FP64)
       tcRows<double>(ctx, as<double>(ctx->psi), as<double>(ctx->phi), ctx->D, ctx->M, ctx->D, ctx->tc_lt_kpad, ctx->M, 1,
                      ctx->tc_lt_img, ctx->tc_lt_exp, acc, false);
@@ -871,7 +872,7 @@ int doLTimes(kgb_ctx *ctx, bool acc) {
 int doLPlusTimes(kgb_ctx *ctx, bool acc) {
   FamScope fs(ctx, "lplustimes");
   const int64_t rows = ctx->Z * ctx->G;
-  if (ctx->tc_lp) {
+  if (ctx->tc_lp && ctx->use_tc_lp) {
     if (ctx->prec == KGB_FP64)
       tcRows<double>(ctx, as<double>(ctx->phi_out), as<double>(ctx->rhs), ctx->M, ctx->D, ctx->M, 32, ctx->D,
                      ctx->tc_lp_nhalf, ctx->tc_lp_img, ctx->tc_lp_exp, acc, true);
@@ -1017,6 +1018,9 @@ int kgb_setup(kgb_ctx *ctx, const kgb_dims *d) {
   ctx->dims = *d;
   ctx->prec = d->precision;
   ctx->tsz = ctx->prec == KGB_FP64 ? 8 : 4;
+  // measured defaults: the digit-product tensor path wins for FP64, SIMT for the mixed form;
+  // kgb_autotune re-measures both on the actual problem
+  ctx->use_tc_lt = ctx->use_tc_lp = ctx->prec == KGB_FP64;
   ctx->dc.SP = d->num_groupsets;
   ctx->dc.SQ = d->num_dirsets;
   ctx->dc.Sx = d->num_zonesets[0];
@@ -1514,6 +1518,7 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
   }
   if (!std::strcmp(key, "moments_tensor")) {
     ctx->allow_tc = value != 0;
+    ctx->use_tc_lt = ctx->use_tc_lp = value != 0;
     ctx->dirty_ell = true;
     return KGB_OK;
   }
@@ -1567,9 +1572,47 @@ int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_
   ctx->ty = bxy % 10;
   ctx->tz = btz;
   if ((rc = buildTiles(ctx))) return rc;
+  // moment transforms: tensor-core digit products or SIMT, whichever is faster here
+  cudaEvent_t f0, f1;
+  CK(cudaEventCreate(&f0));
+  CK(cudaEventCreate(&f1));
+  auto timeIt = [&](bool lt, bool tc, float &ms) -> int {
+    bool &flag = lt ? ctx->use_tc_lt : ctx->use_tc_lp;
+    flag = tc;
+    int r = lt ? doLTimes(ctx, false) : doLPlusTimes(ctx, false);  // warm-up
+    if (r) return r;
+    CK(cudaEventRecord(f0, ctx->stream));
+    for (int k = 0; k < 2 && !r; ++k) r = lt ? doLTimes(ctx, false) : doLPlusTimes(ctx, false);
+    CK(cudaEventRecord(f1, ctx->stream));
+    CK(cudaEventSynchronize(f1));
+    CK(cudaEventElapsedTime(&ms, f0, f1));
+    return r ? r : checkDeviceError(ctx);
+  };
+  for (int lt = 1; lt >= 0 && !rc; --lt) {
+    if (!(lt ? ctx->tc_lt : ctx->tc_lp)) continue;
+    float t_tc = 0.f, t_simt = 0.f;
+    if ((rc = timeIt(lt, true, t_tc)) || (rc = timeIt(lt, false, t_simt))) break;
+    (lt ? ctx->use_tc_lt : ctx->use_tc_lp) = t_tc <= t_simt;
+  }
+  cudaEventDestroy(f0);
+  cudaEventDestroy(f1);
+  if (rc) return rc;
   if (best_ms) *best_ms = best;
   if (tile_xy) *tile_xy = bxy;
   if (tile_z) *tile_z = btz;
+  return KGB_OK;
+}
+
+int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
+  if (!ctx || !key || !value) return KGB_ERR_ARG;
+  if (!std::strcmp(key, "sweep_tile_z")) *value = ctx->tz;
+  else if (!std::strcmp(key, "sweep_tile_xy")) *value = ctx->tx * 10 + ctx->ty;
+  else if (!std::strcmp(key, "sweep_reciprocals")) *value = ctx->allow_recip ? 1 : 0;
+  else if (!std::strcmp(key, "sweep_reciprocals_active")) *value = ctx->use_recip ? 1 : 0;
+  else if (!std::strcmp(key, "moments_tensor")) *value = ctx->allow_tc ? 1 : 0;
+  else if (!std::strcmp(key, "moments_tensor_ltimes")) *value = (ctx->tc_lt && ctx->use_tc_lt) ? 1 : 0;
+  else if (!std::strcmp(key, "moments_tensor_lplustimes")) *value = (ctx->tc_lp && ctx->use_tc_lp) ? 1 : 0;
+  else return fail(ctx, KGB_ERR_ARG, std::string("unknown option '") + key + "'");
   return KGB_OK;
 }
 

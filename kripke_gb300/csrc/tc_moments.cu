@@ -31,8 +31,10 @@
 // Shared-memory operand layout: K-major, no swizzle ("interleaved" core
 // matrices of 8 rows x 16 bytes; core matrices adjacent in K are LBO bytes
 // apart, adjacent 8-row groups SBO = 128 bytes apart).  One CTA per SM
-// (persistent over 128-row tiles); all 128 threads split rows and run the
-// epilogue (thread t owns row t = TMEM lane t), thread 0 issues the MMAs.  The
+// (persistent over 128-row tiles) of 16 warps: four threads split each row
+// (one 8-element K group of every 32-element chunk each), and in the epilogue
+// warp w reads TMEM lane quarter w%4 (rows 32*(w%4)..) for column group w/4;
+// thread 0 issues the MMAs.  The
 // B image reaches shared memory with one cp.async.bulk.  Every mbarrier wait is
 // bounded; on timeout the CTA records the failure, releases its tensor memory
 // and returns.
@@ -47,7 +49,7 @@ namespace kgb {
 
 namespace {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 512;     // 16 warps: 4 threads per row while splitting
 constexpr int kTcRows = 128;            // rows per tile = MMA M
 constexpr int kTcChunk = 32;            // K elements staged per A buffer
 constexpr uint32_t kWaitLimit = 1u << 24;  // mbarrier polls before giving up
@@ -149,17 +151,33 @@ __device__ __forceinline__ float scale2(float x, int e) {
 
 // Combine the S diagonal sums (FP32, exact integers) into the output value.
 template <typename T, int S> struct Combine;
+// Exact double of sign*a*2^sh for 0 < a < 2^53, assembled from its bits (no
+// FP64 instruction); `ok` is cleared when the result is not a normal number.
+__device__ __forceinline__ double exactDouble(long long v, int sh, bool &ok) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = v < 0 ? 1ull : 0ull;
+  const unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+  const int p = 63 - __clzll((long long)a);
+  const int e = p + sh + 1023;
+  if (e < 1 || e > 2046) ok = false;
+  const unsigned long long mant = (a << (52 - p)) & 0xFFFFFFFFFFFFFull;
+  return __longlong_as_double((long long)((sgn << 63) | ((unsigned long long)(e & 0x7FF) << 52) | mant));
+}
+
 template <> struct Combine<double, 8> {
-  // rowexp + colexp = s_r + t_n; value = (H*2^28 + L) * 2^(s_r + t_n - 63)
+  // value = (H*2^28 + L) * 2^(e0 - 63) with H, L below 2^47: both terms are
+  // exact doubles, so the one addition is the only rounding
   static __device__ __forceinline__ double value(const float (&dk)[8], int e0) {
     long long h = 0, l = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) h = h * 128 + (long long)__float2int_rn(dk[k]);
 #pragma unroll
     for (int k = 4; k < 8; ++k) l = l * 128 + (long long)__float2int_rn(dk[k]);
-    // h*2^28 + l is exact in 128 bits; the sum below rounds once
-    const double hs = scale2((double)h, 28);
-    return scale2(hs + (double)l, e0 - 63);
+    bool ok = true;
+    const double hs = exactDouble(h, e0 - 35, ok);
+    const double ls = exactDouble(l, e0 - 63, ok);
+    if (ok) return hs + ls;
+    return scale2(scale2((double)h, 28) + (double)l, e0 - 63);  // outside the normal range
   }
 };
 template <> struct Combine<float, 4> {
@@ -178,9 +196,17 @@ template <> struct TcBias<float> { static constexpr int v = 126; };
 template <typename T, int S, int NB, bool MULTI_N>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ uint64_t bars[3];  // 0,1: A buffers (MMA done), 2: B image load / per-half MMA done
+  __shared__ uint64_t bars[3];  // 0,1: A buffers (MMA done), 2: B image load / per-block MMA done
   __shared__ uint32_t tmem_slot;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  __shared__ int row_emax[kTcRows];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // split phase: 4 threads per row, part p owns the 8-element K group p of every 32-element chunk
+  const int srow = warp * 8 + (lane & 7);
+  const int part = lane >> 3;
+  // epilogue phase: warp w reads TMEM lane quarter w%4 and column group w/4
+  const int erow = (warp & 3) * 32 + lane;
+  const int cgrp = warp >> 2;
+  constexpr int kCols = NB / 4;      // columns per epilogue column group
   constexpr int kTmemCols = S * NB;  // power of two: 128, 256 or 512
   constexpr uint32_t kSliceBytes = kTcChunk * kTcRows * 2;  // one digit slice of one chunk: 8 KB
   constexpr uint32_t kBufBytes = S * kSliceBytes;
@@ -222,15 +248,47 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
 
   const int ntiles = (int)((a.rows + kTcRows - 1) / kTcRows);
   const int nchunks = a.kpad / kTcChunk;
+  const bool vec = (a.lda * sizeof(T)) % 16 == 0;  // 16-byte loads of row segments
   uint32_t item = 0;
   for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-    const int64_t row = (int64_t)tile * kTcRows + tid;
+    const int64_t row = (int64_t)tile * kTcRows + srow;
     const bool valid = row < a.rows;
     const T *arow = a.A + row * a.lda;
-    // row exponent: largest biased exponent of the row (0 for an all-zero row)
+    // row exponent: largest biased exponent of the row, over the 4 threads of the row
     int emax = 1;
-    if (valid)
-      for (int k = 0; k < a.K; ++k) emax = max(emax, expOf(arow[k]));
+    if (valid) {
+      if (vec && a.K % kTcChunk == 0) {
+        // all of this thread's K groups at once (independent 16-byte loads)
+#pragma unroll 4
+        for (int c = 0; c < nchunks; ++c) {
+          const T *p8 = arow + c * kTcChunk + part * 8;
+          if constexpr (sizeof(T) == 8) {
+            double2 v[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) v[e] = *reinterpret_cast<const double2 *>(p8 + 2 * e);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) emax = max(emax, max(expOf(v[e].x), expOf(v[e].y)));
+          } else {
+            float4 v[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) v[e] = *reinterpret_cast<const float4 *>(p8 + 4 * e);
+#pragma unroll
+            for (int e = 0; e < 2; ++e)
+              emax = max(emax, max(max(expOf(v[e].x), expOf(v[e].y)), max(expOf(v[e].z), expOf(v[e].w))));
+          }
+        }
+      } else {
+        for (int c = 0; c < nchunks; ++c) {
+          const int k0 = c * kTcChunk + part * 8;
+#pragma unroll
+          for (int e = 0; e < 8; ++e)
+            if (k0 + e < a.K) emax = max(emax, expOf(arow[k0 + e]));
+        }
+      }
+    }
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 8));
+    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 16));
+    if (part == 0) row_emax[srow] = emax;
 
     for (int c = 0; c < nchunks && ok; ++c, ++item) {
       const int b = MULTI_N ? 0 : (int)(item & 1);
@@ -239,33 +297,48 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
         if (!ok) break;
       }
       unsigned char *buf = sA + b * kBufBytes;
-      // split this chunk of the row into S digit slices (thread = row: 4 core-matrix rows per slice)
-#pragma unroll 1
-      for (int q = 0; q < kTcChunk / 8; ++q) {
-        uint32_t w[S][4];
+      // this thread's 8 elements of the chunk, split into S digit slices
+      const int k0 = c * kTcChunk + part * 8;
+      T x[8];
+      if (valid && vec && k0 + 8 <= a.K) {
+        if constexpr (sizeof(T) == 8) {
 #pragma unroll
-        for (int e = 0; e < 8; e += 2) {
-          uint32_t d0[S], d1[S];
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int k = c * kTcChunk + q * 8 + e + h;
-            uint32_t sign = 0;
-            uint64_t f = 0;
-            if (valid && k < a.K) f = Fixed<T, S>::mag(arow[k], emax, sign);
-#pragma unroll
-            for (int i = 0; i < S; ++i) {
-              const uint32_t dg = (uint32_t)(f >> (7 * (S - 1 - i))) & 127u;
-              (h ? d1 : d0)[i] = digitBf16(dg, sign);
-            }
+          for (int e = 0; e < 8; e += 2) {
+            const double2 v = *reinterpret_cast<const double2 *>(arow + k0 + e);
+            x[e] = v.x;
+            x[e + 1] = v.y;
           }
+        } else {
 #pragma unroll
-          for (int i = 0; i < S; ++i) w[i][e >> 1] = d0[i] | (d1[i] << 16);
+          for (int e = 0; e < 8; e += 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(arow + k0 + e);
+            x[e] = v.x;
+            x[e + 1] = v.y;
+            x[e + 2] = v.z;
+            x[e + 3] = v.w;
+          }
         }
-        const uint32_t off = q * kLboA + (tid >> 3) * 128 + (tid & 7) * 16;
+      } else {
 #pragma unroll
-        for (int i = 0; i < S; ++i)
-          *reinterpret_cast<uint4 *>(buf + i * kSliceBytes + off) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+        for (int e = 0; e < 8; ++e) x[e] = (valid && k0 + e < a.K) ? arow[k0 + e] : T(0);
       }
+      uint32_t w[S][4];
+#pragma unroll
+      for (int e = 0; e < 8; e += 2) {
+        uint32_t s0, s1;
+        const uint64_t f0 = Fixed<T, S>::mag(x[e], emax, s0);
+        const uint64_t f1 = Fixed<T, S>::mag(x[e + 1], emax, s1);
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+          const uint32_t g0 = (uint32_t)(f0 >> (7 * (S - 1 - i))) & 127u;
+          const uint32_t g1 = (uint32_t)(f1 >> (7 * (S - 1 - i))) & 127u;
+          w[i][e >> 1] = digitBf16(g0, s0) | (digitBf16(g1, s1) << 16);
+        }
+      }
+      const uint32_t off = part * kLboA + (srow >> 3) * 128 + (srow & 7) * 16;
+#pragma unroll
+      for (int i = 0; i < S; ++i)
+        *reinterpret_cast<uint4 *>(buf + i * kSliceBytes + off) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
       asm volatile("fence.proxy.async.shared::cta;");
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncthreads();
@@ -280,10 +353,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
             const int kg = c * (kTcChunk / 16) + ks;  // global 16-element K step
             const uint64_t da = matDesc(smemAddr(buf + (i - 1) * kSliceBytes + ks * 2 * kLboA), kLboA, 128);
             for (int n0 = 0; n0 < ncols; n0 += 256) {
-              const int w = min(256, ncols - n0);
+              const int wd = min(256, ncols - n0);
               const uint64_t db = matDesc(smemAddr(sB) + kg * 2 * lboB + (n0 / 8) * 128, lboB, 128);
               // slice 1's first MMA initialises every diagonal block; all later ones accumulate
-              mma(tmem + (uint32_t)((i - 1) * NB + n0), da, db, instrDesc(w), (c > 0 || ks > 0 || i > 1) ? 1u : 0u);
+              mma(tmem + (uint32_t)((i - 1) * NB + n0), da, db, instrDesc(wd), (c > 0 || ks > 0 || i > 1) ? 1u : 0u);
             }
           }
         }
@@ -293,7 +366,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
     }
     if (!ok) break;
 
-    // --- epilogue(s) ---
+    // --- epilogue(s): thread = (row erow, column group cgrp) ---
+    const int64_t orow = (int64_t)tile * kTcRows + erow;
+    const bool ovalid = orow < a.rows;
+    const int oemax = row_emax[erow] - TcBias<T>::v;
+    T *crow = a.C + orow * a.ldc;
     for (int hf = 0; hf < a.nhalf && ok; ++hf) {
       if (MULTI_N) {
         if (tid == 0) {
@@ -305,9 +382,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
             for (int ks = 0; ks < a.kpad / 16; ++ks) {
               const uint64_t da = matDesc(smemAddr(sA + (i - 1) * kSliceBytes + ks * 2 * kLboA), kLboA, 128);
               for (int n0 = 0; n0 < ncols; n0 += 256) {
-                const int w = min(256, ncols - n0);
+                const int wd = min(256, ncols - n0);
                 const uint64_t db = matDesc(smemAddr(bh) + ks * 2 * lboB + (n0 / 8) * 128, lboB, 128);
-                mma(tmem + (uint32_t)((i - 1) * NB + n0), da, db, instrDesc(w), (ks > 0 || i > 1) ? 1u : 0u);
+                mma(tmem + (uint32_t)((i - 1) * NB + n0), da, db, instrDesc(wd), (ks > 0 || i > 1) ? 1u : 0u);
               }
             }
           }
@@ -321,25 +398,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
       }
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t lane = (uint32_t)(warp * 32) << 16;
-      T *crow = a.C + row * a.ldc;
+      const uint32_t lanebase = (uint32_t)((warp & 3) * 32) << 16;
 #pragma unroll 1
-      for (int c0 = 0; c0 < NB; c0 += 8) {
+      for (int c0 = cgrp * kCols; c0 < (cgrp + 1) * kCols; c0 += 8) {
         uint32_t v[S][8];
 #pragma unroll
-        for (int k = 0; k < S; ++k) ld8(tmem + lane + (uint32_t)(k * NB + c0), v[k]);
+        for (int k = 0; k < S; ++k) ld8(tmem + lanebase + (uint32_t)(k * NB + c0), v[k]);
         asm volatile("tcgen05.wait::ld.sync.aligned;");
+        T out[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
           const int n = hf * NB + c0 + u;
           float dk[S];
 #pragma unroll
           for (int k = 0; k < S; ++k) dk[k] = __uint_as_float(v[k][u]);
-          if (valid && n < a.N) {
-            const int e0 = (emax - TcBias<T>::v) + sT[n];
-            const T val = Combine<T, S>::value(dk, e0);
-            crow[n] = a.accumulate ? crow[n] + val : val;
-          }
+          out[u] = n < a.N ? Combine<T, S>::value(dk, oemax + sT[n]) : T(0);
+        }
+        if (ovalid) {
+          const int nb = hf * NB + c0;
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (nb + u < a.N) crow[nb + u] = a.accumulate ? crow[nb + u] + out[u] : out[u];
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
