@@ -198,6 +198,60 @@ int kgb_reset_timers(kgb_ctx *ctx);
 /* Number of kernels this context has launched since it was created. */
 int kgb_launch_count(kgb_ctx *ctx, int64_t *out);
 
+/* --- converged solves, the adjoint and gradients ------------------------
+ * No counterpart in the reference, whose SteadyStateSolver
+ * (src/Kripke/SteadyStateSolver.cpp:24-115) runs a fixed iteration count;
+ * these solve to a tolerance and differentiate a response at the fixed point.
+ * Response: R = sum_z det(z) volume(z) sum_g siga(g,z) sum_d w(d) psi(d,g,z),
+ * the absorption rate in a detector region, with siga(g,z) = sigt_zonal(g,z)
+ * - sum over the zone's mix elements of fraction * sum_g' sigs(mat,0,g',g).
+ * The adjoint iteration is the forward one with L and L+ exchanged, the
+ * scattering transposed over groups and every direction swept in the
+ * reversed orientation; its state lives beside psi, which it leaves alone
+ * (phi, phi_out, rhs and the planes are scratch for either solve). */
+
+/* The generator's material cross sections for `in` (kgb_generate uses the
+ * same): sigt [3][G] per (material, group), and the scattering tables
+ * sigs [3][L+1][G][G] indexed (material, Legendre order, destination group,
+ * source group).  Either output may be NULL. */
+int kgb_material_tables(const kgb_input *in, double *sigt, double *sigs);
+/* Sets the cross sections from per-material tables: sigt [3][G] rebuilds
+ * sigt_zonal through the uploaded mix elements (sum of fraction * sigma_t in
+ * mix order, like the generator); sigs [3][L+1][G][G] replaces data/sigs.
+ * NULL leaves that table unchanged. */
+int kgb_set_materials(kgb_ctx *ctx, const double *sigt, const double *sigs);
+/* Detector weights det(z), z = (k*ny + j)*nx + i over the whole mesh (n must
+ * be nx*ny*nz); NULL = 1 everywhere (the default). */
+int kgb_set_response(kgb_ctx *ctx, const double *det, int64_t n);
+/* Source iterations from psi = 0 until moment 0 of successive iterates
+ * satisfies max|phi_k - phi_(k-1)| <= tol * max|phi_k|, or max_iter
+ * iterations ran.  *iters and *change (either may be NULL) receive the count
+ * and the last relative change; reaching max_iter is not an error. */
+int kgb_solve_converged(kgb_ctx *ctx, double source_strength, double tol, int32_t max_iter, int32_t *iters,
+                        double *change);
+/* The adjoint source iteration for the response, from a zero state, with the
+ * same stopping rule.  Needs ell(0,d) proportional to w(d) (true for the
+ * reference's L); KGB_ERR_ARG otherwise. */
+int kgb_adjoint_solve(kgb_ctx *ctx, double tol, int32_t max_iter, int32_t *iters, double *change);
+/* R at the current psi. */
+int kgb_response(kgb_ctx *ctx, double *response);
+/* R and its gradients at the current psi and adjoint state: dsigt [3][G]
+ * with respect to sigma_t of (material, group), dsigs [3][G] with respect to
+ * the isotropic in-group scattering sigs(material, 0, g, g), dq with respect
+ * to the source strength.  Exact for converged psi and adjoint; KGB_ERR_STATE
+ * when no adjoint solve ran since the inputs last changed.  Outputs may be
+ * NULL. */
+int kgb_gradient(kgb_ctx *ctx, double *response, double *dsigt, double *dsigs, double *dq);
+/* Unrolled (checkpoint) mode: R after exactly niter source iterations from
+ * psi = 0 -- SteadyStateSolver's fixed count -- and its exact gradients, by
+ * reverse mode through the iterations.  Forward iterates are checkpointed
+ * every `stride` iterations (<= 0: ceil(sqrt(niter))) and recomputed one
+ * segment at a time in the reverse pass, holding niter/stride + stride - 1
+ * extra psi-sized buffers (stride 1 stores every iterate and recomputes
+ * none).  Leaves psi at the niter-th iterate; the adjoint state is scratch. */
+int kgb_gradient_unrolled(kgb_ctx *ctx, int32_t niter, double source_strength, int32_t stride, double *response,
+                          double *dsigt, double *dsigs, double *dq);
+
 /* Allocation-free population edit.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory at the point they
  * need the particle count -- code recorded into a CUDA graph, frameworks that

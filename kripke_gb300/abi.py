@@ -26,6 +26,8 @@ EXPORTS = (
     "kgb_population", "kgb_balance", "kgb_solve", "kgb_iterate", "kgb_sync", "kgb_set_stream",
     "kgb_set_option", "kgb_set_timing", "kgb_kernel_time", "kgb_reset_timers", "kgb_default_input",
     "kgb_generate", "kgb_launch_count", "kgb_population_noalloc", "kgb_autotune", "kgb_get_option",
+    "kgb_material_tables", "kgb_set_materials", "kgb_set_response", "kgb_solve_converged", "kgb_adjoint_solve",
+    "kgb_response", "kgb_gradient", "kgb_gradient_unrolled",
 )
 
 INT_FIELDS = ("quadrature/id", "quadrature/jd", "quadrature/kd", "zone_to_mixelem", "zone_to_num_mixelem",
@@ -147,6 +149,15 @@ def load():
         "kgb_autotune": ([P, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)], I),
         "kgb_population_noalloc": ([P, P, P, I64, ctypes.c_int32, ctypes.c_int32, P, P, ctypes.c_char_p,
                                     ctypes.c_int32], I),
+        "kgb_material_tables": ([ctypes.POINTER(KgbInput), P, P], I),
+        "kgb_set_materials": ([P, P, P], I),
+        "kgb_set_response": ([P, P, I64], I),
+        "kgb_solve_converged": ([P, D, D, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(D)], I),
+        "kgb_adjoint_solve": ([P, D, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(D)], I),
+        "kgb_response": ([P, ctypes.POINTER(D)], I),
+        "kgb_gradient": ([P, ctypes.POINTER(D), P, P, ctypes.POINTER(D)], I),
+        "kgb_gradient_unrolled": ([P, ctypes.c_int32, D, ctypes.c_int32, ctypes.POINTER(D), P, P,
+                                   ctypes.POINTER(D)], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -319,3 +330,68 @@ class Context:
 
     def reset_timers(self):
         self._check(self.lib.kgb_reset_timers(self.h), "kgb_reset_timers")
+
+    # --- converged solves, the adjoint and gradients -----------------------
+    def set_materials(self, sigt=None, sigs=None):
+        """Cross sections from per-material tables: sigt [3][G], sigs [3][L+1][G][G] (dest, source)."""
+        a = None if sigt is None else np.ascontiguousarray(sigt, dtype=np.float64).ravel()
+        b = None if sigs is None else np.ascontiguousarray(sigs, dtype=np.float64).ravel()
+        self._check(self.lib.kgb_set_materials(self.h, None if a is None else a.ctypes.data,
+                                               None if b is None else b.ctypes.data), "kgb_set_materials")
+
+    def set_response(self, det=None):
+        """Detector weights per zone, z = (k*ny + j)*nx + i; None = the whole domain."""
+        if det is None:
+            self._check(self.lib.kgb_set_response(self.h, None, 0), "kgb_set_response")
+            return
+        a = np.ascontiguousarray(det, dtype=np.float64).ravel()
+        self._check(self.lib.kgb_set_response(self.h, a.ctypes.data, a.size), "kgb_set_response")
+
+    def solve_converged(self, source_strength=1.0, tol=1e-12, max_iter=1000):
+        it, ch = ctypes.c_int32(), ctypes.c_double()
+        self._check(self.lib.kgb_solve_converged(self.h, float(source_strength), float(tol), int(max_iter),
+                                                 ctypes.byref(it), ctypes.byref(ch)), "kgb_solve_converged")
+        return it.value, ch.value
+
+    def adjoint_solve(self, tol=1e-12, max_iter=1000):
+        it, ch = ctypes.c_int32(), ctypes.c_double()
+        self._check(self.lib.kgb_adjoint_solve(self.h, float(tol), int(max_iter), ctypes.byref(it),
+                                               ctypes.byref(ch)), "kgb_adjoint_solve")
+        return it.value, ch.value
+
+    def response(self):
+        v = ctypes.c_double()
+        self._check(self.lib.kgb_response(self.h, ctypes.byref(v)), "kgb_response")
+        return v.value
+
+    def gradient(self):
+        """(R, dR/dsigt [3][G], dR/dsigs in-group P0 [3][G], dR/dq) at the current psi and adjoint."""
+        G = self.dims.num_groups if self.dims is not None else self.inp.num_groups
+        r, q = ctypes.c_double(), ctypes.c_double()
+        dt = np.zeros((3, G))
+        ds = np.zeros((3, G))
+        self._check(self.lib.kgb_gradient(self.h, ctypes.byref(r), dt.ctypes.data, ds.ctypes.data, ctypes.byref(q)),
+                    "kgb_gradient")
+        return r.value, dt, ds, q.value
+
+    def gradient_unrolled(self, niter, source_strength=1.0, stride=0):
+        """(R, dR/dsigt, dR/dsigs, dR/dq) after exactly niter iterations from psi = 0 (checkpointed reverse mode)."""
+        G = self.dims.num_groups if self.dims is not None else self.inp.num_groups
+        r, q = ctypes.c_double(), ctypes.c_double()
+        dt = np.zeros((3, G))
+        ds = np.zeros((3, G))
+        self._check(self.lib.kgb_gradient_unrolled(self.h, int(niter), float(source_strength), int(stride),
+                                                   ctypes.byref(r), dt.ctypes.data, ds.ctypes.data,
+                                                   ctypes.byref(q)), "kgb_gradient_unrolled")
+        return r.value, dt, ds, q.value
+
+
+def material_tables(inp):
+    """The generator's (sigt [3][G], sigs [3][L+1][G][G]) for a kgb_input."""
+    G, L1 = inp.num_groups, inp.legendre_order + 1
+    st = np.zeros((3, G))
+    sg = np.zeros((3, L1, G, G))
+    rc = load().kgb_material_tables(ctypes.byref(inp), st.ctypes.data, sg.ctypes.data)
+    if rc != KGB_OK:
+        raise KgbError(rc, "kgb_material_tables")
+    return st, sg

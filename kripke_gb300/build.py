@@ -32,7 +32,8 @@ NVCC_FLAGS = ARCH + [
 CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall", "-I" + os.path.join(ROOT, "include"),
              "-I" + HOST]
 
-CU_SOURCES = ["kgb_api.cu", "sweep.cu", "moments.cu", "scatter.cu", "reduce.cu", "xpose.cu", "noalloc.cu", "tc_moments.cu"]
+CU_SOURCES = ["kgb_api.cu", "sweep.cu", "moments.cu", "scatter.cu", "reduce.cu", "xpose.cu", "noalloc.cu", "tc_moments.cu",
+              "adjoint.cu"]
 CPP_SOURCES = ["generate.cpp"]
 HEADERS = ["kgb_internal.h", "kgb_layout.h"]
 

@@ -177,6 +177,47 @@ int materialAt(int geometry, double x, double y, double z) {
 
 double draw(std::mt19937_64 &r) { return (double)(r() >> 11) * 0x1.0p-53; }
 
+// Per-material cross sections of the generator: sigma_t st[m][g], the
+// isotropic in-group sigma_s ss[m][g], and the full scattering tables
+// sg[m][l][g][g'] (destination g, source g').  All random draws of the
+// generator happen here, in the documented order.
+void materialTables(const kgb_input &in, std::vector<double> &st, std::vector<double> &ss, std::vector<double> &sg) {
+  const int G = in.num_groups, L1 = in.legendre_order + 1;
+  std::mt19937_64 rng(in.seed);
+  st.assign((size_t)3 * G, 0.0);
+  ss.assign((size_t)3 * G, 0.0);
+  sg.assign((size_t)3 * L1 * G * G, 0.0);
+  for (int m = 0; m < 3; ++m)
+    for (int g = 0; g < G; ++g) {
+      double ft = 1.0, fs = 1.0;
+      if (in.perturb) {
+        ft = 1.0 + 0.2 * (2.0 * draw(rng) - 1.0);
+        fs = 1.0 + 0.2 * (2.0 * draw(rng) - 1.0);
+      }
+      st[m * G + g] = in.sigt[m] * ft;
+      ss[m * G + g] = in.sigs[m] * fs;
+    }
+  auto at = [&](int m, int l, int g, int gp) -> double & { return sg[(((size_t)m * L1 + l) * G + g) * G + gp]; };
+  if (in.scatter == 1) {
+    std::vector<double> u((size_t)G * G);
+    for (int m = 0; m < 3; ++m)
+      for (int l = 0; l < L1; ++l) {
+        std::fill(u.begin(), u.end(), 0.0);
+        for (int g = 0; g < G; ++g)
+          for (int gp = 0; gp <= g; ++gp) u[(size_t)g * G + gp] = draw(rng);
+        for (int gp = 0; gp < G; ++gp) {
+          double col = 0.0;
+          for (int g = gp; g < G; ++g) col += u[(size_t)g * G + gp];
+          const double scale = 0.5 * st[m * G + gp] / col;
+          for (int g = gp; g < G; ++g) at(m, l, g, gp) = (u[(size_t)g * G + gp] * scale) / (double)(2 * l + 1);
+        }
+      }
+  } else {
+    for (int m = 0; m < 3; ++m)
+      for (int g = 0; g < G; ++g) at(m, 0, g, g) = ss[m * G + g];
+  }
+}
+
 struct Gen {
   kgb_ctx *ctx;
   const kgb_input &in;
@@ -201,19 +242,9 @@ struct Gen {
 
   int run() {
     int rc;
-    // per-(material, group) cross sections
-    std::mt19937_64 rng(in.seed);
-    std::vector<double> st(3 * G), ss(3 * G);
-    for (int m = 0; m < 3; ++m)
-      for (int g = 0; g < G; ++g) {
-        double ft = 1.0, fs = 1.0;
-        if (in.perturb) {
-          ft = 1.0 + 0.2 * (2.0 * draw(rng) - 1.0);
-          fs = 1.0 + 0.2 * (2.0 * draw(rng) - 1.0);
-        }
-        st[m * G + g] = in.sigt[m] * ft;
-        ss[m * G + g] = in.sigs[m] * fs;
-      }
+    // per-(material, group) cross sections and scattering tables
+    std::vector<double> st, ss, sgc;
+    materialTables(in, st, ss, sgc);
 
     // --- angular data, one chunk per direction set ---
     std::vector<QPoint> pts = angularSet(in);
@@ -339,24 +370,10 @@ struct Gen {
       auto at = [&](int m, int l, int g, int gp) -> double & {
         return sg[m * sgs[0] + l * sgs[1] + g * sgs[2] + gp * sgs[3]];
       };
-      if (in.scatter == 1) {
-        std::vector<double> u((size_t)G * G);
-        for (int m = 0; m < 3; ++m)
-          for (int l = 0; l < L1; ++l) {
-            std::fill(u.begin(), u.end(), 0.0);
-            for (int g = 0; g < G; ++g)
-              for (int gp = 0; gp <= g; ++gp) u[(size_t)g * G + gp] = draw(rng);
-            for (int gp = 0; gp < G; ++gp) {
-              double col = 0.0;
-              for (int g = gp; g < G; ++g) col += u[(size_t)g * G + gp];
-              const double scale = 0.5 * st[m * G + gp] / col;
-              for (int g = gp; g < G; ++g) at(m, l, g, gp) = (u[(size_t)g * G + gp] * scale) / (double)(2 * l + 1);
-            }
-          }
-      } else {
-        for (int m = 0; m < 3; ++m)
-          for (int g = 0; g < G; ++g) at(m, 0, g, g) = ss[m * G + g];
-      }
+      for (int m = 0; m < 3; ++m)
+        for (int l = 0; l < L1; ++l)
+          for (int g = 0; g < G; ++g)
+            for (int gp = 0; gp < G; ++gp) at(m, l, g, gp) = sgc[(((size_t)m * L1 + l) * G + g) * G + gp];
       if ((rc = put("data/sigs", sg))) return rc;
     }
     return KGB_OK;
@@ -383,6 +400,15 @@ void kgb_default_input(kgb_input *in) {
   in->seed = 20261203ULL;
   in->sigt[0] = 0.1; in->sigt[1] = 0.0001; in->sigt[2] = 0.1;
   in->sigs[0] = 0.05; in->sigs[1] = 0.00005; in->sigs[2] = 0.05;
+}
+
+int kgb_material_tables(const kgb_input *in, double *sigt, double *sigs) {
+  if (!in || in->num_groups < 1 || in->legendre_order < 0 || in->scatter < 0 || in->scatter > 1) return KGB_ERR_ARG;
+  std::vector<double> st, ss, sg;
+  materialTables(*in, st, ss, sg);
+  if (sigt) std::memcpy(sigt, st.data(), st.size() * sizeof(double));
+  if (sigs) std::memcpy(sigs, sg.data(), sg.size() * sizeof(double));
+  return KGB_OK;
 }
 
 int kgb_generate(kgb_ctx *ctx, const kgb_input *in) {

@@ -227,6 +227,12 @@ void sweepSubdomain(Core::DataStore &ds, SdomId sdom_id);
 void kConst(Core::Field<double> &field, double value);
 }  // namespace Kernel
 
+// Particle count after each source iteration, at full precision (the solver's
+// printout keeps the reference's %e format).
+struct ParticleHistory : public Core::BaseVar {
+  std::vector<double> counts;
+};
+
 // src/Kripke/SweepSolver.h:20-22, SteadyStateSolver.h:18
 void SweepSolver(Core::DataStore &ds, const std::vector<SdomId> &sdom_list, bool block_jacobi);
 int SteadyStateSolver(Core::DataStore &ds, size_t max_iter, bool block_jacobi);

@@ -110,6 +110,8 @@ int SteadyStateSolver(Core::DataStore &ds, size_t max_iter, bool block_jacobi) {
   printf("\nSteady State Solve\n==================\n\n");
   auto field = [&](const char *n) -> Core::Field<double> & { return ds.getVariable<Core::Field<double>>(n); };
   Kernel::kConst(field("psi"), 0.0);
+  if (!ds.isVariableType<ParticleHistory>("particle_history")) ds.newVariable<ParticleHistory>("particle_history");
+  auto &history = ds.getVariable<ParticleHistory>("particle_history");
   double part_last = 0.0;
   for (size_t iter = 0; iter < max_iter; ++iter) {
     Kernel::kConst(field("phi"), 0.0);
@@ -128,6 +130,7 @@ int SteadyStateSolver(Core::DataStore &ds, size_t max_iter, bool block_jacobi) {
       SweepSolver(ds, list, block_jacobi);
     }
     const double part = Kernel::population(ds);
+    history.counts.push_back(part);
     printf("  iter %d: particle count=%e, change=%e\n", (int)iter, part, (part - part_last) / part);
     fflush(stdout);
     part_last = part;

@@ -200,9 +200,13 @@ int main(int argc, char **argv) {
     printf("  Grind time :        %e [(seconds/iteration)/unknowns]\n", grind_time);
     printf("  Sweep efficiency :  %4.5lf [100.0 * SweepSubdomain time / SweepSolver time]\n", sweep_eff);
     printf("  Number of unknowns: %lu\n", (unsigned long)num_unknowns);
-    if (vars.json)
-      printf("{\"throughput\": %.6e, \"grind_time\": %.6e, \"sweep_efficiency\": %.4f, \"unknowns\": %lu, \"iterations\": %lu}\n",
+    if (vars.json) {
+      printf("{\"throughput\": %.6e, \"grind_time\": %.6e, \"sweep_efficiency\": %.4f, \"unknowns\": %lu, \"iterations\": %lu, \"particle_counts\": [",
              throughput, grind_time, sweep_eff, (unsigned long)num_unknowns, (unsigned long)num_iter);
+      const auto &counts = ds.getVariable<ParticleHistory>("particle_history").counts;
+      for (size_t i = 0; i < counts.size(); ++i) printf("%s%.17g", i ? ", " : "", counts[i]);
+      printf("]}\n");
+    }
   } catch (const std::exception &e) {
     printf("ERROR: %s\n", e.what());
     return 1;

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <string>
 #include <vector>
@@ -157,6 +158,26 @@ struct kgb_ctx {
   double *pop_slots = nullptr;
   int64_t npop_slots = 0;
   double vol_uniform = 0.0;
+
+  // converged solves, the adjoint source iteration and gradients (adjoint.cu)
+  void *lam = nullptr;          // adjoint state divided by the cell volume, device nesting [Z][G][D]
+  double *phi_prev = nullptr;   // moment 0 of the previous iterate [Z][G] (convergence test)
+  void *sigsT_adj = nullptr;    // tables of S^T: [mat][l][g'][g] = sigs(mat, l, g', g)
+  int *gp_lo_adj = nullptr, *gp_hi_adj = nullptr;
+  double *colsum_d = nullptr;   // [3][G]: sum over destinations g' of sigs(mat, 0, g', g)
+  double *e0_d = nullptr;       // [2][D]: ell(0, d), ell_plus(d, 0)
+  double *det_d = nullptr;      // detector weights [Z]
+  unsigned long long *norm_d = nullptr;  // max|change|, max|value| as ordered bit patterns
+  double *resp_part = nullptr, *resp_d = nullptr;
+  int resp_nb = 0;
+  bool tc_lt_adj = false, tc_lp_adj = false;
+  uint16_t *tc_lt_img_adj = nullptr, *tc_lp_img_adj = nullptr;
+  int *tc_lt_exp_adj = nullptr, *tc_lp_exp_adj = nullptr;
+  int tc_lt_kpad_adj = 0, tc_lp_nhalf_adj = 0;
+  double inv_c0 = 0.0;          // w(d) / ell(0, d), or 0 when ell(0, .) is not proportional to w
+  bool adj_stale = true;        // adjoint tables must be rebuilt from the host inputs
+  bool have_lam = false;        // an adjoint solve has filled lam
+  int flip = 0;                 // 1 while the adjoint operators are installed
 };
 
 namespace {
@@ -341,7 +362,9 @@ void freeAll(kgb_ctx *c) {
                   c->dxyz_d[0], c->dxyz_d[1], c->dxyz_d[2], c->zmix_start, c->zmix_count, c->mix_mat, c->mix_zone,
                   c->mix_frac, c->gp_lo, c->gp_hi, c->sdoms_d, c->ident_d, c->levels_d, c->tiles_d, c->partials,
                   c->results, c->parts_dev, c->staging, c->cls_d, c->inv_d, c->pop_slots, c->tc_lt_img,
-                  c->tc_lp_img, c->tc_lt_exp, c->tc_lp_exp, c->err_d};
+                  c->tc_lp_img, c->tc_lt_exp, c->tc_lp_exp, c->err_d, c->lam, c->phi_prev, c->sigsT_adj,
+                  c->gp_lo_adj, c->gp_hi_adj, c->colsum_d, c->e0_d, c->det_d, c->norm_d, c->resp_part, c->resp_d,
+                  c->tc_lt_img_adj, c->tc_lp_img_adj, c->tc_lt_exp_adj, c->tc_lp_exp_adj};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->psi = c->rhs = c->phi = c->phi_out = c->sigt = nullptr;
@@ -363,6 +386,17 @@ void freeAll(kgb_ctx *c) {
   c->tc_lt_exp = c->tc_lp_exp = nullptr;
   c->tc_lt = c->tc_lp = false;
   c->err_d = nullptr;
+  c->lam = c->sigsT_adj = nullptr;
+  c->phi_prev = c->colsum_d = c->e0_d = c->det_d = c->resp_part = c->resp_d = nullptr;
+  c->gp_lo_adj = c->gp_hi_adj = nullptr;
+  c->norm_d = nullptr;
+  c->tc_lt_img_adj = c->tc_lp_img_adj = nullptr;
+  c->tc_lt_exp_adj = c->tc_lp_exp_adj = nullptr;
+  c->tc_lt_adj = c->tc_lp_adj = false;
+  c->resp_nb = 0;
+  c->adj_stale = true;
+  c->have_lam = false;
+  c->flip = 0;
   c->npop_slots = 0;
   c->use_recip = false;
   c->staging_bytes = 0;
@@ -462,9 +496,13 @@ int buildReciprocals(kgb_ctx *ctx) {
 // Plan the tensor-core LTimes / LPlusTimes: digit images of L and L+ and the
 // shapes the kernel supports (exact diagonal sums need K <= 128 directions in
 // FP64 and <= 256 in the mixed form; moments fit one 32-wide K chunk).
+// lt_src / lp_src: the [D][M] host tables the LTimes / LPlusTimes operators
+// read (ell and ell_plus for the forward iteration, exchanged for the adjoint).
 template <typename T>
-int planTensorMoments(kgb_ctx *ctx) {
-  ctx->tc_lt = ctx->tc_lp = false;
+int planTensorMomentsFrom(kgb_ctx *ctx, const std::vector<double> &lt_src, const std::vector<double> &lp_src,
+                          bool *lt_ok, uint16_t **lt_img, int **lt_exp, int *lt_kpad, bool *lp_ok, uint16_t **lp_img,
+                          int **lp_exp, int *lp_nhalf) {
+  *lt_ok = *lp_ok = false;
   if (!ctx->allow_tc) return KGB_OK;
   const bool f64 = sizeof(T) == 8;
   const int S = f64 ? 8 : 4;
@@ -488,10 +526,10 @@ int planTensorMoments(kgb_ctx *ctx) {
   // LTimes: B[d][m] = ell(m,d), K = D, N = M (one 32-wide block)
   if (M <= 32 && D <= (f64 ? 128 : 256)) {
     const int kpad = (D + 31) / 32 * 32;
-    tc_build_b<T>(ctx->ell_h.data(), D, M, kpad, S, 32, 1, img, ex);
-    if ((rc = upload(&ctx->tc_lt_img, &ctx->tc_lt_exp, img, ex))) return rc;
-    ctx->tc_lt_kpad = kpad;
-    ctx->tc_lt = true;
+    tc_build_b<T>(lt_src.data(), D, M, kpad, S, 32, 1, img, ex);
+    if ((rc = upload(lt_img, lt_exp, img, ex))) return rc;
+    *lt_kpad = kpad;
+    *lt_ok = true;
   }
   // LPlusTimes: B[m][d] = ell_plus(d,m), K = M (one chunk), N = D in blocks of NB
   if (M <= 32) {
@@ -501,14 +539,20 @@ int planTensorMoments(kgb_ctx *ctx) {
     if (smem <= 227 * 1024) {
       std::vector<double> bt((size_t)M * D);
       for (int d = 0; d < D; ++d)
-        for (int m = 0; m < M; ++m) bt[(size_t)m * D + d] = ctx->ellp_h[(size_t)d * M + m];
+        for (int m = 0; m < M; ++m) bt[(size_t)m * D + d] = lp_src[(size_t)d * M + m];
       tc_build_b<T>(bt.data(), M, D, 32, S, NB, nhalf, img, ex);
-      if ((rc = upload(&ctx->tc_lp_img, &ctx->tc_lp_exp, img, ex))) return rc;
-      ctx->tc_lp_nhalf = nhalf;
-      ctx->tc_lp = true;
+      if ((rc = upload(lp_img, lp_exp, img, ex))) return rc;
+      *lp_nhalf = nhalf;
+      *lp_ok = true;
     }
   }
   return KGB_OK;
+}
+
+template <typename T>
+int planTensorMoments(kgb_ctx *ctx) {
+  return planTensorMomentsFrom<T>(ctx, ctx->ell_h, ctx->ellp_h, &ctx->tc_lt, &ctx->tc_lt_img, &ctx->tc_lt_exp,
+                                  &ctx->tc_lt_kpad, &ctx->tc_lp, &ctx->tc_lp_img, &ctx->tc_lp_exp, &ctx->tc_lp_nhalf);
 }
 
 template <typename T>
@@ -558,6 +602,7 @@ int prepareT(kgb_ctx *ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_quad = false;
     ctx->dirty_geom = true;
+    ctx->adj_stale = true;
   }
   if (ctx->dirty_geom) {
     if ((rc = need(ctx, {"dx", "dy", "dz"}))) return rc;
@@ -581,6 +626,7 @@ int prepareT(kgb_ctx *ctx) {
     if ((rc = uploadVec<T>(ctx, ctx->ellp, ctx->ellp_h))) return rc;
     if ((rc = planTensorMoments<T>(ctx))) return rc;
     ctx->dirty_ell = false;
+    ctx->adj_stale = true;
   }
   if (ctx->dirty_sigs) {
     if ((rc = need(ctx, {"data/sigs"}))) return rc;
@@ -603,6 +649,7 @@ int prepareT(kgb_ctx *ctx) {
     CK(cudaMemcpyAsync(ctx->gp_hi, hi.data(), G * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_sigs = false;
+    ctx->adj_stale = true;
   }
   if (ctx->dirty_vol) {
     if ((rc = need(ctx, {"volume"}))) return rc;
@@ -736,6 +783,7 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop) {
   a.tz = ctx->tz;
   a.tx = ctx->tx;
   a.ty = ctx->ty;
+  a.flip = ctx->flip;
   if (ctx->use_recip) {
     a.cls = ctx->cls_d;
     a.inv = ctx->inv_d;
@@ -783,7 +831,10 @@ int sweepSolver(kgb_ctx *ctx, bool fused_pop = false) {
   for (int k = 0; k < 3; ++k) CK(cudaMemsetAsync(ctx->plane[k], 0, ctx->plane_chunk[k] * ctx->dc.num() * ctx->tsz, ctx->stream));
   const int nlev = (int)ctx->level_off.size() - 1;
   const int S[3] = {ctx->dc.Sx, ctx->dc.Sy, ctx->dc.Sz};
-  for (int lv = 0; lv < nlev; ++lv) {
+  // the reversed (adjoint) orientation visits the zone-set levels last to first
+  const int sgn = ctx->flip ? -1 : 1;
+  for (int step = 0; step < nlev; ++step) {
+    const int lv = ctx->flip ? nlev - 1 - step : step;
     const int b = ctx->level_off[lv], e = ctx->level_off[lv + 1];
     if (e == b) continue;
     int rc = sweepWaveAny(ctx, ctx->levels_d + b, e - b, fused_pop);
@@ -793,7 +844,7 @@ int sweepSolver(kgb_ctx *ctx, bool fused_pop = false) {
       const int s = ctx->level_sdoms[x];
       const SdomDesc &d = ctx->sdoms_h[s];
       int co[5] = {d.p, d.q, d.xs, d.ys, d.zs};
-      const int dirv[3] = {d.id, d.jd, d.kd};
+      const int dirv[3] = {sgn * d.id, sgn * d.jd, sgn * d.kd};
       for (int dim = 0; dim < 3; ++dim) {
         int dn[5] = {co[0], co[1], co[2], co[3], co[4]};
         dn[2 + dim] += dirv[dim];
@@ -949,6 +1000,262 @@ int iterateDevice(kgb_ctx *ctx, double q, double *part_slot) {
   }
   return KGB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Converged solves, the adjoint source iteration, response and gradients
+// ---------------------------------------------------------------------------
+MixArgs mixArgs(const kgb_ctx *ctx) {
+  MixArgs a{};
+  a.Z = ctx->Z;
+  a.G = ctx->G;
+  a.nx = ctx->nx;
+  a.ny = ctx->ny;
+  a.zmix_start = ctx->zmix_start;
+  a.zmix_count = ctx->zmix_count;
+  a.mix_mat = ctx->mix_mat;
+  a.mix_frac = ctx->mix_frac;
+  a.colsum = ctx->colsum_d;
+  a.det = ctx->det_d;
+  a.vol = ctx->vol_d;
+  a.dx = ctx->dxyz_d[0];
+  a.dy = ctx->dxyz_d[1];
+  a.dz = ctx->dxyz_d[2];
+  return a;
+}
+
+constexpr int kRespTerms = 13;  // per group: 4 terms for each of 3 materials, then the response
+
+// Small buffers of the response path, allocated on first use; the detector
+// starts as the whole domain.
+int ensureResponseBuffers(kgb_ctx *ctx) {
+  int rc;
+  if (!ctx->phi_prev && (rc = dmalloc(ctx, &ctx->phi_prev, ctx->Z * ctx->G))) return rc;
+  if (!ctx->norm_d && (rc = dmalloc(ctx, &ctx->norm_d, 2))) return rc;
+  if (!ctx->colsum_d && (rc = dmalloc(ctx, &ctx->colsum_d, 3 * ctx->G))) return rc;
+  if (!ctx->e0_d && (rc = dmalloc(ctx, &ctx->e0_d, 2 * ctx->D))) return rc;
+  if (!ctx->det_d) {
+    if ((rc = dmalloc(ctx, &ctx->det_d, ctx->Z))) return rc;
+    launch_fill<double>(ctx->det_d, ctx->Z, 1.0, ctx->stream);
+    CKN(1);
+  }
+  if (!ctx->resp_d) {
+    const int64_t want = ((int64_t)ctx->nsm * 8 + ctx->G - 1) / ctx->G;
+    ctx->resp_nb = (int)std::max<int64_t>(1, std::min<int64_t>(want, (ctx->Z + 3) / 4));
+    if ((rc = dmalloc(ctx, &ctx->resp_part, (size_t)ctx->resp_nb * ctx->G * kRespTerms)) ||
+        (rc = dmalloc(ctx, &ctx->resp_d, (size_t)ctx->G * kRespTerms)))
+      return rc;
+  }
+  return KGB_OK;
+}
+
+// Tables of the adjoint operators, rebuilt when quadrature, L/L+ or sigs change:
+// S^T (sigs uploaded untransposed, read by the scattering kernel as
+// [mat][l][g'][g]) with its nonzero source ranges, the P0 out-scattering sums,
+// moment-0 rows of L and L+, and tensor-core plans of L+^T and L^T.
+template <typename T>
+int prepareAdjointT(kgb_ctx *ctx) {
+  int rc;
+  if ((rc = ensureResponseBuffers(ctx))) return rc;
+  if (!ctx->adj_stale) return KGB_OK;
+  const int G = ctx->G, L1 = ctx->L + 1, D = ctx->D, M = ctx->M;
+  std::vector<int> lo(G, G), hi(G, -1);
+  std::vector<double> colsum((size_t)3 * G, 0.0);
+  for (int m = 0; m < 3; ++m)
+    for (int l = 0; l < L1; ++l)
+      for (int gp = 0; gp < G; ++gp)
+        for (int g = 0; g < G; ++g)
+          if (ctx->sigs_h[(((size_t)m * L1 + l) * G + gp) * G + g] != 0.0) {
+            lo[g] = std::min(lo[g], gp);
+            hi[g] = std::max(hi[g], gp);
+          }
+  for (int m = 0; m < 3; ++m)
+    for (int g = 0; g < G; ++g)
+      for (int gp = 0; gp < G; ++gp) colsum[(size_t)m * G + g] += ctx->sigs_h[(((size_t)m * L1) * G + gp) * G + g];
+  if (!ctx->sigsT_adj) {
+    if ((rc = dalloc(ctx, &ctx->sigsT_adj, (size_t)3 * L1 * G * G * ctx->tsz)) ||
+        (rc = dmalloc(ctx, &ctx->gp_lo_adj, G)) || (rc = dmalloc(ctx, &ctx->gp_hi_adj, G)))
+      return rc;
+  }
+  if ((rc = uploadVec<T>(ctx, ctx->sigsT_adj, ctx->sigs_h))) return rc;
+  std::vector<double> e0((size_t)2 * D);
+  for (int d = 0; d < D; ++d) {
+    e0[d] = ctx->ell_h[(size_t)d * M];
+    e0[D + d] = ctx->ellp_h[(size_t)d * M];
+  }
+  CK(cudaMemcpyAsync(ctx->gp_lo_adj, lo.data(), G * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->gp_hi_adj, hi.data(), G * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->colsum_d, colsum.data(), colsum.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->e0_d, e0.data(), e0.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  // the response derivative w(d) vol det siga is L^T applied to a moment-0
+  // source exactly when ell(0, d) = c0 w(d) for every direction
+  const std::vector<double> &w = ctx->q[3];
+  const double c0 = w[0] != 0.0 ? ctx->ell_h[0] / w[0] : 0.0;
+  bool prop = c0 != 0.0;
+  for (int d = 0; d < D && prop; ++d) prop = std::fabs(ctx->ell_h[(size_t)d * M] - c0 * w[d]) <= 1e-13 * std::fabs(c0 * w[d]);
+  ctx->inv_c0 = prop ? 1.0 / c0 : 0.0;
+  if ((rc = planTensorMomentsFrom<T>(ctx, ctx->ellp_h, ctx->ell_h, &ctx->tc_lt_adj, &ctx->tc_lt_img_adj,
+                                     &ctx->tc_lt_exp_adj, &ctx->tc_lt_kpad_adj, &ctx->tc_lp_adj, &ctx->tc_lp_img_adj,
+                                     &ctx->tc_lp_exp_adj, &ctx->tc_lp_nhalf_adj)))
+    return rc;
+  ctx->adj_stale = false;
+  return KGB_OK;
+}
+
+int prepareAdjoint(kgb_ctx *ctx) {
+  return ctx->prec == KGB_FP64 ? prepareAdjointT<double>(ctx) : prepareAdjointT<float>(ctx);
+}
+
+// Installs the adjoint operators for its lifetime: lam takes psi's place,
+// L and L+ exchange (their [D][M] tables are each other's transposes), the
+// scattering kernel reads S^T, and the sweep runs reversed.  Nothing may
+// reallocate context buffers while it is installed.
+struct AdjointView {
+  kgb_ctx *c;
+  explicit AdjointView(kgb_ctx *ctx) : c(ctx) { swap(); }
+  ~AdjointView() { swap(); }
+  AdjointView(const AdjointView &) = delete;
+  AdjointView &operator=(const AdjointView &) = delete;
+  void swap() {
+    std::swap(c->psi, c->lam);
+    std::swap(c->ell, c->ellp);
+    std::swap(c->sigsT, c->sigsT_adj);
+    std::swap(c->gp_lo, c->gp_lo_adj);
+    std::swap(c->gp_hi, c->gp_hi_adj);
+    std::swap(c->tc_lt, c->tc_lt_adj);
+    std::swap(c->tc_lp, c->tc_lp_adj);
+    std::swap(c->tc_lt_img, c->tc_lt_img_adj);
+    std::swap(c->tc_lp_img, c->tc_lp_img_adj);
+    std::swap(c->tc_lt_exp, c->tc_lt_exp_adj);
+    std::swap(c->tc_lp_exp, c->tc_lp_exp_adj);
+    std::swap(c->tc_lt_kpad, c->tc_lt_kpad_adj);
+    std::swap(c->tc_lp_nhalf, c->tc_lp_nhalf_adj);
+    c->flip ^= 1;
+  }
+};
+
+int doAdjointSource(kgb_ctx *ctx) {
+  FamScope fs(ctx, "source");
+  const MixArgs a = mixArgs(ctx);
+  if (ctx->prec == KGB_FP64)
+    launch_adjoint_source<double>(as<double>(ctx->phi_out), ctx->M, as<double>(ctx->sigt), a, ctx->inv_c0, ctx->stream);
+  else
+    launch_adjoint_source<float>(as<float>(ctx->phi_out), ctx->M, as<float>(ctx->sigt), a, ctx->inv_c0, ctx->stream);
+  CKN(1);
+  return KGB_OK;
+}
+
+// Source iterations from a zero state until moment 0 of successive iterates
+// changes by at most tol relative to its largest magnitude.  The change is
+// measured on the moments each iteration computes first (phi = L psi of the
+// previous iterate), so the test lags one sweep and the returned state is
+// one iteration past the converged one.  With the adjoint operators
+// installed it runs the adjoint iteration with the response source.
+int convergeLoop(kgb_ctx *ctx, bool adjoint, double q, double tol, int max_iter, int32_t *iters, double *change) {
+  int rc;
+  const int64_t rows = ctx->Z * ctx->G;
+  CK(cudaMemsetAsync(ctx->psi, 0, rows * ctx->D * ctx->tsz, ctx->stream));
+  CK(cudaMemsetAsync(ctx->phi_prev, 0, rows * sizeof(double), ctx->stream));
+  double ch = std::numeric_limits<double>::infinity();
+  int it = 0;
+  while (it < max_iter) {
+    ++it;
+    if ((rc = doLTimes(ctx, false))) return rc;
+    CK(cudaMemsetAsync(ctx->norm_d, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    {
+      FamScope fs(ctx, "convergence");
+      if (ctx->prec == KGB_FP64)
+        launch_change_norm<double>(as<double>(ctx->phi), ctx->M, ctx->phi_prev, rows, ctx->norm_d, ctx->stream);
+      else
+        launch_change_norm<float>(as<float>(ctx->phi), ctx->M, ctx->phi_prev, rows, ctx->norm_d, ctx->stream);
+      CKN(1);
+    }
+    if ((rc = doScattering(ctx, false))) return rc;
+    if ((rc = adjoint ? doAdjointSource(ctx) : doSource(ctx, q))) return rc;
+    if ((rc = doLPlusTimes(ctx, false))) return rc;
+    if ((rc = sweepSolver(ctx, false))) return rc;
+    unsigned long long h[2] = {0ull, 0ull};
+    CK(cudaMemcpyAsync(h, ctx->norm_d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (it >= 2) {
+      double dmax, amax;
+      std::memcpy(&dmax, &h[0], sizeof(double));
+      std::memcpy(&amax, &h[1], sizeof(double));
+      if (!std::isfinite(dmax) || !std::isfinite(amax))
+        return fail(ctx, KGB_ERR_STATE, "the source iteration produced a non-finite flux");
+      ch = amax > 0.0 ? dmax / amax : (dmax > 0.0 ? std::numeric_limits<double>::infinity() : 0.0);
+      if (ch <= tol) break;
+    }
+  }
+  if (iters) *iters = it;
+  if (change) *change = ch;
+  return KGB_OK;
+}
+
+// Per-group response terms (kRespTerms per group) of state psi and, when lam
+// is given, the adjoint terms against lam with moments from psi0.
+int responseTermsOf(kgb_ctx *ctx, const void *psi, const void *psi0, const void *lam, std::vector<double> &out) {
+  {
+    FamScope fs(ctx, "response");
+    const MixArgs a = mixArgs(ctx);
+    const double *ell0 = ctx->e0_d, *ellp0 = ctx->e0_d + ctx->D;
+    if (ctx->prec == KGB_FP64)
+      launch_response<double>((const double *)psi, (const double *)psi0, (const double *)lam, ctx->D, ctx->w_d, ell0,
+                              ellp0, as<double>(ctx->sigt), a, ctx->resp_part, ctx->resp_nb, ctx->resp_d, ctx->stream);
+    else
+      launch_response<float>((const float *)psi, (const float *)psi0, (const float *)lam, ctx->D, ctx->w_d, ell0,
+                             ellp0, as<float>(ctx->sigt), a, ctx->resp_part, ctx->resp_nb, ctx->resp_d, ctx->stream);
+    CKN(2);
+  }
+  out.assign((size_t)ctx->G * kRespTerms, 0.0);
+  CK(cudaMemcpyAsync(out.data(), ctx->resp_d, out.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return KGB_OK;
+}
+
+// One forward source iteration from state `in` (nullptr: zero) into `out`;
+// the sweep writes only `out`, so both may be any psi-sized buffers.
+int forwardStep(kgb_ctx *ctx, void *in, void *out, double q) {
+  void *const keep = ctx->psi;
+  int rc = KGB_OK;
+  if (in) {
+    ctx->psi = in;
+    rc = doLTimes(ctx, false);
+  } else if (cudaMemsetAsync(ctx->phi, 0, ctx->Z * ctx->G * ctx->M * ctx->tsz, ctx->stream) != cudaSuccess) {
+    rc = fail(ctx, KGB_ERR_CUDA, "memset failed");
+  }
+  if (!rc) rc = doScattering(ctx, false);
+  if (!rc) rc = doSource(ctx, q);
+  if (!rc) rc = doLPlusTimes(ctx, false);
+  ctx->psi = out;
+  if (!rc) rc = sweepSolver(ctx, false);
+  ctx->psi = keep;
+  return rc;
+}
+
+// One step of the reverse pass through unrolled iterations (adjoint operators
+// installed, psi = the reverse state): the first step sweeps the response
+// source alone, later ones apply L^T S^T L+^T to the state and sweep.
+int reverseStep(kgb_ctx *ctx, bool first) {
+  int rc;
+  if (first) {
+    CK(cudaMemsetAsync(ctx->phi_out, 0, ctx->Z * ctx->G * ctx->M * ctx->tsz, ctx->stream));
+    if ((rc = doAdjointSource(ctx))) return rc;
+  } else {
+    if ((rc = doLTimes(ctx, false))) return rc;
+    if ((rc = doScattering(ctx, false))) return rc;
+  }
+  if ((rc = doLPlusTimes(ctx, false))) return rc;
+  return sweepSolver(ctx, false);
+}
+
+// psi-sized device buffers held for one call
+struct PsiBuffers {
+  std::vector<void *> b;
+  ~PsiBuffers() {
+    for (void *p : b) cudaFree(p);
+  }
+};
 
 }  // namespace
 
@@ -1133,6 +1440,7 @@ int kgb_field_upload(kgb_ctx *ctx, const char *name, const void *host, int64_t n
   const FieldInfo *f = findField(name);
   if (!f) return fail(ctx, KGB_ERR_ARG, std::string("unknown field '") + (name ? name : "(null)") + "'");
   if (!host && nbytes > 0) return fail(ctx, KGB_ERR_ARG, "null host pointer");
+  ctx->have_lam = false;  // an adjoint state belongs to the inputs it was computed for
   const int64_t want = fieldBytes(ctx, f);
   if (nbytes != want)
     return fail(ctx, KGB_ERR_ARG, std::string("field '") + name + "' expects " + std::to_string(want) + " bytes, got " + std::to_string(nbytes));
@@ -1649,6 +1957,181 @@ int kgb_launch_count(kgb_ctx *ctx, int64_t *out) {
   if (!ctx || !out) return KGB_ERR_ARG;
   *out = ctx->launches;
   return KGB_OK;
+}
+
+// --- converged solves, the adjoint and gradients ---------------------------
+
+int kgb_set_materials(kgb_ctx *ctx, const double *sigt, const double *sigs) {
+  if (!ctx) return KGB_ERR_ARG;
+  if (!ctx->ready) return fail(ctx, KGB_ERR_STATE, "kgb_setup has not been called");
+  if (sigs) {
+    ctx->sigs_h.assign(sigs, sigs + (size_t)3 * (ctx->L + 1) * ctx->G * ctx->G);
+    ctx->have[fieldIndex(findField("data/sigs"))] = true;
+    ctx->dirty_sigs = true;
+  }
+  if (sigt) ctx->have[fieldIndex(findField("sigt_zonal"))] = true;
+  ctx->have_lam = false;
+  int rc = prepare(ctx);  // mixture tables on the device
+  if (rc || !sigt) return rc;
+  if ((rc = ensureStaging(ctx, (size_t)3 * ctx->G * sizeof(double)))) return rc;
+  CK(cudaMemcpyAsync(ctx->staging, sigt, (size_t)3 * ctx->G * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  const MixArgs a = mixArgs(ctx);
+  if (ctx->prec == KGB_FP64)
+    launch_material_sigt<double>(as<double>(ctx->sigt), ctx->staging, a, ctx->stream);
+  else
+    launch_material_sigt<float>(as<float>(ctx->sigt), ctx->staging, a, ctx->stream);
+  CKN(1);
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->dirty_sigt = true;  // tabulated sweep reciprocals
+  return prepare(ctx);
+}
+
+int kgb_set_response(kgb_ctx *ctx, const double *det, int64_t n) {
+  if (!ctx) return KGB_ERR_ARG;
+  if (!ctx->ready) return fail(ctx, KGB_ERR_STATE, "kgb_setup has not been called");
+  if (det && n != ctx->Z) return fail(ctx, KGB_ERR_ARG, "detector weights need one value per zone");
+  CK(cudaSetDevice(ctx->device));
+  int rc = ensureResponseBuffers(ctx);
+  if (rc) return rc;
+  if (det) {
+    CK(cudaMemcpyAsync(ctx->det_d, det, ctx->Z * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  } else {
+    launch_fill<double>(ctx->det_d, ctx->Z, 1.0, ctx->stream);
+    CKN(1);
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_lam = false;
+  return KGB_OK;
+}
+
+int kgb_solve_converged(kgb_ctx *ctx, double source_strength, double tol, int32_t max_iter, int32_t *iters,
+                        double *change) {
+  int rc = prepare(ctx);
+  if (rc) return rc;
+  if (max_iter < 1 || !(tol >= 0.0)) return fail(ctx, KGB_ERR_ARG, "need max_iter >= 1 and tol >= 0");
+  if ((rc = ensureResponseBuffers(ctx))) return rc;
+  if ((rc = convergeLoop(ctx, false, source_strength, tol, max_iter, iters, change))) return rc;
+  return checkDeviceError(ctx);
+}
+
+int kgb_adjoint_solve(kgb_ctx *ctx, double tol, int32_t max_iter, int32_t *iters, double *change) {
+  int rc = prepare(ctx);
+  if (rc) return rc;
+  if (max_iter < 1 || !(tol >= 0.0)) return fail(ctx, KGB_ERR_ARG, "need max_iter >= 1 and tol >= 0");
+  if ((rc = prepareAdjoint(ctx))) return rc;
+  if (ctx->inv_c0 == 0.0)
+    return fail(ctx, KGB_ERR_ARG, "the adjoint source needs ell(0, d) proportional to the quadrature weight w(d)");
+  if (!ctx->lam && (rc = dalloc(ctx, &ctx->lam, (size_t)ctx->Z * ctx->G * ctx->D * ctx->tsz))) return rc;
+  ctx->have_lam = false;
+  {
+    AdjointView view(ctx);
+    rc = convergeLoop(ctx, true, 0.0, tol, max_iter, iters, change);
+  }
+  if (rc) return rc;
+  if ((rc = checkDeviceError(ctx))) return rc;
+  ctx->have_lam = true;
+  return KGB_OK;
+}
+
+int kgb_response(kgb_ctx *ctx, double *response) {
+  if (!response) return fail(ctx, KGB_ERR_ARG, "null output");
+  int rc = prepare(ctx);
+  if (rc || (rc = prepareAdjoint(ctx))) return rc;
+  std::vector<double> t;
+  if ((rc = responseTermsOf(ctx, ctx->psi, nullptr, nullptr, t))) return rc;
+  double r = 0.0;
+  for (int g = 0; g < ctx->G; ++g) r += t[(size_t)g * kRespTerms + 12];
+  *response = r;
+  return KGB_OK;
+}
+
+int kgb_gradient(kgb_ctx *ctx, double *response, double *dsigt, double *dsigs, double *dq) {
+  int rc = prepare(ctx);
+  if (rc || (rc = prepareAdjoint(ctx))) return rc;
+  if (!ctx->have_lam || !ctx->lam) return fail(ctx, KGB_ERR_STATE, "kgb_adjoint_solve has not run for these inputs");
+  std::vector<double> t;
+  if ((rc = responseTermsOf(ctx, ctx->psi, ctx->psi, ctx->lam, t))) return rc;
+  const int G = ctx->G;
+  double r = 0.0, q = 0.0;
+  for (int g = 0; g < G; ++g) {
+    const double *x = &t[(size_t)g * kRespTerms];
+    r += x[12];
+    q += x[3];  // material 0 carries the source
+    for (int m = 0; m < 3; ++m) {
+      if (dsigt) dsigt[m * G + g] = x[m * 4 + 0] - x[m * 4 + 1];
+      if (dsigs) dsigs[m * G + g] = x[m * 4 + 2] - x[m * 4 + 0];
+    }
+  }
+  if (response) *response = r;
+  if (dq) *dq = q;
+  return KGB_OK;
+}
+
+int kgb_gradient_unrolled(kgb_ctx *ctx, int32_t niter, double source_strength, int32_t stride, double *response,
+                          double *dsigt, double *dsigs, double *dq) {
+  int rc = prepare(ctx);
+  if (rc || (rc = prepareAdjoint(ctx))) return rc;
+  if (niter < 1) return fail(ctx, KGB_ERR_ARG, "need niter >= 1");
+  if (ctx->inv_c0 == 0.0)
+    return fail(ctx, KGB_ERR_ARG, "the adjoint source needs ell(0, d) proportional to the quadrature weight w(d)");
+  if (!ctx->lam && (rc = dalloc(ctx, &ctx->lam, (size_t)ctx->Z * ctx->G * ctx->D * ctx->tsz))) return rc;
+  ctx->have_lam = false;
+  const int K = niter;
+  const int c = stride > 0 ? std::min<int>(stride, K) : std::max(1, (int)std::ceil(std::sqrt((double)K)));
+  const int ncp = (K - 1) / c;  // checkpoints psi_c, psi_2c, ... below psi_K
+  const size_t pbytes = (size_t)ctx->Z * ctx->G * ctx->D * ctx->tsz;
+  PsiBuffers cp, seg;
+  for (int i = 0; i < ncp + c - 1; ++i) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, pbytes) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, KGB_ERR_OOM, "checkpoint buffers do not fit: raise the stride");
+    }
+    (i < ncp ? cp.b : seg.b).push_back(p);
+  }
+  // iterate j lives in: psi (j = K), a checkpoint (j a multiple of c) or a segment slot
+  auto buf = [&](int j) -> void * {
+    if (j == 0) return nullptr;
+    if (j == K) return ctx->psi;
+    return j % c == 0 ? cp.b[j / c - 1] : seg.b[j % c - 1];
+  };
+  for (int j = 1; j <= K; ++j)
+    if ((rc = forwardStep(ctx, buf(j - 1), buf(j), source_strength))) return rc;
+  const int G = ctx->G;
+  std::vector<double> tot((size_t)G * kRespTerms, 0.0), t;
+  bool first = true;
+  for (int sgm = ncp; sgm >= 0; --sgm) {
+    const int j0 = sgm * c, j1 = std::min(j0 + c, K);
+    if (sgm < ncp)  // the last segment's iterates are still resident from the forward pass
+      for (int j = j0 + 1; j < j1; ++j)
+        if ((rc = forwardStep(ctx, buf(j - 1), buf(j), source_strength))) return rc;
+    for (int k = j1 - 1; k >= j0; --k) {
+      {
+        AdjointView view(ctx);
+        rc = reverseStep(ctx, first);
+      }
+      if (rc) return rc;
+      if ((rc = responseTermsOf(ctx, buf(k + 1), buf(k), ctx->lam, t))) return rc;
+      for (size_t i = 0; i < tot.size(); ++i) {
+        const int term = (int)(i % kRespTerms);
+        if (first || (term != 12 && term % 4 != 0)) tot[i] += t[i];  // E and R belong to psi_K alone
+      }
+      first = false;
+    }
+  }
+  double r = 0.0, q = 0.0;
+  for (int g = 0; g < G; ++g) {
+    const double *x = &tot[(size_t)g * kRespTerms];
+    r += x[12];
+    q += x[3];
+    for (int m = 0; m < 3; ++m) {
+      if (dsigt) dsigt[m * G + g] = x[m * 4 + 0] - x[m * 4 + 1];
+      if (dsigs) dsigs[m * G + g] = x[m * 4 + 2] - x[m * 4 + 0];
+    }
+  }
+  if (response) *response = r;
+  if (dq) *dq = q;
+  return checkDeviceError(ctx);
 }
 
 int kgb_reset_timers(kgb_ctx *ctx) {

@@ -45,6 +45,7 @@ struct SweepArgs {
   int nx, ny, nz, G, D, Gs, Ds, nxs, nys, nzs;
   int tz;                     // tile depth in k
   int tx, ty;                 // tile footprint in i and j: 4x4, 4x2 or 2x2
+  int flip;                   // 1: sweep every direction in the reversed orientation (adjoint)
   // tabulated reciprocals (uniform mesh): 1/((cx+cy+cz)[d] + sigt) per (sigt class, direction)
   const uint16_t *cls;        // [Z][G] class of sigt_zonal, or null: divide per cell
   const double *inv;          // [nclass][D]
@@ -137,5 +138,26 @@ template <typename Td>
 void launch_download_xpose(const Td *dev, double *staging, const XposeDesc &x, cudaStream_t s);
 template <typename T>
 void launch_fill(T *p, int64_t n, double v, cudaStream_t s);
+
+// Response, adjoint source and gradients (adjoint.cu).
+struct MixArgs {
+  int64_t Z;
+  int G, nx, ny;
+  const int *zmix_start, *zmix_count, *mix_mat;
+  const double *mix_frac;
+  const double *colsum;       // [3][G]: sum over destinations of the P0 scattering of source group g
+  const double *det, *vol;    // detector weights and zone volumes [Z]
+  const double *dx, *dy, *dz; // mesh spacing (cell volume dx*dy*dz scales the adjoint state)
+};
+template <typename T>
+void launch_adjoint_source(T *phi_out, int M, const T *sigt, const MixArgs &a, double inv_c0, cudaStream_t s);
+template <typename T>
+void launch_response(const T *psi, const T *psi0, const T *lam, int D, const double *w, const double *ell0,
+                     const double *ellp0, const T *sigt, const MixArgs &a, double *partials, int nblocks_z,
+                     double *out, cudaStream_t s);
+template <typename T>
+void launch_change_norm(const T *phi, int M, double *prev, int64_t rows, unsigned long long *out, cudaStream_t s);
+template <typename T>
+void launch_material_sigt(T *sigt, const double *sigt_mat, const MixArgs &a, cudaStream_t s);
 
 }  // namespace kgb

@@ -24,6 +24,11 @@
 // exactly as per cell (same operands, same association) and rounded once to
 // 1/den; the cell then multiplies (psi differs from num/den by at most 1.5 ulp).
 //
+// The transposed (adjoint) sweep is the same recurrence run from the opposite
+// corner: the diamond-difference matrix of a direction is triangular in its
+// sweep order with the alternating face coupling (2, -2, 2, ...) along each
+// axis, and its transpose has the same entries ordered from the other end.
+//
 // The population edit (Kernel::population) is fused: each thread accumulates
 // volume * psi over its cells (FP64, or compensated FP32 in the mixed form),
 // scales by w(d), and each block writes one partial; a fixed-order reduction
@@ -73,6 +78,8 @@ template <typename T, int TX, int TY, bool RECIP, bool POP>
 __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const SweepArgs<T> a) {
   const int sdom = a.wave[blockIdx.z];
   const SdomDesc sd = a.sdoms[sdom];
+  // the adjoint sweep (transposed operator) runs every direction in its reversed orientation
+  const int sid = a.flip ? -sd.id : sd.id, sjd = a.flip ? -sd.jd : sd.jd, skd = a.flip ? -sd.kd : sd.kd;
   const int4 t = a.tiles[a.tile_off + blockIdx.y];
   const int nchain = a.Ds * a.Gs;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -96,14 +103,14 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const SweepAr
     for (int ii = 0; ii < TX; ++ii) {
       const int ip = ib + ii;
       iv[ii] = ip < a.nxs;
-      iloc[ii] = sd.id > 0 ? ip : a.nxs - 1 - ip;
+      iloc[ii] = sid > 0 ? ip : a.nxs - 1 - ip;
       cxr[ii] = iv[ii] ? a.cx[(int64_t)d * a.nx + sd.io + iloc[ii]] : T(0);
     }
 #pragma unroll
     for (int jj = 0; jj < TY; ++jj) {
       const int jp = jb + jj;
       jv[jj] = jp < a.nys;
-      jloc[jj] = sd.jd > 0 ? jp : a.nys - 1 - jp;
+      jloc[jj] = sjd > 0 ? jp : a.nys - 1 - jp;
       cyr[jj] = jv[jj] ? a.cy[(int64_t)d * a.ny + sd.jo + jloc[jj]] : T(0);
     }
 
@@ -123,7 +130,7 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const SweepAr
     const int kend = min(a.tz, a.nzs - kb);
     for (int kk = 0; kk < kend; ++kk) {
       const int kq = kb + kk;
-      const int k = sd.kd > 0 ? kq : a.nzs - 1 - kq;
+      const int k = skd > 0 ? kq : a.nzs - 1 - kq;
       const T czk = a.cz[(int64_t)d * a.nz + sd.ko + k];
       // The slice's loads do not depend on the upwind chain: issue them all
       // before the first cell so their latency overlaps.
