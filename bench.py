@@ -14,6 +14,11 @@ larger than L2, so no L2 flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--precision fp64|mixed]
 
+The FP64 line also carries, from the same run, the mixed form on the same
+workload ("mixed": throughput, speed-up over FP64, phi error against FP64
+after 20 iterations) and the adjoint report ("adjoint": gradient/forward time
+and central-difference check at 32^3 zones x 32 groups x 96 directions).
+
 --gpus N > 1 (under torchrun) runs N independent replicas, one per GPU
 (the path has no data exchange); value = all replicas' unknowns / max time.
 --impl reference times the CPU restatement of the reference's OpenMP path
@@ -37,6 +42,12 @@ WORKLOAD_NAME = "kripke 64^3 zones x 64 groups x 128 GL directions, P4, cube100,
 # bounded CPU sample: same physics and per-zone work, 32^3 zones (1/8 of the unknowns)
 CPU_SAMPLE = dict(WORKLOAD, zones=(32, 32, 32))
 FP64_PEAK_GFLOPS = 1196.0  # DFMA rate measured on this machine's GB300 (profiles/fp64_peak_gb300.md)
+MIXED_PHI_ITERS = 20  # the mixed form's phi error is taken against FP64 after this many iterations
+# adjoint gradient workload: cross sections of the reference problem, +-20% per group, isotropic P0
+ADJ_WORKLOAD = dict(zones=(32, 32, 32), groups=32, quad=96, legendre=4, gset=1, dset=8, geometry=1, scatter=0,
+                    perturb=1, layout="DGZ")
+ADJ_NAME = ("32^3 zones x 32 groups x 96 directions, P4, cube100, isotropic P0 with +-20% per-group perturbation; "
+            "absorption in the detector block [80,100]^3 cm")
 
 
 def fp64_peak():
@@ -179,6 +190,117 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def timed_steps(ctx, stream, steps):
+    """K source iterations between CUDA events on the stream the kernels run on; ms per iteration."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.iterate(want_population=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def mixed_report(args, local, w, fp64_ctx, fp64_ms):
+    """The mixed form on the same workload: throughput against the FP64 form and phi error against FP64."""
+    import numpy as np
+    import torch
+    from kripke_gb300 import abi
+    ctx = abi.Context(local)
+    ctx.generate(precision=abi.MIXED, **w)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.fill("psi", 0.0)
+    ctx.iterate(want_population=False)
+    tuned = ctx.autotune() if not args.no_autotune else None
+    ctx.fill("psi", 0.0)
+    for _ in range(args.warmup):
+        ctx.iterate(want_population=False)
+    ms = timed_steps(ctx, stream, args.steps)
+    ctx.solve(MIXED_PHI_ITERS)
+    fp64_ctx.solve(MIXED_PHI_ITERS)
+    a, b = fp64_ctx.download("phi"), ctx.download("phi")
+    err = float(np.abs(b - a).max() / np.abs(a).max())
+    del a, b
+    out = {"value": unknowns(w) / (ms * 1e-3), "unit": "unknowns/s", "ms_per_step": ms,
+           "speedup_vs_fp64": fp64_ms / ms, "phi_rel_err_vs_fp64": err,
+           "phi_err_definition": "max|phi_mixed - phi_fp64| / max|phi_fp64| over all moments, groups and zones "
+                                 "after %d iterations from psi = 0" % MIXED_PHI_ITERS,
+           "autotuned": tuned,
+           "kernels": {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "moments_tensor_ltimes",
+                                                      "moments_tensor_lplustimes")}}
+    ctx.close()
+    return out
+
+
+def adjoint_report(local, fd_params=3):
+    """Gradient / forward time and accuracy of the adjoint at the adjoint workload, FP64 and mixed."""
+    import numpy as np
+    from kripke_gb300 import abi
+    from kripke_gb300.response import context_box_detector
+
+    def timed(fn):
+        t0 = time.perf_counter()
+        r = fn()
+        return r, time.perf_counter() - t0
+
+    res = {"workload": ADJ_NAME, "unknowns": unknowns(ADJ_WORKLOAD)}
+    grads = {}
+    # the mixed form iterates to its FP32 rounding floor (the solves stop when the change stops falling)
+    for name, prec, tol in (("fp64", abi.FP64, 1e-12), ("mixed", abi.MIXED, 1e-9)):
+        ctx = abi.Context(local)
+        inp = ctx.generate(precision=prec, **ADJ_WORKLOAD)
+        ctx.set_response(context_box_detector(ctx, (80.0, 80.0, 80.0), (100.0, 100.0, 100.0)))
+        ctx.solve_converged(1.0, tol, 2000)  # builds the tables; untimed
+        ctx.adjoint_solve(tol, 2000)
+        (fit, fch), t_fwd = timed(lambda: ctx.solve_converged(1.0, tol, 2000))
+        (ait, ach), t_adj = timed(lambda: ctx.adjoint_solve(tol, 2000))
+        g, t_grad = timed(ctx.gradient)
+        grads[name] = g
+        r = {"tol": tol, "forward_s": t_fwd, "forward_iters": fit, "forward_change": fch, "adjoint_s": t_adj,
+             "adjoint_iters": ait, "adjoint_change": ach,
+             "gradient_assembly_s": t_grad, "grad_over_fwd": (t_adj + t_grad) / t_fwd, "response": g[0]}
+        if name == "fp64":
+            # central differences (relative step 1e-4) of the GPU forward at the largest gradient entries
+            st, sg = abi.material_tables(inp)
+            R, dt, ds, dq = g
+
+            def resp(st_, sg_, q=1.0):
+                ctx.set_materials(st_, sg_)
+                ctx.solve_converged(q, tol, 2000)
+                return ctx.response()
+
+            errs = []
+            for arr, kind in ((dt, "sigt"), (ds, "sigs")):
+                for flat in np.argsort(-np.abs(arr).ravel())[:fd_params]:
+                    m, gg = divmod(int(flat), arr.shape[1])
+                    s1, s2, g1, g2 = st.copy(), st.copy(), sg.copy(), sg.copy()
+                    if kind == "sigt":
+                        h = 1e-4 * st[m, gg]
+                        s1[m, gg] += h
+                        s2[m, gg] -= h
+                    else:
+                        h = 1e-4 * sg[m, 0, gg, gg]
+                        g1[m, 0, gg, gg] += h
+                        g2[m, 0, gg, gg] -= h
+                    fd = (resp(s1, g1) - resp(s2, g2)) / (2 * h)
+                    errs.append({"param": "%s[%d][%d]" % (kind, m, gg), "adjoint": float(arr[m, gg]), "fd": fd,
+                                 "rel_err": abs(arr[m, gg] - fd) / abs(fd)})
+            fdq = (resp(st, sg, 1.0 + 1e-4) - resp(st, sg, 1.0 - 1e-4)) / 2e-4
+            errs.append({"param": "q", "adjoint": dq, "fd": fdq, "rel_err": abs(dq - fdq) / abs(fdq)})
+            r["fd_check"] = errs
+            r["fd_max_rel_err"] = max(e["rel_err"] for e in errs)
+        res[name] = r
+        ctx.close()
+    ref, got = grads["fp64"], grads["mixed"]
+    res["mixed"]["grad_rel_err_vs_fp64"] = max(
+        float(np.abs(got[1] - ref[1]).max() / np.abs(ref[1]).max()),
+        float(np.abs(got[2] - ref[2]).max() / np.abs(ref[2]).max()), abs(got[3] - ref[3]) / abs(ref[3]))
+    return res
+
+
 def run_gpu(args, world, rank, local):
     import ctypes
     import numpy as np
@@ -221,17 +343,11 @@ def run_gpu(args, world, rank, local):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        ctx.iterate(want_population=False)
-    e1.record(stream)
-    torch.cuda.synchronize()
+    ms = timed_steps(ctx, stream, args.steps)
     clk = clocks.stop()
     if world > 1:
         torch.distributed.barrier()
     launches = ctx.launch_count() - launches0
-    ms = e0.elapsed_time(e1) / args.steps
     fam = {f: ctx.kernel_time(f) for f in ("sweep", "ltimes", "lplustimes", "scattering", "source", "population")}
     ctx.set_timing(False)
     part = ctx.population()
@@ -312,6 +428,10 @@ def run_gpu(args, world, rank, local):
                 "step": "upload all inputs from pinned host memory + %d-iteration solve + populations to host" % niter},
         "population_after_timed_steps": part,
     }
+    if rank == 0 and world == 1 and precision == abi.FP64 and not args.no_mixed:
+        line["mixed"] = mixed_report(args, local, w, ctx, ms)
+    if rank == 0 and world == 1 and not args.no_adjoint:
+        line["adjoint"] = adjoint_report(local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, dt = cpu_run(CPU_SAMPLE, threads, 1, 2)
@@ -335,6 +455,8 @@ def main():
     ap.add_argument("--option", action="append", default=[], metavar="KEY=VALUE",
                     help="kgb_set_option knob applied before autotuning (repeatable)")
     ap.add_argument("--zones", type=int, default=0, help="override zones per axis (profiling on a smaller case)")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-form comparison")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint gradient report")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

@@ -224,9 +224,11 @@ int kgb_set_materials(kgb_ctx *ctx, const double *sigt, const double *sigs);
  * be nx*ny*nz); NULL = 1 everywhere (the default). */
 int kgb_set_response(kgb_ctx *ctx, const double *det, int64_t n);
 /* Source iterations from psi = 0 until moment 0 of successive iterates
- * satisfies max|phi_k - phi_(k-1)| <= tol * max|phi_k|, or max_iter
- * iterations ran.  *iters and *change (either may be NULL) receive the count
- * and the last relative change; reaching max_iter is not an error. */
+ * satisfies max|phi_k - phi_(k-1)| <= tol * max|phi_k|, the change has made
+ * no new minimum for 4 iterations (the rounding floor: near 1e-7 for the
+ * mixed form's FP32 state), or max_iter iterations ran.  *iters and *change
+ * (either may be NULL) receive the count and the last relative change;
+ * *change > tol tells that tol was not reached, which is not an error. */
 int kgb_solve_converged(kgb_ctx *ctx, double source_strength, double tol, int32_t max_iter, int32_t *iters,
                         double *change);
 /* The adjoint source iteration for the response, from a zero state, with the

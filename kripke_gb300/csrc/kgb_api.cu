@@ -1146,18 +1146,21 @@ int doAdjointSource(kgb_ctx *ctx) {
 }
 
 // Source iterations from a zero state until moment 0 of successive iterates
-// changes by at most tol relative to its largest magnitude.  The change is
-// measured on the moments each iteration computes first (phi = L psi of the
-// previous iterate), so the test lags one sweep and the returned state is
-// one iteration past the converged one.  With the adjoint operators
-// installed it runs the adjoint iteration with the response source.
+// changes by at most tol relative to its largest magnitude, or the change has
+// not reached a new minimum for kStall iterations (the rounding floor, which
+// the FP32 state of the mixed form meets near 1e-7).  The change is measured
+// on the moments each iteration computes first (phi = L psi of the previous
+// iterate), so the test lags one sweep and the returned state is one
+// iteration past the converged one.  With the adjoint operators installed it
+// runs the adjoint iteration with the response source.
+constexpr int kStall = 4;
 int convergeLoop(kgb_ctx *ctx, bool adjoint, double q, double tol, int max_iter, int32_t *iters, double *change) {
   int rc;
   const int64_t rows = ctx->Z * ctx->G;
   CK(cudaMemsetAsync(ctx->psi, 0, rows * ctx->D * ctx->tsz, ctx->stream));
   CK(cudaMemsetAsync(ctx->phi_prev, 0, rows * sizeof(double), ctx->stream));
-  double ch = std::numeric_limits<double>::infinity();
-  int it = 0;
+  double ch = std::numeric_limits<double>::infinity(), best = ch;
+  int it = 0, stall = 0;
   while (it < max_iter) {
     ++it;
     if ((rc = doLTimes(ctx, false))) return rc;
@@ -1185,6 +1188,12 @@ int convergeLoop(kgb_ctx *ctx, bool adjoint, double q, double tol, int max_iter,
         return fail(ctx, KGB_ERR_STATE, "the source iteration produced a non-finite flux");
       ch = amax > 0.0 ? dmax / amax : (dmax > 0.0 ? std::numeric_limits<double>::infinity() : 0.0);
       if (ch <= tol) break;
+      if (ch < best) {
+        best = ch;
+        stall = 0;
+      } else if (++stall >= kStall) {
+        break;
+      }
     }
   }
   if (iters) *iters = it;
