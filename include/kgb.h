@@ -109,7 +109,8 @@ typedef struct kgb_input {
   int32_t precision;
   int32_t num_material_subsamples;
   int32_t geometry;              /* 0: Kobayashi 3i (reference); 1: 100 cm cube, first duct leg only */
-  int32_t scatter;               /* 0: diagonal P0 (reference); 1: seeded lower-triangular downscatter */
+  int32_t scatter;               /* 0: diagonal P0 (reference); 1: seeded lower-triangular downscatter,
+                                    columns summing to (sigs[m] / sigt[m]) * sigma_t(m, g') */
   int32_t perturb;               /* 1: seeded uniform +-20% per (material, group) on sigma_t, sigma_s */
   int32_t pad_;
   uint64_t seed;
@@ -254,7 +255,49 @@ int kgb_gradient(kgb_ctx *ctx, double *response, double *dsigt, double *dsigs, d
 int kgb_gradient_unrolled(kgb_ctx *ctx, int32_t niter, double source_strength, int32_t stride, double *response,
                           double *dsigt, double *dsigs, double *dq);
 
-/* Allocation-free population edit.  No counterpart in the reference: it
+/* --- batches of independent problems ---------------------------------
+ * No counterpart in the reference (one problem per run).  A batch holds
+ * independent problems of uneven sizes, each an ordinary context with one
+ * zone set and Legendre order <= 4, all in the batch's precision, and
+ * advances them together: one launch per kernel family for all problems,
+ * the sweeps of all problems in ONE persistent cooperative launch, and a
+ * whole solve captured once into a CUDA graph and replayed.  LTimes and
+ * LPlusTimes run either as batched SIMT launches (the mixed default) or as
+ * each problem's own kernels -- the tensor-core digit products in FP64, the
+ * FP64 default -- on parallel branches of the graph.  Each problem's results
+ * equal its own context's with the same sweep tiles (and "moments_tensor" 0
+ * when the batch runs its SIMT moment kernels on an FP64 problem). */
+typedef struct kgb_batch kgb_batch;
+int kgb_batch_create(int device, int32_t precision, kgb_batch **out);
+int kgb_batch_destroy(kgb_batch *b);
+const char *kgb_batch_last_error(const kgb_batch *b);
+/* Generates a problem from `in` (precision taken from the batch); *index
+ * receives its position. */
+int kgb_batch_add(kgb_batch *b, const kgb_input *in, int32_t *index);
+int kgb_batch_size(const kgb_batch *b, int32_t *n);
+/* The problem's own context (owned by the batch): its fields can be read and
+ * written, and its kernels run on their own, between batch solves. */
+int kgb_batch_context(kgb_batch *b, int32_t index, kgb_ctx **ctx);
+/* Knobs: "sweep_tile_xy" (44, 42, 22), "sweep_tile_z", "rows_per_item" (rows
+ * of a moment / scattering work item), "graph" (1: capture solves, the
+ * default), "moments_per_problem" (1: each problem's own moment kernels;
+ * 0: batched SIMT; -1: by precision, the default).  Read-only:
+ * "graph_active" (the last solve replayed a graph),
+ * "sweep_grid" (blocks of the persistent sweep), "sweep_steps",
+ * "kernels_per_iteration". */
+int kgb_batch_set_option(kgb_batch *b, const char *key, int64_t value);
+int kgb_batch_get_option(kgb_batch *b, const char *key, int64_t *value);
+/* Times every sweep tile shape (4x4, 4x2, 2x2 x depth 2, 4, 8, 16) and row
+ * item size (256, 1024, 4096) on the batch and keeps the fastest; overwrites
+ * the problems' state. */
+int kgb_batch_autotune(kgb_batch *b, double *best_ms);
+/* niter source iterations from psi = 0 for every problem (SteadyStateSolver
+ * each); part (may be NULL) receives the particle counts [niter][n]. */
+int kgb_batch_solve(kgb_batch *b, int32_t niter, double source_strength, double *part);
+/* Kernels the batch has launched (graph replays included). */
+int kgb_batch_launch_count(kgb_batch *b, int64_t *out);
+
+/* Allocation-free population edit.  No counterpart in the reference: it/* Allocation-free population edit.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory at the point they
  * need the particle count -- code recorded into a CUDA graph, frameworks that
  * own all device memory through their own pool, latency-bound loops.  Same

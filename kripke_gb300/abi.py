@@ -28,6 +28,9 @@ EXPORTS = (
     "kgb_generate", "kgb_launch_count", "kgb_population_noalloc", "kgb_autotune", "kgb_get_option",
     "kgb_material_tables", "kgb_set_materials", "kgb_set_response", "kgb_solve_converged", "kgb_adjoint_solve",
     "kgb_response", "kgb_gradient", "kgb_gradient_unrolled",
+    "kgb_batch_create", "kgb_batch_destroy", "kgb_batch_last_error", "kgb_batch_add", "kgb_batch_size",
+    "kgb_batch_context", "kgb_batch_set_option", "kgb_batch_get_option", "kgb_batch_autotune", "kgb_batch_solve",
+    "kgb_batch_launch_count",
 )
 
 INT_FIELDS = ("quadrature/id", "quadrature/jd", "quadrature/kd", "zone_to_mixelem", "zone_to_num_mixelem",
@@ -158,6 +161,17 @@ def load():
         "kgb_gradient": ([P, ctypes.POINTER(D), P, P, ctypes.POINTER(D)], I),
         "kgb_gradient_unrolled": ([P, ctypes.c_int32, D, ctypes.c_int32, ctypes.POINTER(D), P, P,
                                    ctypes.POINTER(D)], I),
+        "kgb_batch_create": ([I, ctypes.c_int32, ctypes.POINTER(P)], I),
+        "kgb_batch_destroy": ([P], I),
+        "kgb_batch_last_error": ([P], ctypes.c_char_p),
+        "kgb_batch_add": ([P, ctypes.POINTER(KgbInput), ctypes.POINTER(ctypes.c_int32)], I),
+        "kgb_batch_size": ([P, ctypes.POINTER(ctypes.c_int32)], I),
+        "kgb_batch_context": ([P, ctypes.c_int32, ctypes.POINTER(P)], I),
+        "kgb_batch_set_option": ([P, ctypes.c_char_p, I64], I),
+        "kgb_batch_get_option": ([P, ctypes.c_char_p, ctypes.POINTER(I64)], I),
+        "kgb_batch_autotune": ([P, ctypes.POINTER(D)], I),
+        "kgb_batch_solve": ([P, ctypes.c_int32, D, P], I),
+        "kgb_batch_launch_count": ([P, ctypes.POINTER(I64)], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -395,3 +409,89 @@ def material_tables(inp):
     if rc != KGB_OK:
         raise KgbError(rc, "kgb_material_tables")
     return st, sg
+
+
+class BorrowedContext(Context):
+    """A batch problem's own context (owned by the batch; not destroyed here)."""
+
+    def __init__(self, lib, handle, inp, batch):
+        self.lib = lib
+        self.h = handle
+        self.dims = None
+        self.inp = inp
+        self._batch = batch  # keeps the batch alive
+
+    def close(self):
+        self.h = None
+
+
+class Batch:
+    """Independent problems advanced together (kgb_batch_* in include/kgb.h)."""
+
+    def __init__(self, device=0, precision=FP64):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        rc = self.lib.kgb_batch_create(device, precision, ctypes.byref(h))
+        if rc != KGB_OK:
+            raise KgbError(rc, "kgb_batch_create(%d) failed" % device)
+        self.h = h
+        self.inputs = []
+
+    def _check(self, rc, what):
+        if rc != KGB_OK:
+            raise KgbError(rc, "%s: %s" % (what, self.lib.kgb_batch_last_error(self.h).decode()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.kgb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, inp=None, **kw):
+        inp = inp if inp is not None else make_input(**kw)
+        idx = ctypes.c_int32()
+        self._check(self.lib.kgb_batch_add(self.h, ctypes.byref(inp), ctypes.byref(idx)), "kgb_batch_add")
+        self.inputs.append(inp)
+        return idx.value
+
+    def __len__(self):
+        n = ctypes.c_int32()
+        self._check(self.lib.kgb_batch_size(self.h, ctypes.byref(n)), "kgb_batch_size")
+        return n.value
+
+    def context(self, i):
+        c = ctypes.c_void_p()
+        self._check(self.lib.kgb_batch_context(self.h, i, ctypes.byref(c)), "kgb_batch_context")
+        return BorrowedContext(self.lib, c, self.inputs[i], self)
+
+    def set_option(self, key, value):
+        self._check(self.lib.kgb_batch_set_option(self.h, key.encode(), int(value)), "kgb_batch_set_option(%s)" % key)
+
+    def get_option(self, key):
+        v = ctypes.c_int64()
+        self._check(self.lib.kgb_batch_get_option(self.h, key.encode(), ctypes.byref(v)),
+                    "kgb_batch_get_option(%s)" % key)
+        return v.value
+
+    def autotune(self):
+        ms = ctypes.c_double()
+        self._check(self.lib.kgb_batch_autotune(self.h, ctypes.byref(ms)), "kgb_batch_autotune")
+        return {"iteration_ms": ms.value, "sweep_tile_xy": self.get_option("sweep_tile_xy"),
+                "sweep_tile_z": self.get_option("sweep_tile_z"), "rows_per_item": self.get_option("rows_per_item")}
+
+    def solve(self, niter, source_strength=1.0):
+        """Particle counts [niter][problems]."""
+        out = np.zeros((niter, len(self)))
+        self._check(self.lib.kgb_batch_solve(self.h, int(niter), float(source_strength), out.ctypes.data),
+                    "kgb_batch_solve")
+        return out
+
+    def launch_count(self):
+        n = ctypes.c_int64()
+        self._check(self.lib.kgb_batch_launch_count(self.h, ctypes.byref(n)), "kgb_batch_launch_count")
+        return n.value

@@ -12,7 +12,8 @@
 // The reference's inputs must be reproduced bit for bit, so every formula keeps
 // the reference's operation order.  Three generator options are new (the
 // benchmark problems need them): the 100 cm cube geometry with only the first
-// duct leg, seeded lower-triangular downscatter matrices, and a seeded +-20%
+// duct leg, seeded lower-triangular downscatter matrices (columns summing to
+// the scattering ratio sigs/sigt times sigma_t), and a seeded +-20%
 // per-(material, group) perturbation of sigma_t and sigma_s.  Random numbers:
 // std::mt19937_64(seed), u = (x >> 11) * 2^-53, drawn first for the
 // perturbation in (material, group, [t, s]) order, then for the downscatter
@@ -202,13 +203,15 @@ void materialTables(const kgb_input &in, std::vector<double> &st, std::vector<do
     std::vector<double> u((size_t)G * G);
     for (int m = 0; m < 3; ++m)
       for (int l = 0; l < L1; ++l) {
+        // columns sum to c_m * sigma_t(m, g'), c_m = sigs[m] / sigt[m] (0.5 for the reference values)
+        const double ratio = in.sigt[m] != 0.0 ? in.sigs[m] / in.sigt[m] : 0.0;
         std::fill(u.begin(), u.end(), 0.0);
         for (int g = 0; g < G; ++g)
           for (int gp = 0; gp <= g; ++gp) u[(size_t)g * G + gp] = draw(rng);
         for (int gp = 0; gp < G; ++gp) {
           double col = 0.0;
           for (int g = gp; g < G; ++g) col += u[(size_t)g * G + gp];
-          const double scale = 0.5 * st[m * G + gp] / col;
+          const double scale = ratio * st[m * G + gp] / col;
           for (int g = gp; g < G; ++g) at(m, l, g, gp) = (u[(size_t)g * G + gp] * scale) / (double)(2 * l + 1);
         }
       }

@@ -1268,6 +1268,43 @@ struct PsiBuffers {
 
 }  // namespace
 
+namespace kgb {
+int instance_view(kgb_ctx *ctx, InstanceView *v) {
+  int rc = prepare(ctx);
+  if (rc) return rc;
+  InstanceView x{};
+  x.prec = ctx->prec;
+  x.Z = ctx->Z;
+  x.G = ctx->G; x.D = ctx->D; x.M = ctx->M; x.L = ctx->L; x.Gs = ctx->Gs; x.Ds = ctx->Ds;
+  x.nx = ctx->nx; x.ny = ctx->ny; x.nz = ctx->nz;
+  x.nsdom = ctx->dc.num();
+  x.zonesets[0] = ctx->dc.Sx; x.zonesets[1] = ctx->dc.Sy; x.zonesets[2] = ctx->dc.Sz;
+  x.psi = ctx->psi; x.rhs = ctx->rhs; x.phi = ctx->phi; x.phi_out = ctx->phi_out; x.sigt = ctx->sigt;
+  for (int k = 0; k < 3; ++k) {
+    x.plane[k] = ctx->plane[k];
+    x.plane_chunk[k] = ctx->plane_chunk[k];
+  }
+  x.ell = ctx->ell; x.ellp = ctx->ellp; x.sigsT = ctx->sigsT; x.cx = ctx->cx; x.cy = ctx->cy; x.cz = ctx->cz;
+  x.w = ctx->w_d; x.vol = ctx->vol_d; x.mix_frac = ctx->mix_frac;
+  x.zmix_start = ctx->zmix_start; x.zmix_count = ctx->zmix_count; x.mix_mat = ctx->mix_mat;
+  x.gp_lo = ctx->gp_lo; x.gp_hi = ctx->gp_hi;
+  x.sdoms = ctx->sdoms_d;
+  x.vol_uniform = ctx->vol_uniform;
+  x.cls = ctx->use_recip ? ctx->cls_d : nullptr;
+  x.inv = ctx->use_recip ? ctx->inv_d : nullptr;
+  *v = x;
+  return KGB_OK;
+}
+
+int instance_moments(kgb_ctx *ctx, bool plus, cudaStream_t s) {
+  cudaStream_t keep = ctx->stream;
+  ctx->stream = s;
+  const int rc = plus ? doLPlusTimes(ctx, false) : doLTimes(ctx, false);
+  ctx->stream = keep;
+  return rc;
+}
+}  // namespace kgb
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

@@ -139,6 +139,80 @@ void launch_download_xpose(const Td *dev, double *staging, const XposeDesc &x, c
 template <typename T>
 void launch_fill(T *p, int64_t n, double v, cudaStream_t s);
 
+// Batched problems (batch.cu): one launch per kernel family covers many
+// independent problems.  Work items of the row kernels are row ranges of one
+// problem each.
+struct BatchRows {
+  int inst;
+  int pad_;
+  int64_t r0, r1;
+};
+template <typename T>
+struct BatchMom {      // LTimes: src psi, dst phi, mat ell; LPlusTimes: src phi_out, dst rhs, mat ell_plus
+  const T *src;
+  T *dst;
+  const T *mat;        // [D][M]
+  int D, M;
+};
+template <typename T>
+struct BatchScat {
+  const T *phi;
+  T *phi_out;
+  const T *sigsT;
+  ScatterArgsBase a;
+  double q;            // source strength of material 0 (Kernel::source, fused)
+};
+int moment_class(int M);
+template <typename T>
+void launch_batch_moments(const BatchMom<T> *inst, const BatchRows *items, int nitems, int M, int Dmax, bool plus,
+                          bool vec, int grid, cudaStream_t s);
+template <typename T>
+void launch_batch_scattering(const BatchScat<T> *inst, const BatchRows *items, int nitems, int L, int grid,
+                             cudaStream_t s);
+// Persistent batched sweep: zero every plane, then every global hyperplane
+// step of every problem, separated by a bounded grid barrier; launched
+// cooperatively so all blocks are resident.
+struct BatchZero {
+  int inst, plane;
+  int64_t begin, end;  // element range of the problem's plane array
+};
+struct BatchSweepPlan {
+  const int4 *items;      // (problem, subdomain, tile, chain block), grouped by global step
+  const int *step_off;    // [nsteps + 1]
+  int nsteps;
+  const BatchZero *zero;  // plane zeroing ranges
+  int nzero;
+  unsigned int *bar;      // [2] grid barrier: arrivals, generation (zero before a launch)
+  int *err;               // set when a barrier wait gives up
+};
+template <typename T>
+int batch_sweep_grid(int tx, int ty, int nsm);
+template <typename T>
+cudaError_t launch_batch_sweep(const SweepArgs<T> *inst, const BatchSweepPlan &p, int tx, int ty, int grid,
+                               cudaStream_t s);
+// per-problem fixed-order sums of the fused population partials: out[i] = sum of slots[i][0 .. n[i])
+void launch_batch_pop_finish(const double *const *slots, const int64_t *n, int ninst, double *out, cudaStream_t s);
+
+// Device view of one prepared context (kgb_api.cu), for the batched driver.
+struct InstanceView {
+  int prec;
+  int64_t Z;
+  int G, D, M, L, Gs, Ds, nx, ny, nz, nsdom, zonesets[3];
+  void *psi, *rhs, *phi, *phi_out, *sigt, *plane[3];
+  int64_t plane_chunk[3];
+  void *ell, *ellp, *sigsT, *cx, *cy, *cz;
+  const double *w, *vol, *mix_frac;
+  const int *zmix_start, *zmix_count, *mix_mat, *gp_lo, *gp_hi;
+  const SdomDesc *sdoms;
+  double vol_uniform;
+  const uint16_t *cls;  // tabulated sweep reciprocals, or null (divide per cell)
+  const double *inv;
+};
+int instance_view(kgb_ctx *ctx, InstanceView *v);
+// The context's own LTimes (plus = false) or LPlusTimes, overwriting phi / rhs,
+// launched on stream s (tensor-core or SIMT as the context chooses).
+int instance_moments(kgb_ctx *ctx, bool plus, cudaStream_t s);
+
 // Response, adjoint source and gradients (adjoint.cu).
 struct MixArgs {
   int64_t Z;

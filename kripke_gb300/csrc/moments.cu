@@ -29,102 +29,73 @@ __device__ __forceinline__ void store16(T *dst, const T (&src)[Vec16<T>::n]) {
   *reinterpret_cast<typename Vec16<T>::type *>(dst) = *reinterpret_cast<const typename Vec16<T>::type *>(src);
 }
 
-// VEC: every psi row starts on a 16-byte boundary (D*sizeof(T) % 16 == 0).
-template <typename T, int MB, bool VEC>
-__global__ void __launch_bounds__(kMomThreads) ltimes_kernel(const T *__restrict__ psi, T *__restrict__ phi,
-                                                            const T *__restrict__ ell_dm, int64_t rows, int D,
-                                                            int M, int m0, int mc, bool accumulate) {
-  constexpr int V = Vec16<T>::n;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *sell = reinterpret_cast<T *>(smem_raw);  // [D][MB]
+// Rows of the two transforms, shared by the per-call kernels and the batched
+// kernels (one launch over many problems).  VEC: every psi / rhs row starts on
+// a 16-byte boundary (D*sizeof(T) % 16 == 0).
+
+// L rows [d][MB] (moments m0 .. m0+mc-1, zero padded) into shared memory
+template <typename T, int MB>
+__device__ __forceinline__ void loadRows(T *sm, const T *__restrict__ mat_dm, int D, int M, int m0, int mc) {
   for (int i = threadIdx.x; i < D * MB; i += blockDim.x) {
     const int d = i / MB, m = i - d * MB;
-    sell[i] = (m < mc) ? ell_dm[(int64_t)d * M + m0 + m] : T(0);
+    sm[i] = (m < mc) ? mat_dm[(int64_t)d * M + m0 + m] : T(0);
   }
-  __syncthreads();
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
-    T acc[MB];
+}
+
+// phi(m0 .. m0+mc-1) of one (zone, group) row: sum over directions, ascending
+template <typename T, int MB, bool VEC>
+__device__ __forceinline__ void ltimesRow(const T *__restrict__ p, const T *sell, int D, T *o, int mc,
+                                          bool accumulate) {
+  constexpr int V = Vec16<T>::n;
+  T acc[MB];
 #pragma unroll
-    for (int m = 0; m < MB; ++m) acc[m] = T(0);
-    const T *p = psi + r * D;
-    const int dv = VEC ? D - D % V : 0;
-    for (int d0 = 0; d0 < dv; d0 += V) {
-      T pv[V];
-      load16(pv, p + d0);
+  for (int m = 0; m < MB; ++m) acc[m] = T(0);
+  const int dv = VEC ? D - D % V : 0;
+  for (int d0 = 0; d0 < dv; d0 += V) {
+    T pv[V];
+    load16(pv, p + d0);
 #pragma unroll
-      for (int v = 0; v < V; ++v) {
-        const T *e = sell + (d0 + v) * MB;
-#pragma unroll
-        for (int m = 0; m < MB; m += V) {
-          T ev[V];
-          load16(ev, e + m);
-#pragma unroll
-          for (int u = 0; u < V; ++u) acc[m + u] += ev[u] * pv[v];
-        }
-      }
-    }
-    for (int d = dv; d < D; ++d) {
-      const T pd = p[d];
-      const T *e = sell + d * MB;
+    for (int v = 0; v < V; ++v) {
+      const T *e = sell + (d0 + v) * MB;
 #pragma unroll
       for (int m = 0; m < MB; m += V) {
         T ev[V];
         load16(ev, e + m);
 #pragma unroll
-        for (int u = 0; u < V; ++u) acc[m + u] += ev[u] * pd;
+        for (int u = 0; u < V; ++u) acc[m + u] += ev[u] * pv[v];
       }
     }
-    T *o = phi + r * M + m0;
-#pragma unroll
-    for (int m = 0; m < MB; ++m)
-      if (m < mc) o[m] = accumulate ? o[m] + acc[m] : acc[m];
   }
+  for (int d = dv; d < D; ++d) {
+    const T pd = p[d];
+    const T *e = sell + d * MB;
+#pragma unroll
+    for (int m = 0; m < MB; m += V) {
+      T ev[V];
+      load16(ev, e + m);
+#pragma unroll
+      for (int u = 0; u < V; ++u) acc[m + u] += ev[u] * pd;
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < MB; ++m)
+    if (m < mc) o[m] = accumulate ? o[m] + acc[m] : acc[m];
 }
 
+// rhs(d) of one (zone, group) row: sum over moments, ascending
 template <typename T, int MB, bool VEC>
-__global__ void __launch_bounds__(kMomThreads) lplustimes_kernel(const T *__restrict__ phi_out, T *__restrict__ rhs,
-                                                                const T *__restrict__ ellp_dm, int64_t rows, int D,
-                                                                int M, bool accumulate) {
+__device__ __forceinline__ void lplusRow(const T *__restrict__ src, const T *sel, int D, int M, T *o,
+                                         bool accumulate) {
   constexpr int V = Vec16<T>::n;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *sel = reinterpret_cast<T *>(smem_raw);  // [D][MB]
-  for (int i = threadIdx.x; i < D * MB; i += blockDim.x) {
-    const int d = i / MB, m = i - d * MB;
-    sel[i] = (m < M) ? ellp_dm[(int64_t)d * M + m] : T(0);
-  }
-  __syncthreads();
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
-    T po[MB];
-    const T *src = phi_out + r * M;
+  T po[MB];
 #pragma unroll
-    for (int m = 0; m < MB; ++m) po[m] = (m < M) ? src[m] : T(0);
-    T *o = rhs + r * D;
-    const int dv = VEC ? D - D % V : 0;
-    for (int d0 = 0; d0 < dv; d0 += V) {
-      T out[V];
+  for (int m = 0; m < MB; ++m) po[m] = (m < M) ? src[m] : T(0);
+  const int dv = VEC ? D - D % V : 0;
+  for (int d0 = 0; d0 < dv; d0 += V) {
+    T out[V];
 #pragma unroll
-      for (int v = 0; v < V; ++v) {
-        const T *e = sel + (d0 + v) * MB;
-        T acc = T(0);
-#pragma unroll
-        for (int m = 0; m < MB; m += V) {
-          T ev[V];
-          load16(ev, e + m);
-#pragma unroll
-          for (int u = 0; u < V; ++u) acc += ev[u] * po[m + u];
-        }
-        out[v] = acc;
-      }
-      if (accumulate) {
-        T old[V];
-        load16(old, o + d0);
-#pragma unroll
-        for (int v = 0; v < V; ++v) out[v] = old[v] + out[v];
-      }
-      store16(o + d0, out);
-    }
-    for (int d = dv; d < D; ++d) {
-      const T *e = sel + d * MB;
+    for (int v = 0; v < V; ++v) {
+      const T *e = sel + (d0 + v) * MB;
       T acc = T(0);
 #pragma unroll
       for (int m = 0; m < MB; m += V) {
@@ -133,7 +104,74 @@ __global__ void __launch_bounds__(kMomThreads) lplustimes_kernel(const T *__rest
 #pragma unroll
         for (int u = 0; u < V; ++u) acc += ev[u] * po[m + u];
       }
-      o[d] = accumulate ? o[d] + acc : acc;
+      out[v] = acc;
+    }
+    if (accumulate) {
+      T old[V];
+      load16(old, o + d0);
+#pragma unroll
+      for (int v = 0; v < V; ++v) out[v] = old[v] + out[v];
+    }
+    store16(o + d0, out);
+  }
+  for (int d = dv; d < D; ++d) {
+    const T *e = sel + d * MB;
+    T acc = T(0);
+#pragma unroll
+    for (int m = 0; m < MB; m += V) {
+      T ev[V];
+      load16(ev, e + m);
+#pragma unroll
+      for (int u = 0; u < V; ++u) acc += ev[u] * po[m + u];
+    }
+    o[d] = accumulate ? o[d] + acc : acc;
+  }
+}
+
+template <typename T, int MB, bool VEC>
+__global__ void __launch_bounds__(kMomThreads) ltimes_kernel(const T *__restrict__ psi, T *__restrict__ phi,
+                                                            const T *__restrict__ ell_dm, int64_t rows, int D,
+                                                            int M, int m0, int mc, bool accumulate) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *sell = reinterpret_cast<T *>(smem_raw);  // [D][MB]
+  loadRows<T, MB>(sell, ell_dm, D, M, m0, mc);
+  __syncthreads();
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x)
+    ltimesRow<T, MB, VEC>(psi + r * D, sell, D, phi + r * M + m0, mc, accumulate);
+}
+
+template <typename T, int MB, bool VEC>
+__global__ void __launch_bounds__(kMomThreads) lplustimes_kernel(const T *__restrict__ phi_out, T *__restrict__ rhs,
+                                                                const T *__restrict__ ellp_dm, int64_t rows, int D,
+                                                                int M, bool accumulate) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *sel = reinterpret_cast<T *>(smem_raw);  // [D][MB]
+  loadRows<T, MB>(sel, ellp_dm, D, M, 0, M);
+  __syncthreads();
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x)
+    lplusRow<T, MB, VEC>(phi_out + r * M, sel, D, M, rhs + r * D, accumulate);
+}
+
+// Batched transforms: work items are row ranges of one problem each; a block
+// reloads the L / L+ rows when its next item belongs to another problem.
+template <typename T, int MB, bool VEC, bool PLUS>
+__global__ void __launch_bounds__(kMomThreads) batch_moments_kernel(const BatchMom<T> *__restrict__ inst,
+                                                                   const BatchRows *__restrict__ items, int nitems) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *sm = reinterpret_cast<T *>(smem_raw);  // [D][MB]
+  int cur = -1;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const BatchRows w = items[it];
+    const BatchMom<T> b = inst[w.inst];
+    if (w.inst != cur) {
+      __syncthreads();
+      loadRows<T, MB>(sm, b.mat, b.D, b.M, 0, b.M);
+      __syncthreads();
+      cur = w.inst;
+    }
+    for (int64_t r = w.r0 + threadIdx.x; r < w.r1; r += blockDim.x) {
+      if (PLUS) lplusRow<T, MB, VEC>(b.src + r * b.M, sm, b.D, b.M, b.dst + r * b.D, false);
+      else ltimesRow<T, MB, VEC>(b.src + r * b.D, sm, b.D, b.dst + r * b.M, b.M, false);
     }
   }
 }
@@ -211,6 +249,45 @@ void launch_lplustimes(const T *phi_out, T *rhs, const T *ellp_dm, int64_t rows,
   byMoments<T, LPlusLaunch>(M, KGB_L(4), KGB_L(12), KGB_L(16), KGB_L(28), KGB_L(36), KGB_L(52), KGB_L(64));
 #undef KGB_L
 }
+
+// Batched launches: MB is the moment class of every problem in the items (all
+// share one vector width); FP64 LPlusTimes runs scalar like the per-call path.
+template <typename T, int MB>
+struct BatchMomLaunch {
+  const BatchMom<T> *inst; const BatchRows *items; int nitems, Dmax; bool plus, vec; int grid; cudaStream_t s;
+  void operator()() const {
+    const size_t smem = sizeof(T) * (size_t)Dmax * MB;
+    auto go = [&](auto kernel) {
+      setSmem(kernel, smem);
+      kernel<<<grid, kMomThreads, smem, s>>>(inst, items, nitems);
+    };
+    if (plus) {
+      if (vec) go(batch_moments_kernel<T, MB, true, true>);
+      else go(batch_moments_kernel<T, MB, false, true>);
+    } else {
+      if (vec) go(batch_moments_kernel<T, MB, true, false>);
+      else go(batch_moments_kernel<T, MB, false, false>);
+    }
+  }
+};
+
+template <typename T>
+void launch_batch_moments(const BatchMom<T> *inst, const BatchRows *items, int nitems, int M, int Dmax, bool plus,
+                          bool vec, int grid, cudaStream_t s) {
+  if (nitems <= 0) return;
+#define KGB_L(MBV) BatchMomLaunch<T, MBV>{inst, items, nitems, Dmax, plus, vec, grid, s}
+  byMoments<T, BatchMomLaunch>(M, KGB_L(4), KGB_L(12), KGB_L(16), KGB_L(28), KGB_L(36), KGB_L(52), KGB_L(64));
+#undef KGB_L
+}
+
+int moment_class(int M) {
+  return M <= 4 ? 4 : M <= 12 ? 12 : M <= 16 ? 16 : M <= 28 ? 28 : M <= 36 ? 36 : M <= 52 ? 52 : 64;
+}
+
+template void launch_batch_moments<double>(const BatchMom<double> *, const BatchRows *, int, int, int, bool, bool, int,
+                                           cudaStream_t);
+template void launch_batch_moments<float>(const BatchMom<float> *, const BatchRows *, int, int, int, bool, bool, int,
+                                          cudaStream_t);
 
 template void launch_ltimes<double>(const double *, double *, const double *, int64_t, int, int, bool, cudaStream_t);
 template void launch_ltimes<float>(const float *, float *, const float *, int64_t, int, int, bool, cudaStream_t);

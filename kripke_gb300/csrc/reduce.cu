@@ -98,6 +98,17 @@ __global__ void __launch_bounds__(kRedThreads) finish_kernel(const double *__res
   const double b = blockSum(acc);
   if (threadIdx.x == 0) out[0] = add ? out[0] + b : b;
 }
+// one block per problem: the finish_kernel sum of that problem's partials
+__global__ void __launch_bounds__(kRedThreads) batch_pop_finish_kernel(const double *const *__restrict__ slots,
+                                                                      const int64_t *__restrict__ n,
+                                                                      double *__restrict__ out) {
+  const double *p = slots[blockIdx.x];
+  const int nn = (int)n[blockIdx.x];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nn; i += blockDim.x) acc += p[i];
+  const double b = blockSum(acc);
+  if (threadIdx.x == 0) out[blockIdx.x] = b;
+}
 }  // namespace
 
 template <typename T>
@@ -120,6 +131,10 @@ void launch_leakage(const T *plane, int64_t nelem, int Gs, int Ds, int dlo, int 
                     const double *wa, const double *wb, double *partials, int nblocks, double *out, cudaStream_t s) {
   leakage_kernel<T><<<nblocks, kRedThreads, 0, s>>>(plane, nelem, Gs, Ds, dlo, na, w, cosv, wa, wb, partials);
   finish_kernel<<<1, kRedThreads, 0, s>>>(partials, nblocks, 1, 0, out, true);
+}
+
+void launch_batch_pop_finish(const double *const *slots, const int64_t *n, int ninst, double *out, cudaStream_t s) {
+  if (ninst > 0) batch_pop_finish_kernel<<<ninst, kRedThreads, 0, s>>>(slots, n, out);
 }
 
 void launch_sum_partials(const double *partials, int64_t n, double *out, cudaStream_t s) {

@@ -25,48 +25,73 @@ __host__ __device__ constexpr int legendreOf(int m) {
   return l;
 }
 
+// One (zone, destination group) row of phi_out; with SRC the isotropic source
+// of material 0 is added to moment 0 afterwards, as Kernel::source does.
+template <typename T, int LMAX, bool SRC>
+__device__ __forceinline__ void scatterRow(const T *__restrict__ phi, T *__restrict__ phi_out,
+                                           const T *__restrict__ sigsT, const ScatterArgsBase &a, int64_t r,
+                                           bool accumulate, double q) {
+  constexpr int MM = (LMAX + 1) * (LMAX + 1);
+  const int Gd = a.dst_ghi - a.dst_glo;
+  const int64_t z = r / Gd;
+  const int g = a.dst_glo + (int)(r - z * Gd);
+  const int ms = a.zmix_start[z], mcnt = a.zmix_count[z];
+  // a single-material zone has fraction exactly 1, where the reference's
+  // 0 + sigs*fraction is sigs itself
+  const bool pure = mcnt == 1 && a.mix_frac[ms] == 1.0;
+  const int mat0 = a.mix_mat[ms];
+  const int lo = max(a.gp_lo[g], a.src_glo);
+  const int hi = min(a.gp_hi[g] + 1, a.src_ghi);
+  T acc[MM];
+#pragma unroll
+  for (int m = 0; m < MM; ++m) acc[m] = T(0);
+  for (int gp = lo; gp < hi; ++gp) {
+    T sl[LMAX + 1];
+    if (pure) {
+#pragma unroll
+      for (int l = 0; l <= LMAX; ++l) sl[l] = sigsT[(((int64_t)mat0 * (LMAX + 1) + l) * a.G + gp) * a.G + g];
+    } else {
+#pragma unroll
+      for (int l = 0; l <= LMAX; ++l) sl[l] = T(0);
+      for (int x = 0; x < mcnt; ++x) {
+        const int mat = a.mix_mat[ms + x];
+        const T f = (T)a.mix_frac[ms + x];
+#pragma unroll
+        for (int l = 0; l <= LMAX; ++l) sl[l] += sigsT[(((int64_t)mat * (LMAX + 1) + l) * a.G + gp) * a.G + g] * f;
+      }
+    }
+    const T *ph = phi + (z * a.G + gp) * MM;
+#pragma unroll
+    for (int m = 0; m < MM; ++m) acc[m] += sl[legendreOf(m)] * ph[m];
+  }
+  T *o = phi_out + (z * a.G + g) * MM;
+#pragma unroll
+  for (int m = 0; m < MM; ++m) o[m] = accumulate ? o[m] + acc[m] : acc[m];
+  if (SRC)
+    for (int x = 0; x < mcnt; ++x)
+      if (a.mix_mat[ms + x] == 0) o[0] += (T)(q * a.mix_frac[ms + x]);
+}
+
 template <typename T, int LMAX>
 __global__ void __launch_bounds__(kScatThreads) scattering_kernel(const T *__restrict__ phi, T *__restrict__ phi_out,
                                                                  const T *__restrict__ sigsT, const ScatterArgsBase a,
                                                                  bool accumulate) {
-  constexpr int MM = (LMAX + 1) * (LMAX + 1);
-  const int Gd = a.dst_ghi - a.dst_glo;
-  const int64_t rows = a.Z * Gd;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t z = r / Gd;
-    const int g = a.dst_glo + (int)(r - z * Gd);
-    const int ms = a.zmix_start[z], mcnt = a.zmix_count[z];
-    // a single-material zone has fraction exactly 1, where the reference's
-    // 0 + sigs*fraction is sigs itself
-    const bool pure = mcnt == 1 && a.mix_frac[ms] == 1.0;
-    const int mat0 = a.mix_mat[ms];
-    const int lo = max(a.gp_lo[g], a.src_glo);
-    const int hi = min(a.gp_hi[g] + 1, a.src_ghi);
-    T acc[MM];
-#pragma unroll
-    for (int m = 0; m < MM; ++m) acc[m] = T(0);
-    for (int gp = lo; gp < hi; ++gp) {
-      T sl[LMAX + 1];
-      if (pure) {
-#pragma unroll
-        for (int l = 0; l <= LMAX; ++l) sl[l] = sigsT[(((int64_t)mat0 * (LMAX + 1) + l) * a.G + gp) * a.G + g];
-      } else {
-#pragma unroll
-        for (int l = 0; l <= LMAX; ++l) sl[l] = T(0);
-        for (int x = 0; x < mcnt; ++x) {
-          const int mat = a.mix_mat[ms + x];
-          const T f = (T)a.mix_frac[ms + x];
-#pragma unroll
-          for (int l = 0; l <= LMAX; ++l) sl[l] += sigsT[(((int64_t)mat * (LMAX + 1) + l) * a.G + gp) * a.G + g] * f;
-        }
-      }
-      const T *ph = phi + (z * a.G + gp) * MM;
-#pragma unroll
-      for (int m = 0; m < MM; ++m) acc[m] += sl[legendreOf(m)] * ph[m];
-    }
-    T *o = phi_out + (z * a.G + g) * MM;
-#pragma unroll
-    for (int m = 0; m < MM; ++m) o[m] = accumulate ? o[m] + acc[m] : acc[m];
+  const int64_t rows = a.Z * (a.dst_ghi - a.dst_glo);
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x)
+    scatterRow<T, LMAX, false>(phi, phi_out, sigsT, a, r, accumulate, 0.0);
+}
+
+// Batched scattering with the source fused: work items are row ranges of one
+// problem each.
+template <typename T, int LMAX>
+__global__ void __launch_bounds__(kScatThreads) batch_scattering_kernel(const BatchScat<T> *__restrict__ inst,
+                                                                       const BatchRows *__restrict__ items,
+                                                                       int nitems) {
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const BatchRows w = items[it];
+    const BatchScat<T> &b = inst[w.inst];
+    for (int64_t r = w.r0 + threadIdx.x; r < w.r1; r += blockDim.x)
+      scatterRow<T, LMAX, true>(b.phi, b.phi_out, b.sigsT, b.a, r, false, b.q);
   }
 }
 
@@ -117,6 +142,23 @@ void launch_source(T *phi_out, int64_t nmix, const int *mix_zone, const int *mix
   source_kernel<T><<<gridFor(n, 256), 256, 0, s>>>(phi_out, nmix, mix_zone, mix_mat, mix_frac, G, M, strength);
 }
 
+template <typename T>
+void launch_batch_scattering(const BatchScat<T> *inst, const BatchRows *items, int nitems, int L, int grid,
+                             cudaStream_t s) {
+  if (nitems <= 0) return;
+  switch (L) {
+    case 0: batch_scattering_kernel<T, 0><<<grid, kScatThreads, 0, s>>>(inst, items, nitems); break;
+    case 1: batch_scattering_kernel<T, 1><<<grid, kScatThreads, 0, s>>>(inst, items, nitems); break;
+    case 2: batch_scattering_kernel<T, 2><<<grid, kScatThreads, 0, s>>>(inst, items, nitems); break;
+    case 3: batch_scattering_kernel<T, 3><<<grid, kScatThreads, 0, s>>>(inst, items, nitems); break;
+    default: batch_scattering_kernel<T, 4><<<grid, kScatThreads, 0, s>>>(inst, items, nitems); break;
+  }
+}
+
+template void launch_batch_scattering<double>(const BatchScat<double> *, const BatchRows *, int, int, int,
+                                              cudaStream_t);
+template void launch_batch_scattering<float>(const BatchScat<float> *, const BatchRows *, int, int, int,
+                                             cudaStream_t);
 template void launch_scattering<double>(const double *, double *, const double *, const ScatterArgsBase &, bool, cudaStream_t);
 template void launch_scattering<float>(const float *, float *, const float *, const ScatterArgsBase &, bool, cudaStream_t);
 template void launch_source<double>(double *, int64_t, const int *, const int *, const double *, int, int, double, cudaStream_t);

@@ -25,9 +25,16 @@
 // 1/den; the cell then multiplies (psi differs from num/den by at most 1.5 ulp).
 //
 // The transposed (adjoint) sweep is the same recurrence run from the opposite
-// corner: the diamond-difference matrix of a direction is triangular in its
-// sweep order with the alternating face coupling (2, -2, 2, ...) along each
-// axis, and its transpose has the same entries ordered from the other end.
+// corner (flip): along a direction the diamond-difference coupling of two
+// cells is a product of 2c/den and -1 face factors, and read backwards it
+// differs only in which end's c = 2|cos|/delta enters, so on a mesh with
+// varying spacing the transpose is the reversed sweep conjugated by the cell
+// volumes, which the caller applies.
+//
+// The tile body is a device function shared by the per-step launches here
+// and by the persistent batched sweep (batch.cu), which passes COH = true to
+// read the running face planes through L2 only: there the tiles of one step
+// read faces written by other blocks earlier in the same launch.
 //
 // The population edit (Kernel::population) is fused: each thread accumulates
 // volume * psi over its cells (FP64, or compensated FP32 in the mixed form),
@@ -69,20 +76,29 @@ __device__ __forceinline__ double blockSum128(double v) {
   double r = 0.0;
   if (threadIdx.x == 0)
     for (int i = 0; i < kSweepThreads / 32; ++i) r += part[i];
+  __syncthreads();  // part is reused by the block's next tile
   return r;
+}
+
+template <bool COH, typename T>
+__device__ __forceinline__ T ldFace(const T *p) {
+  if constexpr (COH) return __ldcg(p);
+  else return *p;
 }
 
 }  // namespace
 
-template <typename T, int TX, int TY, bool RECIP, bool POP>
-__global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const SweepArgs<T> a) {
-  const int sdom = a.wave[blockIdx.z];
+// One tile of one subdomain for one block of chains: tile is the index into
+// a.tiles, cb the chain block (chains cb*blockDim.x + threadIdx.x) of ncb.
+template <typename T, int TX, int TY, bool RECIP, bool POP, bool COH>
+__device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom, const int tile, const int cb,
+                                          const int ncb) {
   const SdomDesc sd = a.sdoms[sdom];
   // the adjoint sweep (transposed operator) runs every direction in its reversed orientation
   const int sid = a.flip ? -sd.id : sd.id, sjd = a.flip ? -sd.jd : sd.jd, skd = a.flip ? -sd.kd : sd.kd;
-  const int4 t = a.tiles[a.tile_off + blockIdx.y];
+  const int4 t = a.tiles[tile];
   const int nchain = a.Ds * a.Gs;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = cb * blockDim.x + threadIdx.x;
   typename AccOf<T>::type pop;
   double wd = 0.0;
   if (c < nchain) {
@@ -123,7 +139,7 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const SweepAr
     for (int ii = 0; ii < TX; ++ii)
 #pragma unroll
       for (int jj = 0; jj < TY; ++jj)
-        bo[ii][jj] = (iv[ii] && jv[jj]) ? kpl[((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c] : T(0);
+        bo[ii][jj] = (iv[ii] && jv[jj]) ? ldFace<COH>(kpl + ((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c) : T(0);
 
     const T *__restrict__ rhs = a.rhs;
     T *__restrict__ psi = a.psi;
@@ -154,13 +170,13 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const SweepAr
       }
       T fr[TX];
 #pragma unroll
-      for (int ii = 0; ii < TX; ++ii) fr[ii] = iv[ii] ? jpl[((int64_t)k * a.nxs + iloc[ii]) * nchain + c] : T(0);
+      for (int ii = 0; ii < TX; ++ii) fr[ii] = iv[ii] ? ldFace<COH>(jpl + ((int64_t)k * a.nxs + iloc[ii]) * nchain + c) : T(0);
 #pragma unroll
       for (int jj = 0; jj < TY; ++jj) {
         if (!jv[jj]) continue;
         const int j = jloc[jj];
         T *const lfp = ipl + ((int64_t)k * a.nys + j) * nchain + c;
-        T lf = *lfp;
+        T lf = ldFace<COH>(lfp);
         const int64_t zrow = (zslice + (sd.jo + j)) * a.nx + sd.io;
 #pragma unroll
         for (int ii = 0; ii < TX; ++ii) {
@@ -200,8 +216,80 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const SweepAr
     double v = pop.value() * wd;
     if (a.vol_uniform > 0.0) v *= a.vol_uniform;
     const double b = blockSum128(v);
-    if (threadIdx.x == 0)
-      a.pop[((int64_t)(a.tile_off + blockIdx.y) * a.nsdom + sdom) * gridDim.x + blockIdx.x] = b;
+    if (threadIdx.x == 0) a.pop[((int64_t)tile * a.nsdom + sdom) * ncb + cb] = b;
+  }
+}
+
+template <typename T, int TX, int TY, bool RECIP, bool POP>
+__global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const __grid_constant__ SweepArgs<T> a) {
+  sweepTile<T, TX, TY, RECIP, POP, false>(a, a.wave[blockIdx.z], a.tile_off + blockIdx.y, blockIdx.x, gridDim.x);
+}
+
+namespace {
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // a barrier wait gives up after 2 s
+
+__device__ __forceinline__ unsigned long long globalNs() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid-wide barrier of a cooperative launch (all blocks resident): arrivals
+// are counted in bar[0]; the last block resets the count and advances the
+// generation bar[1], which the others wait on -- for at most
+// kBarrierLimitNs, after which they record the failure in *err and go on.
+// Once *err is set no block waits any more, so a failed launch ends quickly.
+__device__ __forceinline__ void gridBarrier(unsigned int *bar, unsigned int nblocks, int *err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int *gen = bar + 1;
+    volatile int *failed = err;
+    const unsigned int g = *gen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == nblocks - 1u) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const unsigned long long t0 = globalNs();
+      while (*gen == g && !*failed) {
+        __nanosleep(64);
+        if (globalNs() - t0 > kBarrierLimitNs) {
+          atomicExch(err, 1);
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+}  // namespace
+
+// Persistent sweep of many independent problems: every block takes work items
+// of the current global step (one tile of one subdomain for one chain block
+// of one problem); a grid barrier separates the steps.  Faces between tiles
+// move through the plane arrays, read through L2.
+template <typename T, int TX, int TY>
+__global__ void __launch_bounds__(kSweepThreads) batch_sweep_kernel(const SweepArgs<T> *__restrict__ inst,
+                                                                   const BatchSweepPlan p) {
+  const unsigned int nb = gridDim.x;
+  for (int i = blockIdx.x; i < p.nzero; i += gridDim.x) {
+    const BatchZero z = p.zero[i];
+    const SweepArgs<T> &a = inst[z.inst];
+    T *base = z.plane == 0 ? a.iplane : (z.plane == 1 ? a.jplane : a.kplane);
+    for (int64_t e = z.begin + threadIdx.x; e < z.end; e += blockDim.x) base[e] = T(0);
+  }
+  gridBarrier(p.bar, nb, p.err);
+  for (int st = 0; st < p.nsteps; ++st) {
+    for (int i = p.step_off[st] + blockIdx.x; i < p.step_off[st + 1]; i += gridDim.x) {
+      const int4 w = p.items[i];
+      const SweepArgs<T> &a = inst[w.x];
+      const int ncb = (a.Ds * a.Gs + kSweepThreads - 1) / kSweepThreads;
+      if (a.cls != nullptr) sweepTile<T, TX, TY, true, true, true>(a, w.y, w.z, w.w, ncb);
+      else sweepTile<T, TX, TY, false, true, true>(a, w.y, w.z, w.w, ncb);
+    }
+    gridBarrier(p.bar, nb, p.err);
   }
 }
 
@@ -226,6 +314,39 @@ void launch_sweep_step(const SweepArgs<T> &a, int ntiles, int nwave, cudaStream_
   else launchTile<T, 2, 2>(a, grid, s);
 }
 
+template <typename T>
+int batch_sweep_grid(int tx, int ty, int nsm) {
+  int nb = 0;
+  if (tx == 4 && ty == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_sweep_kernel<T, 4, 4>, kSweepThreads, 0);
+  else if (tx == 4 && ty == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_sweep_kernel<T, 4, 2>, kSweepThreads, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_sweep_kernel<T, 2, 2>, kSweepThreads, 0);
+  return nb * nsm;
+}
+
+template <typename T>
+cudaError_t launch_batch_sweep(const SweepArgs<T> *inst, const BatchSweepPlan &p, int tx, int ty, int grid,
+                               cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kSweepThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (tx == 4 && ty == 4) return cudaLaunchKernelEx(&cfg, batch_sweep_kernel<T, 4, 4>, inst, p);
+  if (tx == 4 && ty == 2) return cudaLaunchKernelEx(&cfg, batch_sweep_kernel<T, 4, 2>, inst, p);
+  return cudaLaunchKernelEx(&cfg, batch_sweep_kernel<T, 2, 2>, inst, p);
+}
+
+template int batch_sweep_grid<double>(int, int, int);
+template int batch_sweep_grid<float>(int, int, int);
+template cudaError_t launch_batch_sweep<double>(const SweepArgs<double> *, const BatchSweepPlan &, int, int, int,
+                                                cudaStream_t);
+template cudaError_t launch_batch_sweep<float>(const SweepArgs<float> *, const BatchSweepPlan &, int, int, int,
+                                               cudaStream_t);
 template void launch_sweep_step<double>(const SweepArgs<double> &, int, int, cudaStream_t);
 template void launch_sweep_step<float>(const SweepArgs<float> &, int, int, cudaStream_t);
 

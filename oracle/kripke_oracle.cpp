@@ -564,17 +564,20 @@ bool generate(orc_problem &p) {
       // New generator option: per material m and Legendre order l a seeded
       // lower-triangular matrix U[g][g'] (g >= g', uniform [0,1), drawn in
       // (m, l, g, g') order), columns scaled so that sum_g S0[g][g'] =
-      // 0.5 * sigma_t(m, g'), order l damped by 1/(2l+1).
+      // c_m * sigma_t(m, g') with the scattering ratio c_m = sigs[m] / sigt[m]
+      // of the input (0.5 for the reference cross sections), order l damped
+      // by 1/(2l+1).
       std::vector<double> U((size_t)G * G);
       for (int m = 0; m < 3; ++m)
         for (int l = 0; l <= p.L; ++l) {
+          const double ratio = in.sigt[m] != 0.0 ? in.sigs[m] / in.sigt[m] : 0.0;
           std::fill(U.begin(), U.end(), 0.0);
           for (int g = 0; g < G; ++g)
             for (int gp = 0; gp <= g; ++gp) U[(size_t)g * G + gp] = unitDraw(rng);
           for (int gp = 0; gp < G; ++gp) {
             double col = 0.0;
             for (int g = gp; g < G; ++g) col += U[(size_t)g * G + gp];
-            double scale = 0.5 * sigt_mg[m * G + gp] / col;
+            double scale = ratio * sigt_mg[m * G + gp] / col;
             for (int g = gp; g < G; ++g) at(m, l, g, gp) = (U[(size_t)g * G + gp] * scale) / (double)(2 * l + 1);
           }
         }

@@ -1,0 +1,109 @@
+"""Batched problems: one launch per kernel family, the sweeps of every problem
+in one persistent launch, a solve replayed from a CUDA graph.
+
+Parity: each problem's particle counts and psi equal, bit for bit, those of
+the same problem's own context run with the batch's sweep tiles (and the SIMT
+moment kernels when the batch runs its batched SIMT moments), since the
+arithmetic is term for term the same; the particle counts match the CPU
+oracle within 1e-12 (FP64).
+"""
+import numpy as np
+import pytest
+
+from kripke_gb300.batching import uneven_inputs
+
+
+def small_set(kgb, n=5, seed=11, precision=None):
+    kw = dict(zones=(3, 10), groups=(2, 4, 8), directions=(32, 48, 64), legendre=(0, 2, 4))
+    return uneven_inputs(n, seed=seed, precision=kgb.FP64 if precision is None else precision, **kw)
+
+
+def make_batch(kgb, inputs, precision):
+    b = kgb.Batch(precision=precision)
+    for inp in inputs:
+        b.add(inp)
+    return b
+
+
+def single_run(kgb, b, i, niter):
+    c = b.context(i)
+    c.set_option("sweep_tile_xy", b.get_option("sweep_tile_xy"))
+    c.set_option("sweep_tile_z", b.get_option("sweep_tile_z"))
+    if not b.get_option("moments_per_problem"):
+        c.set_option("moments_tensor", 0)
+    return np.array(c.solve(niter)), c.download("psi")
+
+
+def test_uneven_inputs_are_seeded(kgb):
+    a = uneven_inputs(4, seed=5)
+    b = uneven_inputs(4, seed=5)
+    assert [(x.nx, x.ny, x.nz, x.num_groups, x.num_directions, x.seed) for x in a] == \
+           [(x.nx, x.ny, x.nz, x.num_groups, x.num_directions, x.seed) for x in b]
+    assert all(8 <= x.nx <= 48 and x.num_groups in (8, 16, 32, 64) and x.num_directions in (48, 96, 192) for x in a)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,own", [("fp64", -1), ("fp64", 0), ("mixed", -1), ("mixed", 1)])
+@pytest.mark.parametrize("tiles", [(22, 8), (44, 2), (42, 4)])
+def test_batch_equals_single_contexts(kgb, prec, own, tiles):
+    precision = kgb.FP64 if prec == "fp64" else kgb.MIXED
+    b = make_batch(kgb, small_set(kgb, precision=precision), precision)
+    b.set_option("sweep_tile_xy", tiles[0])
+    b.set_option("sweep_tile_z", tiles[1])
+    b.set_option("moments_per_problem", own)
+    niter = 4
+    parts = b.solve(niter)
+    assert b.get_option("graph_active") == 1
+    psis = [b.context(i).download("psi") for i in range(len(b))]
+    for i in range(len(b)):
+        want, psi = single_run(kgb, b, i, niter)
+        np.testing.assert_array_equal(parts[:, i], want)
+        np.testing.assert_array_equal(psis[i], psi)
+
+
+@pytest.mark.gpu
+def test_batch_matches_oracle(kgb, oracle):
+    inputs = small_set(kgb, n=4, seed=3)
+    b = make_batch(kgb, inputs, kgb.FP64)
+    parts = b.solve(5)
+    for i, inp in enumerate(inputs):
+        p = oracle.Problem(zones=(inp.nx, inp.ny, inp.nz), groups=inp.num_groups,
+                           quad=(inp.quad_num_polar, inp.quad_num_azimuthal), legendre=inp.legendre_order, gset=1,
+                           dset=8, geometry=1, scatter=1, sigt=tuple(inp.sigt), sigs=tuple(inp.sigs), seed=inp.seed)
+        np.testing.assert_allclose(parts[:, i], p.solve(5), rtol=1e-12)
+
+
+@pytest.mark.gpu
+def test_batch_replay_is_deterministic(kgb):
+    b = make_batch(kgb, small_set(kgb, n=6, seed=8), kgb.MIXED)
+    a = b.solve(3)
+    c = b.solve(3)
+    np.testing.assert_array_equal(a, c)
+    assert b.get_option("graph_active") == 1
+    b.set_option("graph", 0)
+    d = b.solve(3)
+    assert b.get_option("graph_active") == 0
+    np.testing.assert_array_equal(a, d)
+    assert b.launch_count() == 3 * 3 * b.get_option("kernels_per_iteration")
+
+
+@pytest.mark.gpu
+def test_batch_autotune_then_parity(kgb):
+    b = make_batch(kgb, small_set(kgb, n=4, seed=21), kgb.FP64)
+    t = b.autotune()
+    assert t["iteration_ms"] > 0 and t["sweep_tile_xy"] in (22, 42, 44) and t["sweep_tile_z"] in (2, 4, 8, 16)
+    parts = b.solve(3)
+    for i in range(len(b)):
+        want, _ = single_run(kgb, b, i, 3)
+        np.testing.assert_array_equal(parts[:, i], want)
+
+
+@pytest.mark.gpu
+def test_batch_rejects_unsupported(kgb):
+    b = kgb.Batch(precision=kgb.FP64)
+    with pytest.raises(kgb.KgbError):
+        b.add(zones=(8, 8, 8), groups=4, quad=(4, 8), legendre=2, zsets=(2, 1, 1))
+    with pytest.raises(kgb.KgbError):
+        b.add(zones=(8, 8, 8), groups=4, quad=(4, 8), legendre=5)
+    with pytest.raises(kgb.KgbError):
+        b.solve(1)  # empty
