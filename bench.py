@@ -16,8 +16,10 @@ larger than L2, so no L2 flush is needed between steps.
 
 The FP64 line also carries, from the same run, the mixed form on the same
 workload ("mixed": throughput, speed-up over FP64, phi error against FP64
-after 20 iterations) and the adjoint report ("adjoint": gradient/forward time
-and central-difference check at 32^3 zones x 32 groups x 96 directions).
+after 20 iterations), the adjoint report ("adjoint": gradient/forward time
+and central-difference check at 32^3 zones x 32 groups x 96 directions) and
+the batching form ("batch": 48 uneven problems in one graph-replayed solve,
+mixed and FP64, against solving them one by one).
 
 --gpus N > 1 (under torchrun) runs N independent replicas, one per GPU
 (the path has no data exchange); value = all replicas' unknowns / max time.
@@ -46,6 +48,10 @@ MIXED_PHI_ITERS = 20  # the mixed form's phi error is taken against FP64 after t
 # adjoint gradient workload: cross sections of the reference problem, +-20% per group, isotropic P0
 ADJ_WORKLOAD = dict(zones=(32, 32, 32), groups=32, quad=96, legendre=4, gset=1, dset=8, geometry=1, scatter=0,
                     perturb=1, layout="DGZ")
+BATCH_PROBLEMS = 48
+BATCH_NAME = ("48 independent problems (seed 2026): zones per axis uniform in [8,48], groups from {8,16,32,64}, "
+              "directions from {48,96,192} (Gauss-Legendre product sets), Legendre order from {2,4}; cube100 "
+              "geometry, per-material sigma_t in [0.05,0.5]/cm, scattering ratio in [0.3,0.9], seeded downscatter")
 ADJ_NAME = ("32^3 zones x 32 groups x 96 directions, P4, cube100, isotropic P0 with +-20% per-group perturbation; "
             "absorption in the detector block [80,100]^3 cm")
 
@@ -301,6 +307,39 @@ def adjoint_report(local, fd_params=3):
     return res
 
 
+def batch_report(local, niter=10):
+    """The batching form: all problems in one graph-replayed solve against each problem run on its own."""
+    from kripke_gb300 import abi
+    from kripke_gb300.batching import uneven_inputs, unknowns as problem_unknowns
+    out = {"workload": BATCH_NAME, "iterations_per_solve": niter}
+    for name, prec in (("mixed", abi.MIXED), ("fp64", abi.FP64)):
+        inputs = uneven_inputs(BATCH_PROBLEMS, seed=2026, precision=prec)
+        U = sum(problem_unknowns(x) for x in inputs)
+        b = abi.Batch(device=local, precision=prec)
+        for x in inputs:
+            b.add(x)
+        tune = b.autotune()
+        b.solve(niter)  # captures the solve graph
+        l0 = b.launch_count()
+        t0 = time.perf_counter()
+        b.solve(niter)
+        t_batch = (time.perf_counter() - t0) / niter
+        kernels = (b.launch_count() - l0) // niter
+        phases = b.profile()
+        t0 = time.perf_counter()
+        for i in range(len(b)):
+            b.context(i).solve(niter)
+        t_seq = (time.perf_counter() - t0) / niter
+        out[name] = {"value": U / t_batch, "unit": "unknowns/s", "unknowns": U, "ms_per_iteration": t_batch * 1e3,
+                     "graph_active": b.get_option("graph_active"), "kernels_per_iteration": kernels,
+                     "autotuned": tune, "phase_ms": phases,
+                     "one_by_one": {"value": U / t_seq, "ms_per_iteration": t_seq * 1e3,
+                                    "how": "each problem's own context, default options, solved in turn"},
+                     "speedup_vs_one_by_one": t_seq / t_batch}
+        b.close()
+    return out
+
+
 def run_gpu(args, world, rank, local):
     import ctypes
     import numpy as np
@@ -432,6 +471,8 @@ def run_gpu(args, world, rank, local):
         line["mixed"] = mixed_report(args, local, w, ctx, ms)
     if rank == 0 and world == 1 and not args.no_adjoint:
         line["adjoint"] = adjoint_report(local)
+    if rank == 0 and world == 1 and not args.no_batch:
+        line["batch"] = batch_report(local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, dt = cpu_run(CPU_SAMPLE, threads, 1, 2)
@@ -457,6 +498,7 @@ def main():
     ap.add_argument("--zones", type=int, default=0, help="override zones per axis (profiling on a smaller case)")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-form comparison")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint gradient report")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-problems report")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

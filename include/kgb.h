@@ -294,6 +294,10 @@ int kgb_batch_autotune(kgb_batch *b, double *best_ms);
 /* niter source iterations from psi = 0 for every problem (SteadyStateSolver
  * each); part (may be NULL) receives the particle counts [niter][n]. */
 int kgb_batch_solve(kgb_batch *b, int32_t niter, double source_strength, double *part);
+/* Device time (ms) of each phase of one iteration run launch by launch:
+ * ms[0] LTimes, [1] scattering + source, [2] LPlusTimes, [3] persistent sweep,
+ * [4] population; advances the problems' state by two iterations. */
+int kgb_batch_profile(kgb_batch *b, double ms[5]);
 /* Kernels the batch has launched (graph replays included). */
 int kgb_batch_launch_count(kgb_batch *b, int64_t *out);
 

@@ -30,7 +30,7 @@ EXPORTS = (
     "kgb_response", "kgb_gradient", "kgb_gradient_unrolled",
     "kgb_batch_create", "kgb_batch_destroy", "kgb_batch_last_error", "kgb_batch_add", "kgb_batch_size",
     "kgb_batch_context", "kgb_batch_set_option", "kgb_batch_get_option", "kgb_batch_autotune", "kgb_batch_solve",
-    "kgb_batch_launch_count",
+    "kgb_batch_launch_count", "kgb_batch_profile",
 )
 
 INT_FIELDS = ("quadrature/id", "quadrature/jd", "quadrature/kd", "zone_to_mixelem", "zone_to_num_mixelem",
@@ -172,6 +172,7 @@ def load():
         "kgb_batch_autotune": ([P, ctypes.POINTER(D)], I),
         "kgb_batch_solve": ([P, ctypes.c_int32, D, P], I),
         "kgb_batch_launch_count": ([P, ctypes.POINTER(I64)], I),
+        "kgb_batch_profile": ([P, ctypes.POINTER(D)], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -495,3 +496,9 @@ class Batch:
         n = ctypes.c_int64()
         self._check(self.lib.kgb_batch_launch_count(self.h, ctypes.byref(n)), "kgb_batch_launch_count")
         return n.value
+
+    def profile(self):
+        """Device ms per phase of one iteration: ltimes, scattering, lplustimes, sweep, population."""
+        ms = (ctypes.c_double * 5)()
+        self._check(self.lib.kgb_batch_profile(self.h, ms), "kgb_batch_profile")
+        return dict(zip(("ltimes", "scattering", "lplustimes", "sweep", "population"), list(ms)))

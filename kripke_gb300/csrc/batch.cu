@@ -349,13 +349,16 @@ int forkMoments(kgb_batch *b, bool plus) {
   return KGB_OK;
 }
 
+// ev (optional, 6 events): recorded at the phase boundaries LTimes | scattering
+// | LPlusTimes | sweep | population.
 template <typename T>
-int enqueueIteration(kgb_batch *b, double *pop_out) {
+int enqueueIteration(kgb_batch *b, double *pop_out, cudaEvent_t *ev = nullptr) {
   const auto *lt = (const BatchMom<T> *)b->lt_desc;
   const auto *lp = (const BatchMom<T> *)b->lp_desc;
   const auto *sc = (const BatchScat<T> *)b->sc_desc;
   const bool own = perProblemMoments(b);
   int rc;
+  if (ev) BCK(cudaEventRecord(ev[0], b->stream));
   if (own) {
     if ((rc = forkMoments(b, false))) return rc;
   } else {
@@ -363,8 +366,10 @@ int enqueueIteration(kgb_batch *b, double *pop_out) {
       launch_batch_moments<T>(lt, b->rows_lt + c.off, c.n, c.key, b->Dmax, false, c.vec,
                               std::min(c.n, b->row_grid), b->stream);
   }
+  if (ev) BCK(cudaEventRecord(ev[1], b->stream));
   for (auto &c : b->sc_cls)
     launch_batch_scattering<T>(sc, b->rows_sc + c.off, c.n, c.key, std::min(c.n, b->row_grid), b->stream);
+  if (ev) BCK(cudaEventRecord(ev[2], b->stream));
   if (own) {
     if ((rc = forkMoments(b, true))) return rc;
   } else {
@@ -374,9 +379,12 @@ int enqueueIteration(kgb_batch *b, double *pop_out) {
   }
   BCK(cudaGetLastError());
   BCK(cudaMemsetAsync(b->bar, 0, 2 * sizeof(unsigned int), b->stream));
+  if (ev) BCK(cudaEventRecord(ev[3], b->stream));
   BatchSweepPlan p{b->sweep_items, b->step_off, b->nsteps, b->zero, b->nzero, b->bar, b->err_d};
   BCK(launch_batch_sweep<T>((const SweepArgs<T> *)b->sweep_args, p, b->tx, b->ty, b->sweep_grid, b->stream));
+  if (ev) BCK(cudaEventRecord(ev[4], b->stream));
   launch_batch_pop_finish(b->slot_ptrs, b->slot_n, (int)b->inst.size(), pop_out, b->stream);
+  if (ev) BCK(cudaEventRecord(ev[5], b->stream));
   BCK(cudaGetLastError());
   return KGB_OK;
 }
@@ -669,6 +677,26 @@ int kgb_batch_autotune(kgb_batch *b, double *best_ms) {
   if ((rc = plan(b))) return rc;
   if (best_ms) *best_ms = best;
   return KGB_OK;
+}
+
+int kgb_batch_profile(kgb_batch *b, double ms[5]) {
+  if (!b || !ms) return KGB_ERR_ARG;
+  BCK(cudaSetDevice(b->device));
+  int rc = ensurePlan(b);
+  if (rc || (rc = ensurePop(b, 1))) return rc;
+  cudaEvent_t ev[6];
+  for (auto &e : ev) BCK(cudaEventCreate(&e));
+  for (int rep = 0; rep < 2 && !rc; ++rep)  // the second iteration is measured
+    rc = b->prec == KGB_FP64 ? enqueueIteration<double>(b, b->pop, ev) : enqueueIteration<float>(b, b->pop, ev);
+  if (!rc && cudaEventSynchronize(ev[5]) == cudaSuccess)
+    for (int k = 0; k < 5; ++k) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+      ms[k] = t;
+    }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (!rc) rc = checkBarrier(b);
+  return rc;
 }
 
 int kgb_batch_launch_count(kgb_batch *b, int64_t *out) {
