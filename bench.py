@@ -177,12 +177,26 @@ def dist_init():
     return world, rank, local
 
 
+def max_over_ranks(value, world):
+    """The largest value over all ranks (the timed region ends when the slowest replica does)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sample_name = "32^3-zone sample of the workload (same groups, directions, order, physics), 1 iteration per step"
-    value, dt = cpu_run(CPU_SAMPLE, threads, args.warmup, args.steps)
+    sample = dict(CPU_SAMPLE, zones=(args.zones,) * 3) if args.zones else CPU_SAMPLE
+    sample_name = ("%d^3-zone sample of the workload (same groups, directions, order, physics), 1 iteration per step"
+                   % sample["zones"][0])
+    value, dt = cpu_run(sample, threads, args.warmup, args.steps)
     line = {
         "impl": "reference", "metric": "unknowns/s per source iteration", "value": value,
         "unit": "unknowns/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -229,11 +243,18 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     fp64_ctx.solve(MIXED_PHI_ITERS)
     a, b = fp64_ctx.download("phi"), ctx.download("phi")
     err = float(np.abs(b - a).max() / np.abs(a).max())
-    del a, b
+    err_l2 = float(np.linalg.norm(b - a) / np.linalg.norm(a))
+    # moment 0 (DGZ host nesting: phi chunks are [M][G][Z], one chunk per group set)
+    M = (w["legendre"] + 1) ** 2
+    a0, b0 = a.reshape(M, -1)[0], b.reshape(M, -1)[0]
+    err0 = float(np.abs(b0 - a0).max() / np.abs(a0).max())
+    del a, b, a0, b0
     out = {"value": unknowns(w) / (ms * 1e-3), "unit": "unknowns/s", "ms_per_step": ms,
-           "speedup_vs_fp64": fp64_ms / ms, "phi_rel_err_vs_fp64": err,
-           "phi_err_definition": "max|phi_mixed - phi_fp64| / max|phi_fp64| over all moments, groups and zones "
-                                 "after %d iterations from psi = 0" % MIXED_PHI_ITERS,
+           "speedup_vs_fp64": fp64_ms / ms, "phi_rel_err_vs_fp64": err, "phi_rel_err_l2": err_l2,
+           "phi0_rel_err_max": err0,
+           "phi_err_definition": "after %d iterations from psi = 0: max|phi_mixed - phi_fp64| / max|phi_fp64| over "
+                                 "all moments, groups and zones; also the 2-norm ratio and the max-abs relative "
+                                 "error of moment 0" % MIXED_PHI_ITERS,
            "autotuned": tuned,
            "kernels": {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "moments_tensor_ltimes",
                                                       "moments_tensor_lplustimes")}}
@@ -307,13 +328,14 @@ def adjoint_report(local, fd_params=3):
     return res
 
 
-def batch_report(local, niter=10):
+def batch_report(local, problems=BATCH_PROBLEMS, niter=10):
     """The batching form: all problems in one graph-replayed solve against each problem run on its own."""
     from kripke_gb300 import abi
     from kripke_gb300.batching import uneven_inputs, unknowns as problem_unknowns
-    out = {"workload": BATCH_NAME, "iterations_per_solve": niter}
+    name = BATCH_NAME if problems == BATCH_PROBLEMS else BATCH_NAME.replace("48 independent", "%d independent" % problems)
+    out = {"workload": name, "iterations_per_solve": niter}
     for name, prec in (("mixed", abi.MIXED), ("fp64", abi.FP64)):
-        inputs = uneven_inputs(BATCH_PROBLEMS, seed=2026, precision=prec)
+        inputs = uneven_inputs(problems, seed=2026, precision=prec)
         U = sum(problem_unknowns(x) for x in inputs)
         b = abi.Batch(device=local, precision=prec)
         for x in inputs:
@@ -390,10 +412,7 @@ def run_gpu(args, world, rank, local):
     fam = {f: ctx.kernel_time(f) for f in ("sweep", "ltimes", "lplustimes", "scattering", "source", "population")}
     ctx.set_timing(False)
     part = ctx.population()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world)
 
     # end to end through the public API with host buffers: upload every generated input from
     # pinned host memory, run a 10-iteration solve (psi reset, populations read back each solve)
@@ -472,7 +491,7 @@ def run_gpu(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_adjoint:
         line["adjoint"] = adjoint_report(local)
     if rank == 0 and world == 1 and not args.no_batch:
-        line["batch"] = batch_report(local)
+        line["batch"] = batch_report(local, args.batch_problems)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, dt = cpu_run(CPU_SAMPLE, threads, 1, 2)
@@ -499,6 +518,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-form comparison")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint gradient report")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-problems report")
+    ap.add_argument("--batch-problems", type=int, default=BATCH_PROBLEMS,
+                    help="problems in the batched report (profiling on a smaller batch)")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

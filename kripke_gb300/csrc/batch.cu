@@ -152,7 +152,7 @@ bool sameViews(const InstanceView &a, const InstanceView &c) {
          a.plane[0] == c.plane[0] && a.plane[1] == c.plane[1] && a.plane[2] == c.plane[2] && a.ell == c.ell &&
          a.ellp == c.ellp && a.sigsT == c.sigsT && a.mix_frac == c.mix_frac && a.mix_mat == c.mix_mat &&
          a.zmix_start == c.zmix_start && a.gp_lo == c.gp_lo && a.sdoms == c.sdoms && a.cx == c.cx &&
-         a.cls == c.cls && a.inv == c.inv;
+         a.cls == c.cls && a.inv == c.inv && a.gen == c.gen;
 }
 
 // Row items of every problem, grouped by a class key (stable: problem order within a class).

@@ -178,6 +178,21 @@ struct kgb_ctx {
   bool adj_stale = true;        // adjoint tables must be rebuilt from the host inputs
   bool have_lam = false;        // an adjoint solve has filled lam
   int flip = 0;                 // 1 while the adjoint operators are installed
+
+  // captured solves (kgb_solve): valid while gen, bumped whenever a table,
+  // tile list or kernel choice a capture baked in may have changed, is unchanged
+  uint64_t gen = 0;
+  struct SolveGraph {
+    int niter;
+    double q;
+    uint64_t gen;
+    cudaStream_t stream;
+    cudaGraph_t g;
+    cudaGraphExec_t x;
+    int64_t launches;
+  };
+  std::vector<SolveGraph> solve_graphs;
+  bool use_graph = true, graph_active = false;
 };
 
 namespace {
@@ -356,7 +371,17 @@ int dalloc(kgb_ctx *ctx, void **p, size_t bytes) {
   return KGB_OK;
 }
 
+void dropSolveGraphs(kgb_ctx *c) {
+  for (auto &e : c->solve_graphs) {
+    cudaGraphExecDestroy(e.x);
+    cudaGraphDestroy(e.g);
+  }
+  c->solve_graphs.clear();
+}
+
 void freeAll(kgb_ctx *c) {
+  dropSolveGraphs(c);
+  ++c->gen;
   void *ptrs[] = {c->psi, c->rhs, c->phi, c->phi_out, c->sigt, c->plane[0], c->plane[1], c->plane[2], c->ell, c->ellp,
                   c->sigsT, c->cx, c->cy, c->cz, c->w_d, c->cos_d[0], c->cos_d[1], c->cos_d[2], c->vol_d,
                   c->dxyz_d[0], c->dxyz_d[1], c->dxyz_d[2], c->zmix_start, c->zmix_count, c->mix_mat, c->mix_zone,
@@ -601,6 +626,7 @@ int prepareT(kgb_ctx *ctx) {
     CK(cudaMemcpyAsync(ctx->levels_d, ctx->level_sdoms.data(), ctx->level_sdoms.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_quad = false;
+    ++ctx->gen;
     ctx->dirty_geom = true;
     ctx->adj_stale = true;
   }
@@ -618,6 +644,7 @@ int prepareT(kgb_ctx *ctx) {
     }
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_geom = false;
+    ++ctx->gen;
     ctx->dirty_sigt = true;  // the tabulated reciprocals depend on 2*cos/delta
   }
   if (ctx->dirty_ell) {
@@ -626,6 +653,7 @@ int prepareT(kgb_ctx *ctx) {
     if ((rc = uploadVec<T>(ctx, ctx->ellp, ctx->ellp_h))) return rc;
     if ((rc = planTensorMoments<T>(ctx))) return rc;
     ctx->dirty_ell = false;
+    ++ctx->gen;
     ctx->adj_stale = true;
   }
   if (ctx->dirty_sigs) {
@@ -649,6 +677,7 @@ int prepareT(kgb_ctx *ctx) {
     CK(cudaMemcpyAsync(ctx->gp_hi, hi.data(), G * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_sigs = false;
+    ++ctx->gen;
     ctx->adj_stale = true;
   }
   if (ctx->dirty_vol) {
@@ -659,6 +688,7 @@ int prepareT(kgb_ctx *ctx) {
     for (double v : ctx->vol_h)
       if (v != ctx->vol_uniform || !(v > 0.0)) { ctx->vol_uniform = 0.0; break; }
     ctx->dirty_vol = false;
+    ++ctx->gen;
   }
   if (ctx->dirty_mix) {
     if ((rc = need(ctx, {"zone_to_mixelem", "zone_to_num_mixelem", "mixelem_to_zone", "mixelem_to_material",
@@ -713,11 +743,13 @@ int prepareT(kgb_ctx *ctx) {
     CK(cudaMemcpyAsync(ctx->mix_frac, mfr.data(), total * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_mix = false;
+    ++ctx->gen;
   }
   if (ctx->dirty_sigt) {
     if ((rc = need(ctx, {"sigt_zonal"}))) return rc;
     if ((rc = buildReciprocals(ctx))) return rc;
     ctx->dirty_sigt = false;
+    ++ctx->gen;
   }
   return KGB_OK;
 }
@@ -730,6 +762,7 @@ int prepare(kgb_ctx *ctx) {
 }
 
 int buildTiles(kgb_ctx *ctx) {
+  ++ctx->gen;
   const int ntx = (ctx->nxs + ctx->tx - 1) / ctx->tx;
   const int nty = (ctx->nys + ctx->ty - 1) / ctx->ty;
   const int ntz = (ctx->nzs + ctx->tz - 1) / ctx->tz;
@@ -1268,6 +1301,59 @@ struct PsiBuffers {
 
 }  // namespace
 
+namespace {
+// The whole solve (psi reset + niter iterations with their particle counts)
+// captured once per (niter, q, stream) and replayed while the context's
+// tables are unchanged.  A capture that fails leaves *out null: the caller
+// runs the solve launch by launch.
+int solveGraph(kgb_ctx *ctx, int niter, double q, const kgb_ctx::SolveGraph **out) {
+  *out = nullptr;
+  auto &v = ctx->solve_graphs;
+  for (auto it = v.begin(); it != v.end();) {
+    if (it->gen != ctx->gen) {
+      cudaGraphExecDestroy(it->x);
+      cudaGraphDestroy(it->g);
+      it = v.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  for (auto &e : v)
+    if (e.niter == niter && e.q == q && e.stream == ctx->stream) {
+      *out = &e;
+      return KGB_OK;
+    }
+  if (v.size() >= 4) {
+    cudaGraphExecDestroy(v.front().x);
+    cudaGraphDestroy(v.front().g);
+    v.erase(v.begin());
+  }
+  if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return KGB_OK;
+  }
+  const int64_t l0 = ctx->launches;
+  const std::string err0 = ctx->err;
+  int rc = cudaMemsetAsync(ctx->psi, 0, ctx->Z * ctx->G * ctx->D * ctx->tsz, ctx->stream) == cudaSuccess
+               ? KGB_OK : KGB_ERR_CUDA;
+  for (int it = 0; it < niter && !rc; ++it) rc = iterateDevice(ctx, q, ctx->parts_dev + it);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  const int64_t captured = ctx->launches - l0;
+  ctx->launches = l0;  // counted when replayed
+  cudaGraphExec_t x = nullptr;
+  if (rc || e != cudaSuccess || !g || cudaGraphInstantiate(&x, g, 0) != cudaSuccess) {
+    cudaGetLastError();
+    if (g) cudaGraphDestroy(g);
+    ctx->err = err0;
+    return KGB_OK;
+  }
+  v.push_back({niter, q, ctx->gen, ctx->stream, g, x, captured});
+  *out = &v.back();
+  return KGB_OK;
+}
+}  // namespace
+
 namespace kgb {
 int instance_view(kgb_ctx *ctx, InstanceView *v) {
   int rc = prepare(ctx);
@@ -1292,6 +1378,7 @@ int instance_view(kgb_ctx *ctx, InstanceView *v) {
   x.vol_uniform = ctx->vol_uniform;
   x.cls = ctx->use_recip ? ctx->cls_d : nullptr;
   x.inv = ctx->use_recip ? ctx->inv_d : nullptr;
+  x.gen = ctx->gen;
   *v = x;
   return KGB_OK;
 }
@@ -1830,12 +1917,25 @@ int kgb_solve(kgb_ctx *ctx, int32_t niter, double q, double *part) {
     if (ctx->parts_dev) cudaFree(ctx->parts_dev);
     ctx->parts_dev = nullptr;
     ctx->parts_cap = 0;
+    ++ctx->gen;
     if ((rc = dmalloc(ctx, &ctx->parts_dev, niter))) return rc;
     ctx->parts_cap = niter;
   }
-  CK(cudaMemsetAsync(ctx->psi, 0, ctx->Z * ctx->G * ctx->D * ctx->tsz, ctx->stream));  // kConst(psi, 0)
-  for (int it = 0; it < niter; ++it)
-    if ((rc = iterateDevice(ctx, q, ctx->parts_dev + it))) return rc;
+  ctx->graph_active = false;
+  if (ctx->use_graph && !ctx->timing) {
+    const kgb_ctx::SolveGraph *sg = nullptr;
+    if ((rc = solveGraph(ctx, niter, q, &sg))) return rc;
+    if (sg) {
+      CK(cudaGraphLaunch(sg->x, ctx->stream));
+      ctx->launches += sg->launches;
+      ctx->graph_active = true;
+    }
+  }
+  if (!ctx->graph_active) {
+    CK(cudaMemsetAsync(ctx->psi, 0, ctx->Z * ctx->G * ctx->D * ctx->tsz, ctx->stream));  // kConst(psi, 0)
+    for (int it = 0; it < niter; ++it)
+      if ((rc = iterateDevice(ctx, q, ctx->parts_dev + it))) return rc;
+  }
   if (part) CK(cudaMemcpyAsync(part, ctx->parts_dev, niter * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return checkDeviceError(ctx);
@@ -1857,6 +1957,11 @@ int kgb_set_stream(kgb_ctx *ctx, void *s) {
 
 int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
   if (!ctx || !key) return KGB_ERR_ARG;
+  ++ctx->gen;
+  if (!std::strcmp(key, "graph")) {
+    ctx->use_graph = value != 0;
+    return KGB_OK;
+  }
   if (!std::strcmp(key, "sweep_tile_z")) {
     if (value < 1 || value > 1024) return fail(ctx, KGB_ERR_ARG, "sweep_tile_z must be in [1, 1024]");
     ctx->tz = (int)value;
@@ -1948,6 +2053,7 @@ int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_
     if ((rc = timeIt(lt, true, t_tc)) || (rc = timeIt(lt, false, t_simt))) break;
     (lt ? ctx->use_tc_lt : ctx->use_tc_lp) = t_tc <= t_simt;
   }
+  ++ctx->gen;  // kernel choices may have changed
   cudaEventDestroy(f0);
   cudaEventDestroy(f1);
   if (rc) return rc;
@@ -1966,6 +2072,8 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "moments_tensor")) *value = ctx->allow_tc ? 1 : 0;
   else if (!std::strcmp(key, "moments_tensor_ltimes")) *value = (ctx->tc_lt && ctx->use_tc_lt) ? 1 : 0;
   else if (!std::strcmp(key, "moments_tensor_lplustimes")) *value = (ctx->tc_lp && ctx->use_tc_lp) ? 1 : 0;
+  else if (!std::strcmp(key, "graph")) *value = ctx->use_graph ? 1 : 0;
+  else if (!std::strcmp(key, "graph_active")) *value = ctx->graph_active ? 1 : 0;
   else return fail(ctx, KGB_ERR_ARG, std::string("unknown option '") + key + "'");
   return KGB_OK;
 }

@@ -207,6 +207,7 @@ struct InstanceView {
   double vol_uniform;
   const uint16_t *cls;  // tabulated sweep reciprocals, or null (divide per cell)
   const double *inv;
+  uint64_t gen;         // the context's table generation: changes whenever a table, tile list or kernel choice changes
 };
 int instance_view(kgb_ctx *ctx, InstanceView *v);
 // The context's own LTimes (plus = false) or LPlusTimes, overwriting phi / rhs,

@@ -1,0 +1,51 @@
+"""Captured solves: kgb_solve records the whole solve (psi reset and every
+iteration with its particle count) into a CUDA graph once and replays it
+while the context's tables are unchanged.  The replay must equal the
+launch-by-launch solve bit for bit, and any change of inputs or options must
+be picked up.
+"""
+import numpy as np
+import pytest
+
+KW = dict(zones=(10, 9, 8), groups=8, quad=(4, 8), legendre=2, geometry=1, scatter=1, gset=2, dset=8)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_replay_equals_eager(kgb, precision):
+    c = kgb.Context()
+    c.generate(precision=precision, **KW)
+    a = c.solve(6)
+    assert c.get_option("graph_active") == 1
+    psi_a = c.download("psi")
+    b = c.solve(6)  # replay
+    assert c.get_option("graph_active") == 1
+    c.set_option("graph", 0)
+    e = c.solve(6)
+    assert c.get_option("graph_active") == 0
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, e)
+    np.testing.assert_array_equal(psi_a, c.download("psi"))
+
+
+@pytest.mark.gpu
+def test_graph_follows_changes(kgb, oracle):
+    c = kgb.Context()
+    inp = c.generate(**KW)
+    c.solve(4)
+    # new tile shape: the captured solve must not be reused
+    c.set_option("sweep_tile_xy", 22)
+    c.set_option("sweep_tile_z", 2)
+    got = c.solve(4)
+    assert c.get_option("graph_active") == 1
+    p = oracle.Problem(zones=KW["zones"], groups=8, quad=(4, 8), legendre=2, geometry=1, scatter=1, gset=2)
+    np.testing.assert_allclose(got, p.solve(4), rtol=1e-12)
+    # new cross sections (and with them the tabulated sweep reciprocals)
+    st, sg = kgb.material_tables(inp)
+    c.set_materials(st * 1.5, sg)
+    p.set("sigt_zonal", p.get("sigt_zonal") * 1.5)
+    np.testing.assert_allclose(c.solve(4), p.solve(4), rtol=1e-12)
+    # another source strength is another graph
+    a = np.array(c.solve(3, 2.0))
+    b = np.array(c.solve(3, 1.0))
+    np.testing.assert_allclose(a, 2.0 * b, rtol=1e-13)
