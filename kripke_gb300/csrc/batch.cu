@@ -225,7 +225,7 @@ int planT(kgb_batch *b) {
     a.cz = (const T *)v.cz;
     a.sdoms = v.sdoms;
     a.cls = v.cls;
-    a.inv = v.inv;
+    a.inv = (const T *)v.inv;
     a.tiles = tiles_d;
     a.nx = v.nx; a.ny = v.ny; a.nz = v.nz; a.G = v.G; a.D = v.D; a.Gs = v.Gs; a.Ds = v.Ds;
     a.nxs = v.nx; a.nys = v.ny; a.nzs = v.nz;

@@ -143,7 +143,7 @@ struct kgb_ctx {
   bool use_recip = false;
   bool allow_recip = true;
   uint16_t *cls_d = nullptr;
-  double *inv_d = nullptr;
+  void *inv_d = nullptr;  // double (FP64) or float (mixed)
   int64_t ncls = 0;
   // tensor-core moment transforms (tc_moments.cu)
   bool allow_tc = true;
@@ -472,23 +472,24 @@ int need(kgb_ctx *ctx, std::initializer_list<const char *> names) {
   return KGB_OK;
 }
 
-// Tabulated sweep reciprocals (FP64 only).  On a uniform mesh the per-cell
-// denominator ((2mu/dx + 2eta/dy) + 2xi/dz) + sigt depends on the direction and
-// on the zone's sigt value alone; the distinct sigt values are few (mixtures of
-// three materials), so 1/den is tabulated per (class, direction) and each
-// (zone, group) stores its class.  Falls back to a per-cell divide when the mesh
-// is not uniform or the classes do not fit 16 bits.
-int buildReciprocals(kgb_ctx *ctx) {
-  ctx->use_recip = false;
-  if (ctx->prec != KGB_FP64 || !ctx->allow_recip) return KGB_OK;
+// Tabulated sweep reciprocals.  On a uniform mesh the per-cell denominator
+// ((2mu/dx + 2eta/dy) + 2xi/dz) + sigt depends on the direction and on the
+// zone's sigt value alone; the distinct sigt values are few (mixtures of three
+// materials), so 1/den is tabulated per (class, direction) and each (zone,
+// group) stores its class.  The denominator is formed exactly as the sweep
+// forms it, in the sweep's precision (FP64, or FP32 in the mixed form), and
+// rounded once to its reciprocal.  Falls back to a per-cell divide when the
+// mesh is not uniform or the classes do not fit 16 bits.
+template <typename T>
+int buildReciprocalsT(kgb_ctx *ctx) {
   for (int k = 0; k < 3; ++k)
     for (double v : ctx->dxyz[k])
       if (v != ctx->dxyz[k][0]) return KGB_OK;
   const int64_t n = ctx->Z * ctx->G;
-  std::vector<double> sig(n);
-  CK(cudaMemcpyAsync(sig.data(), ctx->sigt, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  std::vector<T> sig(n);
+  CK(cudaMemcpyAsync(sig.data(), ctx->sigt, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  std::vector<double> uniq(sig);
+  std::vector<T> uniq(sig);
   std::sort(uniq.begin(), uniq.end());
   uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
   const int64_t ncls = (int64_t)uniq.size();
@@ -496,31 +497,41 @@ int buildReciprocals(kgb_ctx *ctx) {
   std::vector<uint16_t> cls(n);
   for (int64_t e = 0; e < n; ++e)
     cls[e] = (uint16_t)(std::lower_bound(uniq.begin(), uniq.end(), sig[e]) - uniq.begin());
-  std::vector<double> inv((size_t)ncls * ctx->D);
+  std::vector<T> inv((size_t)ncls * ctx->D);
   for (int64_t c = 0; c < ncls; ++c)
     for (int d = 0; d < ctx->D; ++d) {
-      const double cx = 2.0 * ctx->q[0][d] / ctx->dxyz[0][0];
-      const double cy = 2.0 * ctx->q[1][d] / ctx->dxyz[1][0];
-      const double cz = 2.0 * ctx->q[2][d] / ctx->dxyz[2][0];
-      inv[(size_t)c * ctx->D + d] = 1.0 / (cx + cy + cz + uniq[c]);
+      // the coefficient tables hold 2*cos/delta rounded to T
+      const T cx = (T)(2.0 * ctx->q[0][d] / ctx->dxyz[0][0]);
+      const T cy = (T)(2.0 * ctx->q[1][d] / ctx->dxyz[1][0]);
+      const T cz = (T)(2.0 * ctx->q[2][d] / ctx->dxyz[2][0]);
+      const T den = ((cx + cy) + cz) + uniq[c];
+      inv[(size_t)c * ctx->D + d] = T(1) / den;
     }
   if (ctx->cls_d) cudaFree(ctx->cls_d);
   if (ctx->inv_d) cudaFree(ctx->inv_d);
   ctx->cls_d = nullptr;
   ctx->inv_d = nullptr;
   int rc;
-  if ((rc = dmalloc(ctx, &ctx->cls_d, n)) || (rc = dmalloc(ctx, &ctx->inv_d, inv.size()))) return rc;
+  T *inv_d = nullptr;
+  if ((rc = dmalloc(ctx, &ctx->cls_d, n)) || (rc = dmalloc(ctx, &inv_d, inv.size()))) return rc;
+  ctx->inv_d = inv_d;
   CK(cudaMemcpyAsync(ctx->cls_d, cls.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->inv_d, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(inv_d, inv.data(), inv.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->ncls = ncls;
   ctx->use_recip = true;
   return KGB_OK;
 }
 
+int buildReciprocals(kgb_ctx *ctx) {
+  ctx->use_recip = false;
+  if (!ctx->allow_recip) return KGB_OK;
+  return ctx->prec == KGB_FP64 ? buildReciprocalsT<double>(ctx) : buildReciprocalsT<float>(ctx);
+}
+
 // Plan the tensor-core LTimes / LPlusTimes: digit images of L and L+ and the
-// shapes the kernel supports (exact diagonal sums need K <= 128 directions in
-// FP64 and <= 256 in the mixed form; moments fit one 32-wide K chunk).
+// shapes the kernel supports (exact diagonal sums need K <= 128 directions per
+// launch in FP64 and <= 256 in the mixed form; moments fit one 32-wide K chunk).
 // lt_src / lp_src: the [D][M] host tables the LTimes / LPlusTimes operators
 // read (ell and ell_plus for the forward iteration, exchanged for the adjoint).
 template <typename T>
@@ -548,12 +559,23 @@ int planTensorMomentsFrom(kgb_ctx *ctx, const std::vector<double> &lt_src, const
   std::vector<uint16_t> img;
   std::vector<int> ex;
   int rc;
-  // LTimes: B[d][m] = ell(m,d), K = D, N = M (one 32-wide block)
-  if (M <= 32 && D <= (f64 ? 128 : 256)) {
-    const int kpad = (D + 31) / 32 * 32;
-    tc_build_b<T>(lt_src.data(), D, M, kpad, S, 32, 1, img, ex);
-    if ((rc = upload(lt_img, lt_exp, img, ex))) return rc;
-    *lt_kpad = kpad;
+  // LTimes: B[d][m] = ell(m,d), K = D, N = M (one 32-wide block).  Exact diagonal
+  // sums hold for at most 128 (FP64) / 256 (mixed) directions, so larger D runs in
+  // K chunks of equal width kc (a multiple of 32), each with its own digit image,
+  // the chunk results added in the output precision.  *lt_kpad = kc.
+  if (M <= 32) {
+    const int kmax = f64 ? 128 : 256;
+    const int nk = (D + kmax - 1) / kmax;
+    const int kc = ((D + nk - 1) / nk + 31) / 32 * 32;
+    std::vector<uint16_t> all;
+    std::vector<int> allex;
+    for (int k0 = 0; k0 < D; k0 += kc) {
+      tc_build_b<T>(lt_src.data() + (size_t)k0 * M, std::min(kc, D - k0), M, kc, S, 32, 1, img, ex);
+      all.insert(all.end(), img.begin(), img.end());
+      allex.insert(allex.end(), ex.begin(), ex.end());
+    }
+    if ((rc = upload(lt_img, lt_exp, all, allex))) return rc;
+    *lt_kpad = kc;
     *lt_ok = true;
   }
   // LPlusTimes: B[m][d] = ell_plus(d,m), K = M (one chunk), N = D in blocks of NB
@@ -819,7 +841,7 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop) {
   a.flip = ctx->flip;
   if (ctx->use_recip) {
     a.cls = ctx->cls_d;
-    a.inv = ctx->inv_d;
+    a.inv = as<T>(ctx->inv_d);
   }
   if (fused_pop) {
     a.pop = ctx->pop_slots;
@@ -936,13 +958,20 @@ int doLTimes(kgb_ctx *ctx, bool acc) {
   FamScope fs(ctx, "ltimes");
   const int64_t rows = ctx->Z * ctx->G;
   if (ctx->tc_lt && ctx->use_tc_lt) {
-    if (ctx->prec == KGB_FP64)
-      tcRows<double>(ctx, as<double>(ctx->psi), as<double>(ctx->phi), ctx->D, ctx->M, ctx->D, ctx->tc_lt_kpad, ctx->M, 1,
-                     ctx->tc_lt_img, ctx->tc_lt_exp, acc, false);
-    else
-      tcRows<float>(ctx, as<float>(ctx->psi), as<float>(ctx->phi), ctx->D, ctx->M, ctx->D, ctx->tc_lt_kpad, ctx->M, 1,
-                    ctx->tc_lt_img, ctx->tc_lt_exp, acc, false);
-    CKN(1);
+    // one launch per K chunk of kc directions (one chunk up to 128 FP64 / 256 FP32 directions)
+    const int kc = ctx->tc_lt_kpad, S = ctx->prec == KGB_FP64 ? 8 : 4;
+    for (int k0 = 0, c = 0; k0 < ctx->D; k0 += kc, ++c) {
+      const int K = std::min(kc, ctx->D - k0);
+      const uint16_t *img = ctx->tc_lt_img + (size_t)c * kc * S * 32;
+      const int *ex = ctx->tc_lt_exp + (size_t)c * 32;
+      if (ctx->prec == KGB_FP64)
+        tcRows<double>(ctx, as<double>(ctx->psi) + k0, as<double>(ctx->phi), ctx->D, ctx->M, K, kc, ctx->M, 1, img,
+                       ex, acc || c > 0, false);
+      else
+        tcRows<float>(ctx, as<float>(ctx->psi) + k0, as<float>(ctx->phi), ctx->D, ctx->M, K, kc, ctx->M, 1, img, ex,
+                      acc || c > 0, false);
+      CKN(1);
+    }
     return KGB_OK;
   }
   if (ctx->prec == KGB_FP64)

@@ -48,7 +48,7 @@ struct SweepArgs {
   int flip;                   // 1: sweep every direction in the reversed orientation (adjoint)
   // tabulated reciprocals (uniform mesh): 1/((cx+cy+cz)[d] + sigt) per (sigt class, direction)
   const uint16_t *cls;        // [Z][G] class of sigt_zonal, or null: divide per cell
-  const double *inv;          // [nclass][D]
+  const T *inv;               // [nclass][D]
   // fused population: per-block partial sums of w(d)*psi*volume(z), or null
   double *pop;                // slot = ((tile index)*nsdom + sdom)*gridDim.x + blockIdx.x
   int nsdom;
@@ -206,7 +206,7 @@ struct InstanceView {
   const SdomDesc *sdoms;
   double vol_uniform;
   const uint16_t *cls;  // tabulated sweep reciprocals, or null (divide per cell)
-  const double *inv;
+  const void *inv;      // [nclass][D] in the context's precision
   uint64_t gen;         // the context's table generation: changes whenever a table, tile list or kernel choice changes
 };
 int instance_view(kgb_ctx *ctx, InstanceView *v);

@@ -19,10 +19,12 @@
 // fastest, so every global access of a warp is a contiguous run.
 //
 // FP64 on GB300 issues at 1/61 of the FP32 rate and one IEEE divide costs
-// about ten FP64 slots, so on a uniform mesh the denominator's reciprocal is
+// about ten FP64 slots (in FP32 the divide's latency sits on the cell-to-cell
+// dependency chain), so on a uniform mesh the denominator's reciprocal is
 // tabulated per (sigt class, direction): den = ((cx+cy)+cz) + sigt is formed
-// exactly as per cell (same operands, same association) and rounded once to
-// 1/den; the cell then multiplies (psi differs from num/den by at most 1.5 ulp).
+// exactly as per cell (same operands, same association, same precision) and
+// rounded once to 1/den; the cell then multiplies (psi differs from num/den by
+// at most 1.5 ulp).
 //
 // The transposed (adjoint) sweep is the same recurrence run from the opposite
 // corner (flip): along a direction the diamond-difference coupling of two
@@ -160,7 +162,7 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
           const int64_t z = zrow + iloc[ii];
           if (iv[ii] && jv[jj]) {
             rv[jj][ii] = rhs[(z * a.G + g) * a.D + d];
-            if (RECIP) sv[jj][ii] = (T)a.inv[(int64_t)a.cls[z * a.G + g] * a.D + d];
+            if (RECIP) sv[jj][ii] = a.inv[(int64_t)a.cls[z * a.G + g] * a.D + d];
             else sv[jj][ii] = a.sigt[z * a.G + g];
           } else {
             rv[jj][ii] = T(0);

@@ -76,10 +76,12 @@ def test_ltimes_lplustimes(oracle, kgb, layout):
 
 @pytest.mark.parametrize("tensor", [1, 0])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_moment_transforms_wide_range(oracle, kgb, tensor, precision):
+@pytest.mark.parametrize("quad", [(8, 16), (8, 24), (12, 24)])
+def test_moment_transforms_wide_range(oracle, kgb, tensor, precision, quad):
     """LTimes / LPlusTimes on signed values spanning 30 decades, zero rows and partial tiles,
-    through the tensor-core digit path (1) and the SIMT path (0)."""
-    p, ctx = pair(oracle, kgb, precision=precision, quad=(8, 16), legendre=4, zones=(7, 5, 3), groups=5)
+    through the tensor-core digit path (1) and the SIMT path (0); 192 and 288 directions run the
+    tensor-core LTimes in several K chunks."""
+    p, ctx = pair(oracle, kgb, precision=precision, quad=quad, legendre=4, zones=(7, 5, 3), groups=5)
     ctx.set_option("moments_tensor", tensor)
     rng = np.random.default_rng(11)
     n = ctx.field_bytes("psi") // 8
@@ -88,6 +90,7 @@ def test_moment_transforms_wide_range(oracle, kgb, tensor, precision):
     p.set("psi", psi); ctx.upload("psi", psi)
     p.kconst("phi", 0.0); ctx.fill("phi", 0.0)
     p.ltimes(); ctx.ltimes()
+    assert ctx.get_option("moments_tensor_ltimes") == tensor
     want, got = p.get("phi"), ctx.download("phi")
     tol = 1e-13 if precision == 0 else 2e-6
     scale = np.abs(want).max()
