@@ -275,19 +275,24 @@ def adjoint_report(local, fd_params=3):
 
     res = {"workload": ADJ_NAME, "unknowns": unknowns(ADJ_WORKLOAD)}
     grads = {}
-    # the mixed form iterates to its FP32 rounding floor (the solves stop when the change stops falling)
-    for name, prec, tol in (("fp64", abi.FP64, 1e-12), ("mixed", abi.MIXED, 1e-9)):
+    # FP64 solves to 1e-12; the mixed form, whose FP32 change stalls near 1e-7 while the far
+    # (detector) region is still converging, runs the FP64 solves' iteration counts
+    counts = {}
+    for name, prec in (("fp64", abi.FP64), ("mixed", abi.MIXED)):
         ctx = abi.Context(local)
         inp = ctx.generate(precision=prec, **ADJ_WORKLOAD)
         ctx.set_response(context_box_detector(ctx, (80.0, 80.0, 80.0), (100.0, 100.0, 100.0)))
-        ctx.solve_converged(1.0, tol, 2000)  # builds the tables; untimed
-        ctx.adjoint_solve(tol, 2000)
-        (fit, fch), t_fwd = timed(lambda: ctx.solve_converged(1.0, tol, 2000))
-        (ait, ach), t_adj = timed(lambda: ctx.adjoint_solve(tol, 2000))
+        tol, nf, na = (1e-12, 2000, 2000) if name == "fp64" else (-1.0, counts["fwd"], counts["adj"])
+        ctx.solve_converged(1.0, tol, nf)  # builds the tables; untimed
+        ctx.adjoint_solve(tol, na)
+        (fit, fch), t_fwd = timed(lambda: ctx.solve_converged(1.0, tol, nf))
+        (ait, ach), t_adj = timed(lambda: ctx.adjoint_solve(tol, na))
+        counts = {"fwd": fit, "adj": ait}
         g, t_grad = timed(ctx.gradient)
         grads[name] = g
-        r = {"tol": tol, "forward_s": t_fwd, "forward_iters": fit, "forward_change": fch, "adjoint_s": t_adj,
-             "adjoint_iters": ait, "adjoint_change": ach,
+        r = {"tol": tol if tol >= 0 else "fixed iteration counts", "forward_s": t_fwd, "forward_iters": fit,
+             "forward_change": fch if tol >= 0 else None, "adjoint_s": t_adj, "adjoint_iters": ait,
+             "adjoint_change": ach if tol >= 0 else None,
              "gradient_assembly_s": t_grad, "grad_over_fwd": (t_adj + t_grad) / t_fwd, "response": g[0]}
         if name == "fp64":
             # central differences (relative step 1e-4) of the GPU forward at the largest gradient entries

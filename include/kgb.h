@@ -174,14 +174,19 @@ int kgb_sync(kgb_ctx *ctx);
 int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
 /* Tuning knobs: "sweep_tile_z" (tile depth in k, default 4); "sweep_tile_xy"
  * (tile footprint in i and j: 44, 42 or 22, default 44); "sweep_reciprocals"
- * (FP64 on a uniform mesh: 1 = tabulate 1/denominator per (sigt value,
- * direction), the default; 0 = divide in every cell); "moments_tensor" (1 = LTimes
- * and LPlusTimes on the tensor cores with exact digit products when the shapes
- * fit; 0 = SIMT kernels; default: tensor for FP64, SIMT for the mixed form). */
+ * (uniform mesh: 1 = tabulate 1/denominator per (sigt value, direction), the
+ * FP64 default; 0 = divide in every cell, the mixed default); "moments_tensor"
+ * (1 = LTimes and LPlusTimes on the tensor cores with exact digit products when
+ * the shapes fit; 0 = SIMT kernels; default: tensor for FP64, SIMT for the
+ * mixed form); "scattering_tensor" (1 = the single-material zones' scattering on
+ * the tensor cores, exact digit products, when groups <= 64; same defaults);
+ * "graph" (1 = kgb_solve replays a captured CUDA graph, the default). */
 int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
-/* Current value of a knob: the keys above, plus "moments_tensor_ltimes" and
- * "moments_tensor_lplustimes" (1 when that transform runs on the tensor cores)
- * and "sweep_reciprocals_active" (1 when the sweep uses tabulated reciprocals). */
+/* Current value of a knob: the keys above, plus "moments_tensor_ltimes",
+ * "moments_tensor_lplustimes" and "scattering_tensor_active" (1 when that
+ * kernel runs on the tensor cores), "sweep_reciprocals_active" (1 when the
+ * sweep uses tabulated reciprocals) and "graph_active" (1 when the last
+ * kgb_solve replayed a graph). */
 int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value);
 /* Autotuner: times every sweep tile shape (footprint 4x4, 4x2, 2x2 x depth
  * 2, 4, 8, 16 zones) and both LTimes / LPlusTimes paths (tensor-core digit
@@ -227,8 +232,9 @@ int kgb_set_response(kgb_ctx *ctx, const double *det, int64_t n);
 /* Source iterations from psi = 0 until moment 0 of successive iterates
  * satisfies max|phi_k - phi_(k-1)| <= tol * max|phi_k|, the change has made
  * no new minimum for 4 iterations (the rounding floor: near 1e-7 for the
- * mixed form's FP32 state), or max_iter iterations ran.  *iters and *change
- * (either may be NULL) receive the count and the last relative change;
+ * mixed form's FP32 state), or max_iter iterations ran; tol < 0 runs exactly
+ * max_iter iterations.  *iters and *change (either may be NULL) receive the
+ * count and the last relative change (with tol < 0, *change is not measured);
  * *change > tol tells that tol was not reached, which is not an error. */
 int kgb_solve_converged(kgb_ctx *ctx, double source_strength, double tol, int32_t max_iter, int32_t *iters,
                         double *change);
@@ -261,12 +267,13 @@ int kgb_gradient_unrolled(kgb_ctx *ctx, int32_t niter, double source_strength, i
  * zone set and Legendre order <= 4, all in the batch's precision, and
  * advances them together: one launch per kernel family for all problems,
  * the sweeps of all problems in ONE persistent cooperative launch, and a
- * whole solve captured once into a CUDA graph and replayed.  LTimes and
- * LPlusTimes run either as batched SIMT launches (the mixed default) or as
- * each problem's own kernels -- the tensor-core digit products in FP64, the
- * FP64 default -- on parallel branches of the graph.  Each problem's results
- * equal its own context's with the same sweep tiles (and "moments_tensor" 0
- * when the batch runs its SIMT moment kernels on an FP64 problem). */
+ * whole solve captured once into a CUDA graph and replayed.  LTimes,
+ * scattering and LPlusTimes run either as batched SIMT launches (the mixed
+ * default) or as each problem's own kernels -- the tensor-core digit products
+ * in FP64, the FP64 default -- on parallel branches of the graph.  Each
+ * problem's results equal its own context's with the same sweep tiles (and
+ * "moments_tensor" 0, "scattering_tensor" 0 when the batch runs its batched
+ * SIMT kernels on FP64 problems). */
 typedef struct kgb_batch kgb_batch;
 int kgb_batch_create(int device, int32_t precision, kgb_batch **out);
 int kgb_batch_destroy(kgb_batch *b);
@@ -280,8 +287,9 @@ int kgb_batch_size(const kgb_batch *b, int32_t *n);
 int kgb_batch_context(kgb_batch *b, int32_t index, kgb_ctx **ctx);
 /* Knobs: "sweep_tile_xy" (44, 42, 22), "sweep_tile_z", "rows_per_item" (rows
  * of a moment / scattering work item), "graph" (1: capture solves, the
- * default), "moments_per_problem" (1: each problem's own moment kernels;
- * 0: batched SIMT; -1: by precision, the default).  Read-only:
+ * default), "per_problem_kernels" (1: each problem's own LTimes,
+ * scattering and LPlusTimes kernels; 0: batched SIMT; -1: by precision, the
+ * default).  Read-only:
  * "graph_active" (the last solve replayed a graph),
  * "sweep_grid" (blocks of the persistent sweep), "sweep_steps",
  * "kernels_per_iteration". */

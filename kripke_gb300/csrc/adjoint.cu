@@ -149,9 +149,8 @@ __global__ void response_finish_kernel(const double *__restrict__ partials, int 
   }
 }
 
-// max |phi(r,0) - prev(r)| and max |phi(r,0)| over rows, then prev = phi(.,0).
-// Non-negative doubles (and +inf, NaN) order like their bit patterns, so the
-// maxima reduce as unsigned integers.
+// max |phi(r,0) - prev(r)| and max |phi(r,0)| over rows, then prev = phi(.,0).  Non-negative doubles (and +inf, NaN) order
+// like their bit patterns, so the maxima reduce as unsigned integers.
 template <typename T>
 __global__ void change_norm_kernel(const T *__restrict__ phi, int M, double *__restrict__ prev, int64_t rows,
                                    unsigned long long *__restrict__ out) {

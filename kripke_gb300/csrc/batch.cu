@@ -4,9 +4,10 @@
 // those of the single-problem path) with one zone set; the batch adds a
 // driver that advances all of them with one launch per kernel family:
 //   LTimes and LPlusTimes .... one launch per moment class, items = row ranges
-//                              (mixed form); in FP64 each problem's own
-//                              tensor-core kernels on parallel graph branches
 //   scattering + source ...... one launch per Legendre order
+//                              (these two in the mixed form; in FP64 each
+//                              problem's own tensor-core kernels run instead,
+//                              on parallel graph branches)
 //   sweep .................... ONE persistent cooperative launch: every block
 //                              takes (problem, subdomain, tile, chain block)
 //                              items of the current global hyperplane step,
@@ -18,7 +19,7 @@
 // candidates on the batch itself.  Every problem's arithmetic is the
 // single-problem path's, term for term, so a problem's psi and particle
 // counts equal those of its own context run with the same sweep tile shape
-// (and, when the batch uses its SIMT moment kernels, the context's SIMT ones).
+// (and, when the batch uses its batched SIMT kernels, the context's SIMT ones).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -42,7 +43,7 @@ struct kgb_batch {
   int tx = 2, ty = 2, tz = 8;
   int rows_per_item = 1024;
   bool use_graph = true;
-  int moments_mode = -1;  // 1: each problem's own moment kernels; 0: batched SIMT; -1: by precision
+  int own_mode = -1;  // 1: each problem's own LTimes/scattering/LPlusTimes kernels; 0: batched SIMT; -1: by precision
 
   // streams the per-problem moment kernels fork onto (graph branches when captured)
   static constexpr int kForks = 4;
@@ -169,7 +170,7 @@ void groupRows(const std::vector<BatchRows> &rows, KeyFn key, std::vector<BatchR
   }
 }
 
-bool perProblemMoments(const kgb_batch *b) { return b->moments_mode < 0 ? b->prec == KGB_FP64 : b->moments_mode == 1; }
+bool perProblem(const kgb_batch *b) { return b->own_mode < 0 ? b->prec == KGB_FP64 : b->own_mode == 1; }
 
 template <typename T>
 int planT(kgb_batch *b) {
@@ -307,8 +308,8 @@ int planT(kgb_batch *b) {
   b->sweep_grid = batch_sweep_grid<T>(b->tx, b->ty, b->nsm);
   if (b->sweep_grid <= 0) return fail(b, KGB_ERR_CUDA, "the persistent sweep has no resident blocks");
   b->row_grid = b->nsm * 16;
-  b->kernels_per_iter = (perProblemMoments(b) ? 2 * (int64_t)n : (int64_t)b->lt_cls.size() + b->lp_cls.size()) +
-                        (int64_t)b->sc_cls.size() + 2;
+  b->kernels_per_iter = perProblem(b) ? 3 * (int64_t)n + 2
+                                      : (int64_t)b->lt_cls.size() + b->lp_cls.size() + b->sc_cls.size() + 2;
   BCK(cudaStreamSynchronize(b->stream));
   b->planned = true;
   return KGB_OK;
@@ -332,14 +333,14 @@ int ensurePlan(kgb_batch *b) {
   return b->planned ? KGB_OK : plan(b);
 }
 
-// Each problem's own LTimes / LPlusTimes (the tensor-core digit products in
+// Each problem's own kernels for one phase (the tensor-core digit products in
 // FP64), spread over kForks streams forked from and joined back to the batch
 // stream -- parallel branches of the captured graph.
-int forkMoments(kgb_batch *b, bool plus) {
+int forkPhase(kgb_batch *b, InstanceOp op) {
   BCK(cudaEventRecord(b->fork_ev, b->stream));
   for (int k = 0; k < kgb_batch::kForks; ++k) BCK(cudaStreamWaitEvent(b->aux[k], b->fork_ev, 0));
   for (size_t i = 0; i < b->inst.size(); ++i) {
-    const int rc = instance_moments(b->inst[i], plus, b->aux[i % kgb_batch::kForks]);
+    const int rc = instance_op(b->inst[i], op, b->q, b->aux[i % kgb_batch::kForks]);
     if (rc) return fail(b, rc, "problem " + std::to_string(i) + ": " + kgb_last_error(b->inst[i]));
   }
   for (int k = 0; k < kgb_batch::kForks; ++k) {
@@ -356,22 +357,26 @@ int enqueueIteration(kgb_batch *b, double *pop_out, cudaEvent_t *ev = nullptr) {
   const auto *lt = (const BatchMom<T> *)b->lt_desc;
   const auto *lp = (const BatchMom<T> *)b->lp_desc;
   const auto *sc = (const BatchScat<T> *)b->sc_desc;
-  const bool own = perProblemMoments(b);
+  const bool own = perProblem(b);
   int rc;
   if (ev) BCK(cudaEventRecord(ev[0], b->stream));
   if (own) {
-    if ((rc = forkMoments(b, false))) return rc;
+    if ((rc = forkPhase(b, InstanceOp::LTimes))) return rc;
   } else {
     for (auto &c : b->lt_cls)
       launch_batch_moments<T>(lt, b->rows_lt + c.off, c.n, c.key, b->Dmax, false, c.vec,
                               std::min(c.n, b->row_grid), b->stream);
   }
   if (ev) BCK(cudaEventRecord(ev[1], b->stream));
-  for (auto &c : b->sc_cls)
-    launch_batch_scattering<T>(sc, b->rows_sc + c.off, c.n, c.key, std::min(c.n, b->row_grid), b->stream);
+  if (own) {
+    if ((rc = forkPhase(b, InstanceOp::Scatter))) return rc;
+  } else {
+    for (auto &c : b->sc_cls)
+      launch_batch_scattering<T>(sc, b->rows_sc + c.off, c.n, c.key, std::min(c.n, b->row_grid), b->stream);
+  }
   if (ev) BCK(cudaEventRecord(ev[2], b->stream));
   if (own) {
-    if ((rc = forkMoments(b, true))) return rc;
+    if ((rc = forkPhase(b, InstanceOp::LPlusTimes))) return rc;
   } else {
     for (auto &c : b->lp_cls)
       launch_batch_moments<T>(lp, b->rows_lp + c.off, c.n, c.key, b->Dmax, true, c.vec,
@@ -580,8 +585,8 @@ int kgb_batch_set_option(kgb_batch *b, const char *key, int64_t value) {
     b->rows_per_item = (int)value;
   } else if (k == "graph") {
     b->use_graph = value != 0;
-  } else if (k == "moments_per_problem") {
-    b->moments_mode = value < 0 ? -1 : (value != 0 ? 1 : 0);
+  } else if (k == "per_problem_kernels") {
+    b->own_mode = value < 0 ? -1 : (value != 0 ? 1 : 0);
   } else {
     return fail(b, KGB_ERR_ARG, "unknown option '" + k + "'");
   }
@@ -597,7 +602,7 @@ int kgb_batch_get_option(kgb_batch *b, const char *key, int64_t *value) {
   else if (k == "sweep_tile_z") *value = b->tz;
   else if (k == "rows_per_item") *value = b->rows_per_item;
   else if (k == "graph") *value = b->use_graph;
-  else if (k == "moments_per_problem") *value = perProblemMoments(b);
+  else if (k == "per_problem_kernels") *value = perProblem(b);
   else if (k == "graph_active") *value = b->graph_active;
   else if (k == "sweep_grid") *value = b->sweep_grid;
   else if (k == "sweep_steps") *value = b->nsteps;

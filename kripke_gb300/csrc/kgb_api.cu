@@ -179,6 +179,17 @@ struct kgb_ctx {
   bool have_lam = false;        // an adjoint solve has filled lam
   int flip = 0;                 // 1 while the adjoint operators are installed
 
+  // tensor-core scattering of single-material zones: digit images of every
+  // (material, order) matrix (transposed for the forward operator, as is for
+  // the adjoint), the zones of each material, and the other zones (SIMT)
+  bool tc_sc = false, use_tc_sc = true, allow_tc_sc = true, dirty_tcsc = true;
+  uint16_t *tc_sc_img = nullptr, *tc_sc_img_adj = nullptr;
+  int *tc_sc_exp = nullptr, *tc_sc_exp_adj = nullptr;
+  int tc_sc_kpad = 0;
+  int *pure_z = nullptr, *mixed_z = nullptr;
+  int64_t pure_off[4] = {0, 0, 0, 0};
+  int64_t nmixed_z = 0;
+
   // captured solves (kgb_solve): valid while gen, bumped whenever a table,
   // tile list or kernel choice a capture baked in may have changed, is unchanged
   uint64_t gen = 0;
@@ -389,7 +400,8 @@ void freeAll(kgb_ctx *c) {
                   c->results, c->parts_dev, c->staging, c->cls_d, c->inv_d, c->pop_slots, c->tc_lt_img,
                   c->tc_lp_img, c->tc_lt_exp, c->tc_lp_exp, c->err_d, c->lam, c->phi_prev, c->sigsT_adj,
                   c->gp_lo_adj, c->gp_hi_adj, c->colsum_d, c->e0_d, c->det_d, c->norm_d, c->resp_part, c->resp_d,
-                  c->tc_lt_img_adj, c->tc_lp_img_adj, c->tc_lt_exp_adj, c->tc_lp_exp_adj};
+                  c->tc_lt_img_adj, c->tc_lp_img_adj, c->tc_lt_exp_adj, c->tc_lp_exp_adj, c->tc_sc_img,
+                  c->tc_sc_img_adj, c->tc_sc_exp, c->tc_sc_exp_adj, c->pure_z};  // mixed_z lies inside pure_z
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->psi = c->rhs = c->phi = c->phi_out = c->sigt = nullptr;
@@ -418,6 +430,12 @@ void freeAll(kgb_ctx *c) {
   c->tc_lt_img_adj = c->tc_lp_img_adj = nullptr;
   c->tc_lt_exp_adj = c->tc_lp_exp_adj = nullptr;
   c->tc_lt_adj = c->tc_lp_adj = false;
+  c->tc_sc_img = c->tc_sc_img_adj = nullptr;
+  c->tc_sc_exp = c->tc_sc_exp_adj = nullptr;
+  c->pure_z = c->mixed_z = nullptr;
+  c->tc_sc = false;
+  c->dirty_tcsc = true;
+  c->nmixed_z = 0;
   c->resp_nb = 0;
   c->adj_stale = true;
   c->have_lam = false;
@@ -602,6 +620,77 @@ int planTensorMoments(kgb_ctx *ctx) {
                                   &ctx->tc_lt_kpad, &ctx->tc_lp, &ctx->tc_lp_img, &ctx->tc_lp_exp, &ctx->tc_lp_nhalf);
 }
 
+// Tensor-core scattering plan: the single-material zones of each material take
+// phi_out(z, ., m) = S(mat, l(m)) phi(z, ., m) as tcgen05 row products over
+// (zone, moment) rows with the exact digit products of the moment transforms
+// (K = N = groups <= 64); zones with several materials keep the SIMT kernel.
+template <typename T>
+int planTensorScatter(kgb_ctx *ctx) {
+  ctx->tc_sc = false;
+  const int G = ctx->G, L1 = ctx->L + 1, S = sizeof(T) == 8 ? 8 : 4, NB = 64;
+  if (!ctx->allow_tc_sc || G > 64) return KGB_OK;
+  // zone lists from the device mixing tables
+  std::vector<int> zs(ctx->Z), zc(ctx->Z), mm(std::max<int64_t>(ctx->nmix, 1));
+  std::vector<double> mf(std::max<int64_t>(ctx->nmix, 1));
+  CK(cudaMemcpyAsync(zs.data(), ctx->zmix_start, ctx->Z * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(zc.data(), ctx->zmix_count, ctx->Z * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  if (ctx->nmix > 0) {
+    CK(cudaMemcpyAsync(mm.data(), ctx->mix_mat, ctx->nmix * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(mf.data(), ctx->mix_frac, ctx->nmix * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::vector<int> pure[3], mixed;
+  for (int64_t z = 0; z < ctx->Z; ++z) {
+    if (zc[z] == 1 && mf[zs[z]] == 1.0) pure[mm[zs[z]]].push_back((int)z);
+    else mixed.push_back((int)z);
+  }
+  std::vector<int> lists;
+  for (int m = 0; m < 3; ++m) {
+    ctx->pure_off[m] = (int64_t)lists.size();
+    lists.insert(lists.end(), pure[m].begin(), pure[m].end());
+  }
+  ctx->pure_off[3] = (int64_t)lists.size();
+  ctx->nmixed_z = (int64_t)mixed.size();
+  lists.insert(lists.end(), mixed.begin(), mixed.end());
+  if (ctx->pure_z) cudaFree(ctx->pure_z);
+  ctx->pure_z = ctx->mixed_z = nullptr;
+  int rc;
+  if ((rc = dmalloc(ctx, &ctx->pure_z, lists.size()))) return rc;
+  ctx->mixed_z = ctx->pure_z + ctx->pure_off[3];
+  CK(cudaMemcpyAsync(ctx->pure_z, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  // digit images: forward B[k][n] = S(n <- k), adjoint B[k][n] = S(k <- n)
+  const int kpad = (G + 31) / 32 * 32;
+  std::vector<double> b((size_t)G * G);
+  std::vector<uint16_t> img, all;
+  std::vector<int> ex, allex;
+  for (int adj = 0; adj < 2; ++adj) {
+    all.clear();
+    allex.clear();
+    for (int m = 0; m < 3; ++m)
+      for (int l = 0; l < L1; ++l) {
+        const double *sm = ctx->sigs_h.data() + ((size_t)m * L1 + l) * G * G;
+        for (int k = 0; k < G; ++k)
+          for (int n = 0; n < G; ++n) b[(size_t)k * G + n] = adj ? sm[(size_t)k * G + n] : sm[(size_t)n * G + k];
+        tc_build_b<T>(b.data(), G, G, kpad, S, NB, 1, img, ex);
+        all.insert(all.end(), img.begin(), img.end());
+        allex.insert(allex.end(), ex.begin(), ex.end());
+      }
+    uint16_t *&dimg = adj ? ctx->tc_sc_img_adj : ctx->tc_sc_img;
+    int *&dexp = adj ? ctx->tc_sc_exp_adj : ctx->tc_sc_exp;
+    if (dimg) cudaFree(dimg);
+    if (dexp) cudaFree(dexp);
+    dimg = nullptr;
+    dexp = nullptr;
+    if ((rc = dmalloc(ctx, &dimg, all.size())) || (rc = dmalloc(ctx, &dexp, allex.size()))) return rc;
+    CK(cudaMemcpyAsync(dimg, all.data(), all.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(dexp, allex.data(), allex.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // the host vectors are reused
+  }
+  ctx->tc_sc_kpad = kpad;
+  ctx->tc_sc = true;
+  return KGB_OK;
+}
+
 template <typename T>
 int prepareT(kgb_ctx *ctx) {
   int rc;
@@ -699,6 +788,7 @@ int prepareT(kgb_ctx *ctx) {
     CK(cudaMemcpyAsync(ctx->gp_hi, hi.data(), G * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_sigs = false;
+    ctx->dirty_tcsc = true;
     ++ctx->gen;
     ctx->adj_stale = true;
   }
@@ -765,6 +855,12 @@ int prepareT(kgb_ctx *ctx) {
     CK(cudaMemcpyAsync(ctx->mix_frac, mfr.data(), total * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_mix = false;
+    ctx->dirty_tcsc = true;
+    ++ctx->gen;
+  }
+  if (ctx->dirty_tcsc) {
+    if ((rc = planTensorScatter<T>(ctx))) return rc;
+    ctx->dirty_tcsc = false;
     ++ctx->gen;
   }
   if (ctx->dirty_sigt) {
@@ -1003,8 +1099,49 @@ int doLPlusTimes(kgb_ctx *ctx, bool acc) {
   return KGB_OK;
 }
 
+template <typename T>
+int scatterTensor(kgb_ctx *ctx, bool acc) {
+  const int G = ctx->G, L1 = ctx->L + 1, S = sizeof(T) == 8 ? 8 : 4, kpad = ctx->tc_sc_kpad;
+  for (int m = 0; m < 3; ++m) {
+    const int64_t nz = ctx->pure_off[m + 1] - ctx->pure_off[m];
+    if (nz == 0) continue;
+    for (int l = 0; l < L1; ++l) {
+      TcArgs<T> a{};
+      a.A = as<T>(ctx->phi);
+      a.C = as<T>(ctx->phi_out);
+      a.rows = nz * (2 * l + 1);
+      a.K = G;
+      a.kpad = kpad;
+      a.N = G;
+      a.nhalf = 1;
+      a.bimg = ctx->tc_sc_img + ((size_t)m * L1 + l) * kpad * S * 64;
+      a.bexp = ctx->tc_sc_exp + ((size_t)m * L1 + l) * 64;
+      a.err = ctx->err_d;
+      a.accumulate = acc;
+      a.nsm = ctx->nsm;
+      a.zl = ctx->pure_z + ctx->pure_off[m];
+      a.nm = 2 * l + 1;
+      a.m0 = l * l;
+      a.ks = ctx->M;
+      a.zstride = (int64_t)G * ctx->M;
+      launch_tc_gather<T>(a, ctx->stream);
+      CKN(1);
+    }
+  }
+  if (ctx->nmixed_z > 0) {
+    ScatterArgsBase a = scatterArgs(ctx);
+    a.Z = ctx->nmixed_z;
+    a.zlist = ctx->mixed_z;
+    launch_scattering<T>(as<T>(ctx->phi), as<T>(ctx->phi_out), as<T>(ctx->sigsT), a, acc, ctx->stream);
+    CKN(1);
+  }
+  return KGB_OK;
+}
+
 int doScattering(kgb_ctx *ctx, bool acc) {
   FamScope fs(ctx, "scattering");
+  if (ctx->tc_sc && ctx->use_tc_sc)
+    return ctx->prec == KGB_FP64 ? scatterTensor<double>(ctx, acc) : scatterTensor<float>(ctx, acc);
   ScatterArgsBase a = scatterArgs(ctx);
   if (ctx->prec == KGB_FP64)
     launch_scattering<double>(as<double>(ctx->phi), as<double>(ctx->phi_out), as<double>(ctx->sigsT), a, acc, ctx->stream);
@@ -1192,6 +1329,8 @@ struct AdjointView {
     std::swap(c->tc_lp_exp, c->tc_lp_exp_adj);
     std::swap(c->tc_lt_kpad, c->tc_lt_kpad_adj);
     std::swap(c->tc_lp_nhalf, c->tc_lp_nhalf_adj);
+    std::swap(c->tc_sc_img, c->tc_sc_img_adj);
+    std::swap(c->tc_sc_exp, c->tc_sc_exp_adj);
     c->flip ^= 1;
   }
 };
@@ -1210,7 +1349,8 @@ int doAdjointSource(kgb_ctx *ctx) {
 // Source iterations from a zero state until moment 0 of successive iterates
 // changes by at most tol relative to its largest magnitude, or the change has
 // not reached a new minimum for kStall iterations (the rounding floor, which
-// the FP32 state of the mixed form meets near 1e-7).  The change is measured
+// the FP32 state of the mixed form meets near 1e-7; the change falls
+// monotonically above it).  The change is measured
 // on the moments each iteration computes first (phi = L psi of the previous
 // iterate), so the test lags one sweep and the returned state is one
 // iteration past the converged one.  With the adjoint operators installed it
@@ -1242,7 +1382,7 @@ int convergeLoop(kgb_ctx *ctx, bool adjoint, double q, double tol, int max_iter,
     unsigned long long h[2] = {0ull, 0ull};
     CK(cudaMemcpyAsync(h, ctx->norm_d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    if (it >= 2) {
+    if (it >= 2 && tol >= 0.0) {
       double dmax, amax;
       std::memcpy(&dmax, &h[0], sizeof(double));
       std::memcpy(&amax, &h[1], sizeof(double));
@@ -1412,10 +1552,18 @@ int instance_view(kgb_ctx *ctx, InstanceView *v) {
   return KGB_OK;
 }
 
-int instance_moments(kgb_ctx *ctx, bool plus, cudaStream_t s) {
+int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s) {
   cudaStream_t keep = ctx->stream;
   ctx->stream = s;
-  const int rc = plus ? doLPlusTimes(ctx, false) : doLTimes(ctx, false);
+  int rc;
+  switch (op) {
+    case InstanceOp::LTimes: rc = doLTimes(ctx, false); break;
+    case InstanceOp::LPlusTimes: rc = doLPlusTimes(ctx, false); break;
+    default:
+      rc = doScattering(ctx, false);
+      if (!rc) rc = doSource(ctx, q);
+      break;
+  }
   ctx->stream = keep;
   return rc;
 }
@@ -1490,6 +1638,10 @@ int kgb_setup(kgb_ctx *ctx, const kgb_dims *d) {
   // measured defaults: the digit-product tensor path wins for FP64, SIMT for the mixed form;
   // kgb_autotune re-measures both on the actual problem
   ctx->use_tc_lt = ctx->use_tc_lp = ctx->prec == KGB_FP64;
+  ctx->use_tc_sc = ctx->prec == KGB_FP64;
+  // the tabulated reciprocal pays where the divide costs FP64 slots; in FP32 its
+  // dependent table load costs more than the divide it saves
+  ctx->allow_recip = ctx->prec == KGB_FP64;
   ctx->dc.SP = d->num_groupsets;
   ctx->dc.SQ = d->num_dirsets;
   ctx->dc.Sx = d->num_zonesets[0];
@@ -2010,6 +2162,12 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->dirty_ell = true;
     return KGB_OK;
   }
+  if (!std::strcmp(key, "scattering_tensor")) {
+    ctx->allow_tc_sc = value != 0;
+    ctx->use_tc_sc = value != 0;
+    ctx->dirty_tcsc = true;
+    return KGB_OK;
+  }
   if (!std::strcmp(key, "sweep_reciprocals")) {
     ctx->allow_recip = value != 0;
     ctx->dirty_sigt = true;
@@ -2082,6 +2240,22 @@ int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_
     if ((rc = timeIt(lt, true, t_tc)) || (rc = timeIt(lt, false, t_simt))) break;
     (lt ? ctx->use_tc_lt : ctx->use_tc_lp) = t_tc <= t_simt;
   }
+  // scattering: tensor-core digit products for single-material zones, or SIMT
+  auto timeScat = [&](bool tc, float &ms) -> int {
+    ctx->use_tc_sc = tc;
+    int r = doScattering(ctx, false);
+    if (r) return r;
+    CK(cudaEventRecord(f0, ctx->stream));
+    for (int k = 0; k < 2 && !r; ++k) r = doScattering(ctx, false);
+    CK(cudaEventRecord(f1, ctx->stream));
+    CK(cudaEventSynchronize(f1));
+    CK(cudaEventElapsedTime(&ms, f0, f1));
+    return r ? r : checkDeviceError(ctx);
+  };
+  if (!rc && ctx->tc_sc) {
+    float t_tc = 0.f, t_simt = 0.f;
+    if (!(rc = timeScat(true, t_tc)) && !(rc = timeScat(false, t_simt))) ctx->use_tc_sc = t_tc <= t_simt;
+  }
   ++ctx->gen;  // kernel choices may have changed
   cudaEventDestroy(f0);
   cudaEventDestroy(f1);
@@ -2102,6 +2276,8 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "moments_tensor_ltimes")) *value = (ctx->tc_lt && ctx->use_tc_lt) ? 1 : 0;
   else if (!std::strcmp(key, "moments_tensor_lplustimes")) *value = (ctx->tc_lp && ctx->use_tc_lp) ? 1 : 0;
   else if (!std::strcmp(key, "graph")) *value = ctx->use_graph ? 1 : 0;
+  else if (!std::strcmp(key, "scattering_tensor")) *value = ctx->allow_tc_sc ? 1 : 0;
+  else if (!std::strcmp(key, "scattering_tensor_active")) *value = (ctx->tc_sc && ctx->use_tc_sc) ? 1 : 0;
   else if (!std::strcmp(key, "graph_active")) *value = ctx->graph_active ? 1 : 0;
   else return fail(ctx, KGB_ERR_ARG, std::string("unknown option '") + key + "'");
   return KGB_OK;
@@ -2191,7 +2367,7 @@ int kgb_solve_converged(kgb_ctx *ctx, double source_strength, double tol, int32_
                         double *change) {
   int rc = prepare(ctx);
   if (rc) return rc;
-  if (max_iter < 1 || !(tol >= 0.0)) return fail(ctx, KGB_ERR_ARG, "need max_iter >= 1 and tol >= 0");
+  if (max_iter < 1 || std::isnan(tol)) return fail(ctx, KGB_ERR_ARG, "need max_iter >= 1 and a tolerance");
   if ((rc = ensureResponseBuffers(ctx))) return rc;
   if ((rc = convergeLoop(ctx, false, source_strength, tol, max_iter, iters, change))) return rc;
   return checkDeviceError(ctx);
@@ -2200,7 +2376,7 @@ int kgb_solve_converged(kgb_ctx *ctx, double source_strength, double tol, int32_
 int kgb_adjoint_solve(kgb_ctx *ctx, double tol, int32_t max_iter, int32_t *iters, double *change) {
   int rc = prepare(ctx);
   if (rc) return rc;
-  if (max_iter < 1 || !(tol >= 0.0)) return fail(ctx, KGB_ERR_ARG, "need max_iter >= 1 and tol >= 0");
+  if (max_iter < 1 || std::isnan(tol)) return fail(ctx, KGB_ERR_ARG, "need max_iter >= 1 and a tolerance");
   if ((rc = prepareAdjoint(ctx))) return rc;
   if (ctx->inv_c0 == 0.0)
     return fail(ctx, KGB_ERR_ARG, "the adjoint source needs ell(0, d) proportional to the quadrature weight w(d)");

@@ -70,7 +70,8 @@ template <typename T>
 void launch_lplustimes(const T *phi_out, T *rhs, const T *ellp_dm, int64_t rows, int D, int M, bool accumulate, cudaStream_t s);
 
 struct ScatterArgsBase {
-  int64_t Z;
+  int64_t Z;                  // zones (rows = Z * destination groups); with zlist, the list's length
+  const int *zlist;           // zones to update, or null: every zone
   int G, M, L;
   const int *zmix_start, *zmix_count, *mix_mat;
   const double *mix_frac;
@@ -98,12 +99,19 @@ struct TcArgs {
   int *err;              // set to 1 when a bounded wait gives up
   bool accumulate;
   int nsm;
+  // gathered rows (launch_tc_gather): row r = zone zl[r / nm], moment m0 + r % nm;
+  // A and C elements at zone * zstride + moment + k * ks
+  const int *zl;
+  int nm, m0, ks;
+  int64_t zstride;
 };
 template <typename T>
 void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhalf, std::vector<uint16_t> &img,
                 std::vector<int> &texp);
 template <typename T>
 void launch_tc_rows(const TcArgs<T> &a, int S, int NB, bool multi_n, cudaStream_t s);
+template <typename T>
+void launch_tc_gather(const TcArgs<T> &a, cudaStream_t s);
 
 // FP64 reductions, two passes with a fixed order: per-block partials then one block.
 template <typename T>
@@ -210,9 +218,11 @@ struct InstanceView {
   uint64_t gen;         // the context's table generation: changes whenever a table, tile list or kernel choice changes
 };
 int instance_view(kgb_ctx *ctx, InstanceView *v);
-// The context's own LTimes (plus = false) or LPlusTimes, overwriting phi / rhs,
-// launched on stream s (tensor-core or SIMT as the context chooses).
-int instance_moments(kgb_ctx *ctx, bool plus, cudaStream_t s);
+// One of the context's own iteration kernels, launched on stream s with the
+// kernels the context chooses (tensor-core or SIMT): LTimes (phi = L psi),
+// LPlusTimes (rhs = L+ phi_out), or scattering then source (phi_out = S phi + q).
+enum class InstanceOp { LTimes, Scatter, LPlusTimes };
+int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s);
 
 // Response, adjoint source and gradients (adjoint.cu).
 struct MixArgs {

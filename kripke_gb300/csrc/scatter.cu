@@ -33,8 +33,9 @@ __device__ __forceinline__ void scatterRow(const T *__restrict__ phi, T *__restr
                                            bool accumulate, double q) {
   constexpr int MM = (LMAX + 1) * (LMAX + 1);
   const int Gd = a.dst_ghi - a.dst_glo;
-  const int64_t z = r / Gd;
-  const int g = a.dst_glo + (int)(r - z * Gd);
+  const int64_t zi = r / Gd;
+  const int64_t z = a.zlist ? (int64_t)a.zlist[zi] : zi;
+  const int g = a.dst_glo + (int)(r - zi * Gd);
   const int ms = a.zmix_start[z], mcnt = a.zmix_count[z];
   // a single-material zone has fraction exactly 1, where the reference's
   // 0 + sigs*fraction is sigs itself

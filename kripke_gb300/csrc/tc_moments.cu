@@ -193,7 +193,10 @@ template <typename T> struct TcBias;
 template <> struct TcBias<double> { static constexpr int v = 1022; };
 template <> struct TcBias<float> { static constexpr int v = 126; };
 
-template <typename T, int S, int NB, bool MULTI_N>
+// GATHER: rows are (zone, moment) pairs of the device nesting [zone][group][moment]
+// (the scattering's operand): row r is zone zl[r / nm], moment m0 + r % nm, and
+// its element k (A) or n (C) lies ks elements after the row's base.
+template <typename T, int S, int NB, bool MULTI_N, bool GATHER>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ uint64_t bars[3];  // 0,1: A buffers (MMA done), 2: B image load / per-block MMA done
@@ -248,17 +251,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
 
   const int ntiles = (int)((a.rows + kTcRows - 1) / kTcRows);
   const int nchunks = a.kpad / kTcChunk;
-  const bool vec = (a.lda * sizeof(T)) % 16 == 0;  // 16-byte loads of row segments
+  const bool vec = !GATHER && (a.lda * sizeof(T)) % 16 == 0;  // 16-byte loads of row segments
+  // element k of a row at its base + k * kstride
+  const int64_t kstride = GATHER ? a.ks : 1;
+  auto rowBase = [&](int64_t r) -> int64_t {
+    if constexpr (GATHER) {
+      const int64_t q = r / a.nm;
+      return (int64_t)a.zl[q] * a.zstride + a.m0 + (r - q * a.nm);
+    } else {
+      return r * a.lda;
+    }
+  };
   uint32_t item = 0;
   for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
     const int64_t row = (int64_t)tile * kTcRows + srow;
     const bool valid = row < a.rows;
-    const T *arow = a.A + row * a.lda;
+    const T *arow = a.A + (valid ? rowBase(row) : 0);
     // row exponent: largest biased exponent of the row, over the 4 threads of the row
     int emax = 1;
     if (valid) {
-      if (vec && a.K % kTcChunk == 0) {
-        // all of this thread's K groups at once (independent 16-byte loads)
+      if (vec && a.K == a.kpad) {
+        // all of this thread's K groups at once (independent 16-byte loads; the row has kpad elements)
 #pragma unroll 4
         for (int c = 0; c < nchunks; ++c) {
           const T *p8 = arow + c * kTcChunk + part * 8;
@@ -282,7 +295,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
           const int k0 = c * kTcChunk + part * 8;
 #pragma unroll
           for (int e = 0; e < 8; ++e)
-            if (k0 + e < a.K) emax = max(emax, expOf(arow[k0 + e]));
+            if (k0 + e < a.K) emax = max(emax, expOf(arow[(k0 + e) * kstride]));
         }
       }
     }
@@ -320,7 +333,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
         }
       } else {
 #pragma unroll
-        for (int e = 0; e < 8; ++e) x[e] = (valid && k0 + e < a.K) ? arow[k0 + e] : T(0);
+        for (int e = 0; e < 8; ++e) x[e] = (valid && k0 + e < a.K) ? arow[(k0 + e) * kstride] : T(0);
       }
       uint32_t w[S][4];
 #pragma unroll
@@ -370,7 +383,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
     const int64_t orow = (int64_t)tile * kTcRows + erow;
     const bool ovalid = orow < a.rows;
     const int oemax = row_emax[erow] - TcBias<T>::v;
-    T *crow = a.C + orow * a.ldc;
+    T *crow = a.C + (ovalid ? (GATHER ? rowBase(orow) : orow * a.ldc) : 0);
     for (int hf = 0; hf < a.nhalf && ok; ++hf) {
       if (MULTI_N) {
         if (tid == 0) {
@@ -418,7 +431,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
           const int nb = hf * NB + c0;
 #pragma unroll
           for (int u = 0; u < 8; ++u)
-            if (nb + u < a.N) crow[nb + u] = a.accumulate ? crow[nb + u] + out[u] : out[u];
+            if (nb + u < a.N) {
+              T &dst = crow[(nb + u) * kstride];
+              dst = a.accumulate ? dst + out[u] : out[u];
+            }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
@@ -437,16 +453,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
-template <typename T, int S, int NB, bool MULTI_N>
+template <typename T, int S, int NB, bool MULTI_N, bool GATHER = false>
 void launchRows(const TcArgs<T> &a, cudaStream_t s) {
   const size_t halfBytes = (size_t)a.kpad * S * NB * 2;
   const size_t bufBytes = (size_t)S * kTcChunk * kTcRows * 2;
   const size_t smem = 1024 + ((halfBytes * a.nhalf + 1023) & ~(size_t)1023) + (MULTI_N ? 1 : 2) * bufBytes +
                       sizeof(int) * a.nhalf * NB;
-  cudaFuncSetAttribute(tc_rows_kernel<T, S, NB, MULTI_N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(tc_rows_kernel<T, S, NB, MULTI_N, GATHER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
   const int64_t ntiles = (a.rows + kTcRows - 1) / kTcRows;
   const int grid = (int)(ntiles < a.nsm ? ntiles : a.nsm);
-  tc_rows_kernel<T, S, NB, MULTI_N><<<grid, kTcThreads, smem, s>>>(a);
+  tc_rows_kernel<T, S, NB, MULTI_N, GATHER><<<grid, kTcThreads, smem, s>>>(a);
 }
 
 }  // namespace
@@ -511,9 +528,19 @@ void launch_tc_rows(const TcArgs<T> &a, int S, int NB, bool multi_n, cudaStream_
   (void)NB;
 }
 
+// Scattering of pure zones on the tensor cores: K = N = groups (<= 64), rows
+// gathered as (zone, moment) pairs, B = the material's order-l matrix transposed.
+template <typename T>
+void launch_tc_gather(const TcArgs<T> &a, cudaStream_t s) {
+  if constexpr (sizeof(T) == 8) launchRows<T, 8, 64, false, true>(a, s);
+  else launchRows<T, 4, 64, false, true>(a, s);
+}
+
 template void tc_build_b<double>(const double *, int, int, int, int, int, int, std::vector<uint16_t> &, std::vector<int> &);
 template void tc_build_b<float>(const double *, int, int, int, int, int, int, std::vector<uint16_t> &, std::vector<int> &);
 template void launch_tc_rows<double>(const TcArgs<double> &, int, int, bool, cudaStream_t);
 template void launch_tc_rows<float>(const TcArgs<float> &, int, int, bool, cudaStream_t);
+template void launch_tc_gather<double>(const TcArgs<double> &, cudaStream_t);
+template void launch_tc_gather<float>(const TcArgs<float> &, cudaStream_t);
 
 }  // namespace kgb

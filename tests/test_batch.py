@@ -29,8 +29,9 @@ def single_run(kgb, b, i, niter):
     c = b.context(i)
     c.set_option("sweep_tile_xy", b.get_option("sweep_tile_xy"))
     c.set_option("sweep_tile_z", b.get_option("sweep_tile_z"))
-    if not b.get_option("moments_per_problem"):
+    if not b.get_option("per_problem_kernels"):
         c.set_option("moments_tensor", 0)
+        c.set_option("scattering_tensor", 0)
     return np.array(c.solve(niter)), c.download("psi")
 
 
@@ -50,7 +51,7 @@ def test_batch_equals_single_contexts(kgb, prec, own, tiles):
     b = make_batch(kgb, small_set(kgb, precision=precision), precision)
     b.set_option("sweep_tile_xy", tiles[0])
     b.set_option("sweep_tile_z", tiles[1])
-    b.set_option("moments_per_problem", own)
+    b.set_option("per_problem_kernels", own)
     niter = 4
     parts = b.solve(niter)
     assert b.get_option("graph_active") == 1

@@ -105,16 +105,43 @@ def test_moment_transforms_wide_range(oracle, kgb, tensor, precision, quad):
 
 
 @pytest.mark.parametrize("scatter,gset", [(0, 1), (1, 1), (1, 4)])
-def test_scattering_and_source(oracle, kgb, scatter, gset):
+@pytest.mark.parametrize("tensor", [1, 0])
+def test_scattering_and_source(oracle, kgb, scatter, gset, tensor):
+    """Scattering (accumulating into phi_out) and the source; tensor 1 puts the single-material
+    zones on the tcgen05 digit products, tensor 0 keeps every zone on the SIMT kernel."""
     p, ctx = pair(oracle, kgb, scatter=scatter, gset=gset, groups=8, legendre=3, geometry=1, zones=(8, 6, 7))
+    ctx.set_option("scattering_tensor", tensor)
     rng = np.random.default_rng(3)
     phi = rng.uniform(0.0, 1.0, ctx.field_bytes("phi") // 8)
     p.set("phi", phi); ctx.upload("phi", phi)
-    p.kconst("phi_out", 0.0); ctx.fill("phi_out", 0.0)
+    out0 = rng.uniform(0.0, 1.0, ctx.field_bytes("phi_out") // 8)
+    p.set("phi_out", out0); ctx.upload("phi_out", out0)
     p.scattering(); ctx.scattering()
+    assert ctx.get_option("scattering_tensor_active") == tensor
     check(ctx.download("phi_out"), p.get("phi_out"), 1e-13)
     p.source(); ctx.source(1.0)
     check(ctx.download("phi_out"), p.get("phi_out"), 1e-13)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("groups,legendre", [(64, 4), (37, 2), (16, 0)])
+def test_scattering_tensor_wide_range(oracle, kgb, precision, groups, legendre):
+    """Tensor-core scattering on values spanning decades, zero moments and odd group counts,
+    against the oracle (FP64 1e-13, mixed 2e-6 relative to the largest entry)."""
+    p, ctx = pair(oracle, kgb, precision=precision, scatter=1, groups=groups, legendre=legendre, geometry=1,
+                  zones=(9, 7, 5), quad=16)
+    ctx.set_option("scattering_tensor", 1)
+    rng = np.random.default_rng(5)
+    n = ctx.field_bytes("phi") // 8
+    phi = rng.standard_normal(n) * 10.0 ** rng.uniform(-20 if precision == 0 else -6, 2, n)
+    phi[: n // 9] = 0.0
+    p.set("phi", phi); ctx.upload("phi", phi)
+    p.kconst("phi_out", 0.0); ctx.fill("phi_out", 0.0)
+    p.scattering(); ctx.scattering()
+    assert ctx.get_option("scattering_tensor_active") == 1
+    want, got = p.get("phi_out"), ctx.download("phi_out")
+    tol = 1e-13 if precision == 0 else 2e-6
+    assert np.max(np.abs(got - want)) <= tol * np.abs(want).max()
 
 
 @pytest.mark.parametrize("zones,zsets,dset,layout", [
