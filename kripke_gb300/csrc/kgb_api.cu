@@ -596,12 +596,13 @@ int planTensorMomentsFrom(kgb_ctx *ctx, const std::vector<double> &lt_src, const
     *lt_kpad = kc;
     *lt_ok = true;
   }
-  // LPlusTimes: B[m][d] = ell_plus(d,m), K = M (one chunk), N = D in blocks of NB
+  // LPlusTimes: B[m][d] = ell_plus(d,m), K = M (one chunk), N = D in blocks of NB = 32;
+  // the B image and two A stages must fit the 227 KB of shared memory
   if (M <= 32) {
-    const int NB = f64 ? 64 : 128;
+    const int NB = 32;
     const int nhalf = (D + NB - 1) / NB;
-    const size_t smem = (size_t)nhalf * 32 * S * NB * 2 + (size_t)S * 32 * 128 * 2 + 2048 + 4 * nhalf * NB;
-    if (smem <= 227 * 1024) {
+    const size_t smem = 1024 + (size_t)nhalf * 32 * S * NB * 2 + 2 * (size_t)S * 32 * 128 * 2 + 4 * nhalf * NB;
+    if (smem + 4096 <= 227 * 1024) {  // + the kernel's static shared memory
       std::vector<double> bt((size_t)M * D);
       for (int d = 0; d < D; ++d)
         for (int m = 0; m < M; ++m) bt[(size_t)m * D + d] = lp_src[(size_t)d * M + m];
@@ -627,7 +628,7 @@ int planTensorMoments(kgb_ctx *ctx) {
 template <typename T>
 int planTensorScatter(kgb_ctx *ctx) {
   ctx->tc_sc = false;
-  const int G = ctx->G, L1 = ctx->L + 1, S = sizeof(T) == 8 ? 8 : 4, NB = 64;
+  const int G = ctx->G, L1 = ctx->L + 1, S = sizeof(T) == 8 ? 8 : 4, NB = 32;
   if (!ctx->allow_tc_sc || G > 64) return KGB_OK;
   // zone lists from the device mixing tables
   std::vector<int> zs(ctx->Z), zc(ctx->Z), mm(std::max<int64_t>(ctx->nmix, 1));
@@ -658,8 +659,8 @@ int planTensorScatter(kgb_ctx *ctx) {
   if ((rc = dmalloc(ctx, &ctx->pure_z, lists.size()))) return rc;
   ctx->mixed_z = ctx->pure_z + ctx->pure_off[3];
   CK(cudaMemcpyAsync(ctx->pure_z, lists.data(), lists.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-  // digit images: forward B[k][n] = S(n <- k), adjoint B[k][n] = S(k <- n)
-  const int kpad = (G + 31) / 32 * 32;
+  // digit images (N blocks of 32 columns): forward B[k][n] = S(n <- k), adjoint B[k][n] = S(k <- n)
+  const int kpad = (G + 31) / 32 * 32, nbk = (G + 31) / 32;
   std::vector<double> b((size_t)G * G);
   std::vector<uint16_t> img, all;
   std::vector<int> ex, allex;
@@ -671,7 +672,7 @@ int planTensorScatter(kgb_ctx *ctx) {
         const double *sm = ctx->sigs_h.data() + ((size_t)m * L1 + l) * G * G;
         for (int k = 0; k < G; ++k)
           for (int n = 0; n < G; ++n) b[(size_t)k * G + n] = adj ? sm[(size_t)k * G + n] : sm[(size_t)n * G + k];
-        tc_build_b<T>(b.data(), G, G, kpad, S, NB, 1, img, ex);
+        tc_build_b<T>(b.data(), G, G, kpad, S, NB, nbk, img, ex);
         all.insert(all.end(), img.begin(), img.end());
         allex.insert(allex.end(), ex.begin(), ex.end());
       }
@@ -1113,9 +1114,10 @@ int scatterTensor(kgb_ctx *ctx, bool acc) {
       a.K = G;
       a.kpad = kpad;
       a.N = G;
-      a.nhalf = 1;
-      a.bimg = ctx->tc_sc_img + ((size_t)m * L1 + l) * kpad * S * 64;
-      a.bexp = ctx->tc_sc_exp + ((size_t)m * L1 + l) * 64;
+      const int nbk = (G + 31) / 32;  // N blocks of 32 columns
+      a.nhalf = nbk;
+      a.bimg = ctx->tc_sc_img + ((size_t)m * L1 + l) * nbk * kpad * S * 32;
+      a.bexp = ctx->tc_sc_exp + ((size_t)m * L1 + l) * nbk * 32;
       a.err = ctx->err_d;
       a.accumulate = acc;
       a.nsm = ctx->nsm;

@@ -99,10 +99,29 @@ __device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&v)[8]) {
                : "r"(taddr));
 }
 
-// bf16 bit pattern of sign * d for an integer 0 <= d < 128 (exact)
-__device__ __forceinline__ uint32_t digitBf16(uint32_t d, uint32_t sign) {
-  const float f = __uint_as_float(0x4B000000u | d) - 8388608.0f;
-  return (__float_as_uint(f) >> 16) | (sign << 15);
+// The S 7-bit digits (most significant first) of two 7S-bit magnitudes as bf16
+// pairs: element 0 in the low half, element 1 in the high half, each with its
+// sign.  The magnitudes are cut into 28-bit words so every digit comes from
+// one 32-bit shift-and-mask; a digit d < 128 becomes the float d through the
+// 2^23 offset trick and two of them pack into bf16x2 exactly.
+template <int S>
+__device__ __forceinline__ void digitPairs(uint64_t f0, uint32_t s0, uint64_t f1, uint32_t s1, uint32_t (&w)[S][4],
+                                           int col) {
+  static_assert(S == 4 || S == 8, "7S-bit magnitudes of 28 or 56 bits");
+  const uint32_t sg = (s0 << 15) | (s1 << 31);
+  uint32_t a[2], b[2];  // [0]: digits 0..3, [1]: digits 4..7
+  a[0] = (uint32_t)(f0 >> (S == 8 ? 28 : 0)) & 0x0FFFFFFFu;
+  b[0] = (uint32_t)(f1 >> (S == 8 ? 28 : 0)) & 0x0FFFFFFFu;
+  a[1] = (uint32_t)f0 & 0x0FFFFFFFu;
+  b[1] = (uint32_t)f1 & 0x0FFFFFFFu;
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    const int wd = i >> 2, sh = 7 * (3 - (i & 3));
+    const float v0 = __uint_as_float(0x4B000000u | ((a[wd] >> sh) & 127u)) - 8388608.0f;
+    const float v1 = __uint_as_float(0x4B000000u | ((b[wd] >> sh) & 127u)) - 8388608.0f;
+    const __nv_bfloat162 p = __floats2bfloat162_rn(v0, v1);
+    w[i][col] = *reinterpret_cast<const uint32_t *>(&p) | sg;
+  }
 }
 
 // Biased exponent (subnormals count as 1) and significand with the implicit bit.
@@ -303,16 +322,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
     emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 16));
     if (part == 0) row_emax[srow] = emax;
 
-    for (int c = 0; c < nchunks && ok; ++c, ++item) {
-      const int b = MULTI_N ? 0 : (int)(item & 1);
-      if (!MULTI_N && item >= 2) {  // the MMAs that last read this buffer must be done
-        ok = __syncthreads_and(waitParity(&bars[b], (uses[b] - 1) & 1) && ok);
-        if (!ok) break;
-      }
-      unsigned char *buf = sA + b * kBufBytes;
-      // this thread's 8 elements of the chunk, split into S digit slices
+    // this thread's 8 elements of chunk c (zero beyond K or the last row)
+    auto loadChunk = [&](int c, T (&x)[8]) {
       const int k0 = c * kTcChunk + part * 8;
-      T x[8];
       if (valid && vec && k0 + 8 <= a.K) {
         if constexpr (sizeof(T) == 8) {
 #pragma unroll
@@ -335,18 +347,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
 #pragma unroll
         for (int e = 0; e < 8; ++e) x[e] = (valid && k0 + e < a.K) ? arow[(k0 + e) * kstride] : T(0);
       }
+    };
+    T xn[8];
+    loadChunk(0, xn);
+
+    for (int c = 0; c < nchunks && ok; ++c, ++item) {
+      const int b = MULTI_N ? 0 : (int)(item & 1);
+      if (!MULTI_N && item >= 2) {  // the MMAs that last read this buffer must be done
+        ok = __syncthreads_and(waitParity(&bars[b], (uses[b] - 1) & 1) && ok);
+        if (!ok) break;
+      }
+      unsigned char *buf = sA + b * kBufBytes;
+      // this thread's 8 elements of the chunk (loaded one chunk ahead), split into S digit slices
+      T x[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) x[e] = xn[e];
+      if (c + 1 < nchunks) loadChunk(c + 1, xn);
       uint32_t w[S][4];
 #pragma unroll
       for (int e = 0; e < 8; e += 2) {
         uint32_t s0, s1;
         const uint64_t f0 = Fixed<T, S>::mag(x[e], emax, s0);
         const uint64_t f1 = Fixed<T, S>::mag(x[e + 1], emax, s1);
-#pragma unroll
-        for (int i = 0; i < S; ++i) {
-          const uint32_t g0 = (uint32_t)(f0 >> (7 * (S - 1 - i))) & 127u;
-          const uint32_t g1 = (uint32_t)(f1 >> (7 * (S - 1 - i))) & 127u;
-          w[i][e >> 1] = digitBf16(g0, s0) | (digitBf16(g1, s1) << 16);
-        }
+        digitPairs<S>(f0, s0, f1, s1, w, e >> 1);
       }
       const uint32_t off = part * kLboA + (srow >> 3) * 128 + (srow & 7) * 16;
 #pragma unroll
@@ -453,6 +476,314 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
+// ---------------------------------------------------------------------------
+// Pipelined row products (the production kernel).
+//
+// Work items are (128-row tile, 32-column N block) pairs.  Warps 0..15 are
+// workers: they split the A rows of a tile into digit slices (one 32-element K
+// chunk per shared-memory stage, two stages) and, one tile later, drain the
+// finished items from tensor memory (read, combine, store).  Warp 16 issues
+// the MMAs.  Tensor memory holds two accumulators (2 x S x 32 columns), so the
+// epilogue of one item overlaps the MMAs of the next, and the split of tile
+// t+1 overlaps both.  Hand-offs are mbarriers: full[r] (16 worker-warp
+// arrivals: stage r holds a chunk), empty[r] (MMA commit: stage r is free),
+// accfull[s] (MMA commit: accumulator s is complete), accempty[s] (16
+// worker-warp arrivals: accumulator s was read), emaxok[t % 4] (16 worker-warp
+// arrivals: the tile's row exponents are in shared memory).  Every wait is
+// bounded; a wait that gives up records the failure and every role stops.
+// ---------------------------------------------------------------------------
+constexpr int kPipeWorkers = 16;                       // worker warps
+constexpr int kPipeThreads = (kPipeWorkers + 1) * 32;  // + the MMA warp
+constexpr int kPipeNB = 32;                            // columns per N block
+
+__device__ __forceinline__ bool waitParityAbort(uint64_t *bar, uint32_t parity, volatile int *abort) {
+  uint32_t done = 0;
+  for (uint32_t it = 0; it < kWaitLimit && !done; ++it) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(smemAddr(bar)), "r"(parity));
+    if (!done && (it & 255u) == 255u && *abort) return false;
+  }
+  if (!done) *abort = 1;
+  return done != 0;
+}
+
+__device__ __forceinline__ void arriveBar(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(bar)) : "memory");
+}
+
+template <typename T, int S, bool GATHER>
+__global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T> a) {
+  constexpr int NB = kPipeNB;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ uint64_t full[2], empty[2], accfull[2], accempty[2], emaxok[4], bload, drain;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int row_emax[4][kTcRows];
+  __shared__ int abort_flag;
+  volatile int *abort = &abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool worker = warp < kPipeWorkers;
+  const int srow = warp * 8 + (lane & 7), part = lane >> 3;   // split mapping
+  const int erow = (warp & 3) * 32 + lane, cgrp = warp >> 2;  // epilogue: TMEM lane quarter, 8 columns
+  constexpr uint32_t kSliceBytes = kTcChunk * kTcRows * 2;
+  constexpr uint32_t kBufBytes = S * kSliceBytes;
+  constexpr uint32_t kLboA = (kTcRows / 8) * 128;
+  constexpr uint32_t kAccCols = S * NB;             // one accumulator
+  constexpr uint32_t kTmemCols = 2 * kAccCols;      // 512 (FP64) or 256 (mixed)
+  const uint32_t lboB = (uint32_t)S * NB * 16;
+  const uint32_t blkBytes = (uint32_t)a.kpad * S * NB * 2;  // B image of one N block
+  const int nchunks = a.kpad / kTcChunk;
+  const int nb = a.nhalf;
+
+  const uint32_t base = smemAddr(smem_raw);
+  unsigned char *al = smem_raw + (((base + 1023u) & ~1023u) - base);
+  unsigned char *sB = al;
+  unsigned char *sA = al + ((blkBytes * nb + 1023u) & ~1023u);
+  int *sT = reinterpret_cast<int *>(sA + 2 * kBufBytes);
+
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(&full[i])), "r"(kPipeWorkers));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(&empty[i])), "r"(1));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(&accfull[i])), "r"(1));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(&accempty[i])), "r"(kPipeWorkers));
+    }
+    for (int i = 0; i < 4; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(&emaxok[i])), "r"(kPipeWorkers));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(&bload)), "r"(1));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(&drain)), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    abort_flag = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(&tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  for (int i = tid; i < nb * NB; i += kPipeThreads) sT[i] = a.bexp[i];
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_slot;
+  if (tid == 0) {
+    const uint32_t bbytes = blkBytes * nb;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(&bload)), "r"(bbytes));
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smemAddr(sB)),
+                 "l"(a.bimg), "r"(bbytes), "r"(smemAddr(&bload)));
+  }
+  waitParityAbort(&bload, 0, abort);
+
+  const int ntiles = (int)((a.rows + kTcRows - 1) / kTcRows);
+  const bool vec = !GATHER && (a.lda * sizeof(T)) % 16 == 0;
+  const int64_t kstride = GATHER ? a.ks : 1;
+  auto rowBase = [&](int64_t r) -> int64_t {
+    if constexpr (GATHER) {
+      const int64_t q = r / a.nm;
+      return (int64_t)a.zl[q] * a.zstride + a.m0 + (r - q * a.nm);
+    } else {
+      return r * a.lda;
+    }
+  };
+
+  if (worker) {
+    // ---------------- workers: split tile t, then drain tile t-1 ----------------
+    // waits and the abort test are made warp-uniform: the warp-wide shuffles,
+    // __syncwarp and tcgen05.ld below need every lane on the same path
+    auto wwait = [&](uint64_t *bar, uint32_t parity) -> bool {
+      return __all_sync(0xffffffffu, waitParityAbort(bar, parity, abort));
+    };
+    auto aborted = [&]() -> bool { return __any_sync(0xffffffffu, *abort != 0); };
+    auto epilogue = [&](int lt, int tile) {
+      const int64_t orow = (int64_t)tile * kTcRows + erow;
+      const bool ovalid = orow < a.rows;
+      T *crow = a.C + (ovalid ? (GATHER ? rowBase(orow) : orow * a.ldc) : 0);
+      if (!wwait(&emaxok[lt & 3], (uint32_t)(lt >> 2) & 1u)) return;
+      const int oemax = row_emax[lt & 3][erow] - TcBias<T>::v;
+      for (int j = 0; j < nb; ++j) {
+        const int p = lt * nb + j, st = p & 1;
+        if (!wwait(&accfull[st], (uint32_t)(p >> 1) & 1u)) return;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t lanebase = (uint32_t)((warp & 3) * 32) << 16;
+        uint32_t v[S][8];
+#pragma unroll
+        for (int k = 0; k < S; ++k) ld8(tmem + lanebase + (uint32_t)(st * kAccCols + k * NB + cgrp * 8), v[k]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncwarp();
+        if (lane == 0) arriveBar(&accempty[st]);  // the accumulator is in registers: release it
+        if (ovalid) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int n = j * NB + cgrp * 8 + u;
+            if (n < a.N) {
+              float dk[S];
+#pragma unroll
+              for (int k = 0; k < S; ++k) dk[k] = __uint_as_float(v[k][u]);
+              const T out = Combine<T, S>::value(dk, oemax + sT[n]);
+              T &dst = crow[(int64_t)n * kstride];
+              dst = a.accumulate ? dst + out : out;
+            }
+          }
+        }
+      }
+    };
+
+    int lt = 0, prev_tile = -1;
+    for (int tile = blockIdx.x; tile < ntiles && !aborted(); tile += gridDim.x, ++lt) {
+      const int64_t row = (int64_t)tile * kTcRows + srow;
+      const bool valid = row < a.rows;
+      const T *arow = a.A + (valid ? rowBase(row) : 0);
+      int emax = 1;
+      if (valid) {
+        if (vec && a.K == a.kpad) {
+#pragma unroll 4
+          for (int c = 0; c < nchunks; ++c) {
+            const T *p8 = arow + c * kTcChunk + part * 8;
+            if constexpr (sizeof(T) == 8) {
+              double2 v[4];
+#pragma unroll
+              for (int e = 0; e < 4; ++e) v[e] = *reinterpret_cast<const double2 *>(p8 + 2 * e);
+#pragma unroll
+              for (int e = 0; e < 4; ++e) emax = max(emax, max(expOf(v[e].x), expOf(v[e].y)));
+            } else {
+              float4 v[2];
+#pragma unroll
+              for (int e = 0; e < 2; ++e) v[e] = *reinterpret_cast<const float4 *>(p8 + 4 * e);
+#pragma unroll
+              for (int e = 0; e < 2; ++e)
+                emax = max(emax, max(max(expOf(v[e].x), expOf(v[e].y)), max(expOf(v[e].z), expOf(v[e].w))));
+            }
+          }
+        } else {
+          for (int c = 0; c < nchunks; ++c) {
+            const int k0 = c * kTcChunk + part * 8;
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+              if (k0 + e < a.K) emax = max(emax, expOf(arow[(k0 + e) * kstride]));
+          }
+        }
+      }
+      emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 8));
+      emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 16));
+      if (part == 0) row_emax[lt & 3][srow] = emax;
+      __syncwarp();
+      if (lane == 0) arriveBar(&emaxok[lt & 3]);
+
+      auto loadChunk = [&](int c, T (&x)[8]) {
+        const int k0 = c * kTcChunk + part * 8;
+        if (valid && vec && k0 + 8 <= a.K) {
+          if constexpr (sizeof(T) == 8) {
+#pragma unroll
+            for (int e = 0; e < 8; e += 2) {
+              const double2 v = *reinterpret_cast<const double2 *>(arow + k0 + e);
+              x[e] = v.x;
+              x[e + 1] = v.y;
+            }
+          } else {
+#pragma unroll
+            for (int e = 0; e < 8; e += 4) {
+              const float4 v = *reinterpret_cast<const float4 *>(arow + k0 + e);
+              x[e] = v.x;
+              x[e + 1] = v.y;
+              x[e + 2] = v.z;
+              x[e + 3] = v.w;
+            }
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < 8; ++e) x[e] = (valid && k0 + e < a.K) ? arow[(k0 + e) * kstride] : T(0);
+        }
+      };
+      T xn[8];
+      loadChunk(0, xn);
+      for (int c = 0; c < nchunks; ++c) {
+        const int q = lt * nchunks + c, r = q & 1;
+        T x[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) x[e] = xn[e];
+        if (c + 1 < nchunks) loadChunk(c + 1, xn);
+        uint32_t w[S][4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          uint32_t s0, s1;
+          const uint64_t f0 = Fixed<T, S>::mag(x[e], emax, s0);
+          const uint64_t f1 = Fixed<T, S>::mag(x[e + 1], emax, s1);
+          digitPairs<S>(f0, s0, f1, s1, w, e >> 1);
+        }
+        // the MMAs that last read stage r must be done before it is overwritten
+        if (q >= 2 && !wwait(&empty[r], (uint32_t)((q >> 1) - 1) & 1u)) break;
+        unsigned char *buf = sA + r * kBufBytes;
+        const uint32_t off = part * kLboA + (srow >> 3) * 128 + (srow & 7) * 16;
+#pragma unroll
+        for (int i = 0; i < S; ++i)
+          *reinterpret_cast<uint4 *>(buf + i * kSliceBytes + off) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+        asm volatile("fence.proxy.async.shared::cta;");
+        __syncwarp();
+        if (lane == 0) arriveBar(&full[r]);
+      }
+      if (prev_tile >= 0) epilogue(lt - 1, prev_tile);
+      prev_tile = tile;
+    }
+    if (prev_tile >= 0 && !aborted()) epilogue(lt - 1, prev_tile);
+  } else if (lane == 0) {
+    // ---------------- MMA issuer ----------------
+    int p = 0, lt = 0;
+    for (int tile = blockIdx.x; tile < ntiles && !*abort; tile += gridDim.x, ++lt) {
+      for (int j = 0; j < nb && !*abort; ++j, ++p) {
+        const int st = p & 1;
+        if (p >= 2 && !waitParityAbort(&accempty[st], (uint32_t)((p >> 1) - 1) & 1u, abort)) break;
+        for (int c = 0; c < nchunks; ++c) {
+          const int q = lt * nchunks + c, r = q & 1;
+          if (j == 0 && !waitParityAbort(&full[r], (uint32_t)(q >> 1) & 1u, abort)) break;
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const unsigned char *buf = sA + r * kBufBytes;
+#pragma unroll 1
+          for (int i = 1; i <= S; ++i) {
+            const int ncols = NB * (S + 1 - i);
+#pragma unroll 1
+            for (int ks = 0; ks < kTcChunk / 16; ++ks) {
+              const int kg = c * (kTcChunk / 16) + ks;
+              const uint64_t da = matDesc(smemAddr(buf + (i - 1) * kSliceBytes + ks * 2 * kLboA), kLboA, 128);
+              const uint64_t db = matDesc(smemAddr(sB) + j * blkBytes + kg * 2 * lboB, lboB, 128);
+              mma(tmem + (uint32_t)(st * kAccCols + (i - 1) * NB), da, db, instrDesc(ncols),
+                  (c > 0 || ks > 0 || i > 1) ? 1u : 0u);
+            }
+          }
+          if (j == nb - 1) commit(&empty[r]);  // the stage's last reader
+        }
+        if (*abort) break;
+        commit(&accfull[st]);
+      }
+    }
+    // drain: every MMA issued (also on a failed run) must finish before tensor memory is released
+    commit(&drain);
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < kWaitLimit && !done; ++it)
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+          : "=r"(done)
+          : "r"(smemAddr(&drain)));
+    if (!done) *abort = 1;
+  }
+  if (*abort && tid == 0) atomicExch(a.err, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+
+template <typename T, int S, bool GATHER>
+void launchPipe(const TcArgs<T> &a, cudaStream_t s) {
+  const size_t blkBytes = (size_t)a.kpad * S * kPipeNB * 2;
+  const size_t bufBytes = (size_t)S * kTcChunk * kTcRows * 2;
+  const size_t smem = 1024 + ((blkBytes * a.nhalf + 1023) & ~(size_t)1023) + 2 * bufBytes + sizeof(int) * a.nhalf * kPipeNB;
+  cudaFuncSetAttribute(tc_pipe_kernel<T, S, GATHER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int64_t ntiles = (a.rows + kTcRows - 1) / kTcRows;
+  const int grid = (int)(ntiles < a.nsm ? ntiles : a.nsm);
+  tc_pipe_kernel<T, S, GATHER><<<grid, kPipeThreads, smem, s>>>(a);
+}
+
 template <typename T, int S, int NB, bool MULTI_N, bool GATHER = false>
 void launchRows(const TcArgs<T> &a, cudaStream_t s) {
   const size_t halfBytes = (size_t)a.kpad * S * NB * 2;
@@ -517,23 +848,20 @@ void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhal
 
 template <typename T>
 void launch_tc_rows(const TcArgs<T> &a, int S, int NB, bool multi_n, cudaStream_t s) {
-  if constexpr (sizeof(T) == 8) {
-    if (!multi_n) launchRows<T, 8, 32, false>(a, s);
-    else launchRows<T, 8, 64, true>(a, s);
-  } else {
-    if (!multi_n) launchRows<T, 4, 32, false>(a, s);
-    else launchRows<T, 4, 128, true>(a, s);
-  }
+  // the pipelined kernel covers both shapes (N blocks of 32 columns)
+  if constexpr (sizeof(T) == 8) launchPipe<T, 8, false>(a, s);
+  else launchPipe<T, 4, false>(a, s);
   (void)S;
   (void)NB;
+  (void)multi_n;
 }
 
 // Scattering of pure zones on the tensor cores: K = N = groups (<= 64), rows
 // gathered as (zone, moment) pairs, B = the material's order-l matrix transposed.
 template <typename T>
 void launch_tc_gather(const TcArgs<T> &a, cudaStream_t s) {
-  if constexpr (sizeof(T) == 8) launchRows<T, 8, 64, false, true>(a, s);
-  else launchRows<T, 4, 64, false, true>(a, s);
+  if constexpr (sizeof(T) == 8) launchPipe<T, 8, true>(a, s);
+  else launchPipe<T, 4, true>(a, s);
 }
 
 template void tc_build_b<double>(const double *, int, int, int, int, int, int, std::vector<uint16_t> &, std::vector<int> &);
