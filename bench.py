@@ -210,6 +210,14 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def progress(msg):
+    """One line on stderr per section, so a slow section can be told from a stuck one."""
+    print("[bench %.1fs] %s" % (time.perf_counter() - T0, msg), file=sys.stderr, flush=True)
+
+
+T0 = time.perf_counter()
+
+
 def timed_steps(ctx, stream, steps):
     """K source iterations between CUDA events on the stream the kernels run on; ms per iteration."""
     import torch
@@ -345,7 +353,9 @@ def batch_report(local, problems=BATCH_PROBLEMS, niter=10):
         b = abi.Batch(device=local, precision=prec)
         for x in inputs:
             b.add(x)
+        progress("batch %s: autotune" % name)
         tune = b.autotune()
+        progress("batch %s: solves" % name)
         b.solve(niter)  # captures the solve graph
         l0 = b.launch_count()
         t0 = time.perf_counter()
@@ -353,6 +363,7 @@ def batch_report(local, problems=BATCH_PROBLEMS, niter=10):
         t_batch = (time.perf_counter() - t0) / niter
         kernels = (b.launch_count() - l0) // niter
         phases = b.profile()
+        progress("batch %s: one by one" % name)
         t0 = time.perf_counter()
         for i in range(len(b)):
             b.context(i).solve(niter)
@@ -492,10 +503,13 @@ def run_gpu(args, world, rank, local):
         "population_after_timed_steps": part,
     }
     if rank == 0 and world == 1 and precision == abi.FP64 and not args.no_mixed:
+        progress("mixed form")
         line["mixed"] = mixed_report(args, local, w, ctx, ms)
     if rank == 0 and world == 1 and not args.no_adjoint:
+        progress("adjoint")
         line["adjoint"] = adjoint_report(local)
     if rank == 0 and world == 1 and not args.no_batch:
+        progress("batch")
         line["batch"] = batch_report(local, args.batch_problems)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

@@ -163,9 +163,11 @@ int kgb_balance(kgb_ctx *ctx, double out[5]);
  * particle count after iteration i (may be NULL).  source_strength is the
  * reference's 1.0 unless a caller scales the source. */
 int kgb_solve(kgb_ctx *ctx, int32_t niter, double source_strength, double *part);
-/* One source iteration on the current psi (no psi reset).  The particle
- * count is always computed on the device; it is copied to *part (and the
- * call waits) only when part is not NULL. */
+/* One source iteration on the current psi (no psi reset).  With part, the
+ * particle count of the new psi is returned (and the call waits); without
+ * it, a count is still formed on the device (one per iteration, as
+ * SteadyStateSolver does): in FP64 that of the psi the iteration started from,
+ * from the iteration's own moments; in the mixed form that of the new psi. */
 int kgb_iterate(kgb_ctx *ctx, double source_strength, double *part);
 /* Blocks until the context's stream is idle. */
 int kgb_sync(kgb_ctx *ctx);

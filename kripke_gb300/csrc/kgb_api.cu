@@ -152,12 +152,14 @@ struct kgb_ctx {
   uint16_t *tc_lt_img = nullptr, *tc_lp_img = nullptr;
   int *tc_lt_exp = nullptr, *tc_lp_exp = nullptr;
   int tc_lt_kpad = 0, tc_lp_nhalf = 0;
+  int tc_lp_stages = 2;
   int *err_d = nullptr;                     // set by kernels whose bounded waits gave up
   int nsm = 0;
   // fused population partials, one per (tile, subdomain, chain block)
   double *pop_slots = nullptr;
   int64_t npop_slots = 0;
   double vol_uniform = 0.0;
+  double pop_scale = 0.0;  // w(d) / ell(0,d) when L's moment-0 row is proportional to w, else 0
 
   // converged solves, the adjoint source iteration and gradients (adjoint.cu)
   void *lam = nullptr;          // adjoint state divided by the cell volume, device nesting [Z][G][D]
@@ -601,8 +603,11 @@ int planTensorMomentsFrom(kgb_ctx *ctx, const std::vector<double> &lt_src, const
   if (M <= 32) {
     const int NB = 32;
     const int nhalf = (D + NB - 1) / NB;
-    const size_t smem = 1024 + (size_t)nhalf * 32 * S * NB * 2 + 2 * (size_t)S * 32 * 128 * 2 + 4 * nhalf * NB;
-    if (smem + 4096 <= 227 * 1024) {  // + the kernel's static shared memory
+    const size_t stage = (size_t)S * 32 * 128 * 2;
+    const size_t smem1 = 1024 + (size_t)nhalf * 32 * S * NB * 2 + stage + 4 * nhalf * NB;
+    // + the kernel's static shared memory; a second A stage when it fits (overlap across tiles)
+    ctx->tc_lp_stages = smem1 + stage + 4096 <= 227 * 1024 ? 2 : 1;
+    if (smem1 + 4096 <= 227 * 1024) {
       std::vector<double> bt((size_t)M * D);
       for (int d = 0; d < D; ++d)
         for (int m = 0; m < M; ++m) bt[(size_t)m * D + d] = lp_src[(size_t)d * M + m];
@@ -692,9 +697,23 @@ int planTensorScatter(kgb_ctx *ctx) {
   return KGB_OK;
 }
 
+// w(d) / ell(0,d) when it is the same for every direction (Kripke's L: ell(0,d) =
+// w(d) Y_00 / sqrt(4 pi)), else 0: the particle count then comes from psi.
+void updatePopScale(kgb_ctx *ctx) {
+  const std::vector<double> &w = ctx->q[3];
+  const double e0 = ctx->ell_h[0];
+  double s = e0 != 0.0 ? w[0] / e0 : 0.0;
+  for (int d = 0; d < ctx->D && s != 0.0; ++d) {
+    const double e = ctx->ell_h[(size_t)d * ctx->M];
+    if (!(std::fabs(w[d] - s * e) <= 1e-14 * std::fabs(w[d]))) s = 0.0;
+  }
+  ctx->pop_scale = s;
+}
+
 template <typename T>
 int prepareT(kgb_ctx *ctx) {
   int rc;
+  const bool popscale_stale = ctx->dirty_quad || ctx->dirty_ell;
   if (ctx->dirty_quad) {
     if ((rc = need(ctx, {"quadrature/xcos", "quadrature/ycos", "quadrature/zcos", "quadrature/w", "quadrature/id",
                          "quadrature/jd", "quadrature/kd"})))
@@ -859,6 +878,7 @@ int prepareT(kgb_ctx *ctx) {
     ctx->dirty_tcsc = true;
     ++ctx->gen;
   }
+  if (popscale_stale) updatePopScale(ctx);
   if (ctx->dirty_tcsc) {
     if ((rc = planTensorScatter<T>(ctx))) return rc;
     ctx->dirty_tcsc = false;
@@ -1048,6 +1068,7 @@ void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, i
   a.err = ctx->err_d;
   a.accumulate = acc;
   a.nsm = ctx->nsm;
+  a.stages = multi_n ? ctx->tc_lp_stages : 2;
   launch_tc_rows<T>(a, sizeof(T) == 8 ? 8 : 4, 0, multi_n, ctx->stream);
 }
 
@@ -1126,6 +1147,7 @@ int scatterTensor(kgb_ctx *ctx, bool acc) {
       a.m0 = l * l;
       a.ks = ctx->M;
       a.zstride = (int64_t)G * ctx->M;
+      a.stages = 2;  // both K chunks of a tile stay resident across its N blocks
       launch_tc_gather<T>(a, ctx->stream);
       CKN(1);
     }
@@ -1187,9 +1209,28 @@ int checkDeviceError(kgb_ctx *ctx) {
   return KGB_OK;
 }
 
-int iterateDevice(kgb_ctx *ctx, double q, double *part_slot) {
+// One source iteration.  part_slot: particle count of the new psi, fused into
+// the sweep.  prev_slot: particle count of the psi the iteration starts from,
+// taken from this iteration's own moments (one small pass over moment 0) --
+// a solve counts every iterate that way and the last one after its loop.
+int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot = nullptr) {
   int rc;
   if ((rc = doLTimes(ctx, false))) return rc;          // phi = L psi        (kConst + LTimes)
+  if (prev_slot) {
+    FamScope fs(ctx, "population");
+    const int64_t rows = ctx->Z * ctx->G;
+    if (ctx->pop_scale != 0.0) {
+      if (ctx->prec == KGB_FP64)
+        launch_population_moments<double>(as<double>(ctx->phi), ctx->M, ctx->vol_d, rows, ctx->G, ctx->pop_scale,
+                                          ctx->partials, ctx->npart, prev_slot, ctx->stream);
+      else
+        launch_population_moments<float>(as<float>(ctx->phi), ctx->M, ctx->vol_d, rows, ctx->G, ctx->pop_scale,
+                                         ctx->partials, ctx->npart, prev_slot, ctx->stream);
+      CKN(2);
+    } else if ((rc = doPopulation(ctx, prev_slot))) {
+      return rc;
+    }
+  }
   if ((rc = doScattering(ctx, false))) return rc;      // phi_out = S phi    (kConst + scattering)
   if ((rc = doSource(ctx, q))) return rc;              // phi_out += Q
   if ((rc = doLPlusTimes(ctx, false))) return rc;      // rhs = L+ phi_out   (kConst + LPlusTimes)
@@ -1473,6 +1514,25 @@ struct PsiBuffers {
 }  // namespace
 
 namespace {
+// The particle count from the next iteration's moments saves the FP64 sweep
+// its per-cell accumulation; FP32 moments would round the count, so the mixed
+// form keeps the compensated sum fused into its (latency-bound) sweep.
+bool lagPopulation(const kgb_ctx *ctx) { return ctx->prec == KGB_FP64 && ctx->pop_scale != 0.0; }
+
+// niter iterations from the current psi with their particle counts.
+int solveIterations(kgb_ctx *ctx, int niter, double q) {
+  int rc;
+  if (!lagPopulation(ctx)) {
+    for (int it = 0; it < niter; ++it)
+      if ((rc = iterateDevice(ctx, q, ctx->parts_dev + it))) return rc;
+    return KGB_OK;
+  }
+  // the count after iteration it-1 from iteration it's moments, the last one from psi
+  for (int it = 0; it < niter; ++it)
+    if ((rc = iterateDevice(ctx, q, nullptr, it > 0 ? ctx->parts_dev + it - 1 : nullptr))) return rc;
+  return doPopulation(ctx, ctx->parts_dev + niter - 1);
+}
+
 // The whole solve (psi reset + niter iterations with their particle counts)
 // captured once per (niter, q, stream) and replayed while the context's
 // tables are unchanged.  A capture that fails leaves *out null: the caller
@@ -1507,7 +1567,7 @@ int solveGraph(kgb_ctx *ctx, int niter, double q, const kgb_ctx::SolveGraph **ou
   const std::string err0 = ctx->err;
   int rc = cudaMemsetAsync(ctx->psi, 0, ctx->Z * ctx->G * ctx->D * ctx->tsz, ctx->stream) == cudaSuccess
                ? KGB_OK : KGB_ERR_CUDA;
-  for (int it = 0; it < niter && !rc; ++it) rc = iterateDevice(ctx, q, ctx->parts_dev + it);
+  rc = solveIterations(ctx, niter, q);
   cudaGraph_t g = nullptr;
   const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
   const int64_t captured = ctx->launches - l0;
@@ -2083,7 +2143,11 @@ int kgb_balance(kgb_ctx *ctx, double out[5]) {
 int kgb_iterate(kgb_ctx *ctx, double q, double *part) {
   int rc = prepare(ctx);
   if (rc) return rc;
-  if ((rc = iterateDevice(ctx, q, ctx->results))) return rc;
+  // without part, a count is still formed on the device: of the state the iteration starts
+  // from (FP64, from the moments; results[1]) or of the new state (mixed, fused; results[0])
+  if ((rc = (part || !lagPopulation(ctx)) ? iterateDevice(ctx, q, ctx->results)
+                                          : iterateDevice(ctx, q, nullptr, ctx->results + 1)))
+    return rc;
   if (part) {
     CK(cudaMemcpyAsync(part, ctx->results, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -2116,8 +2180,7 @@ int kgb_solve(kgb_ctx *ctx, int32_t niter, double q, double *part) {
   }
   if (!ctx->graph_active) {
     CK(cudaMemsetAsync(ctx->psi, 0, ctx->Z * ctx->G * ctx->D * ctx->tsz, ctx->stream));  // kConst(psi, 0)
-    for (int it = 0; it < niter; ++it)
-      if ((rc = iterateDevice(ctx, q, ctx->parts_dev + it))) return rc;
+    if ((rc = solveIterations(ctx, niter, q))) return rc;
   }
   if (part) CK(cudaMemcpyAsync(part, ctx->parts_dev, niter * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));

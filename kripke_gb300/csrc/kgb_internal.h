@@ -104,6 +104,7 @@ struct TcArgs {
   const int *zl;
   int nm, m0, ks;
   int64_t zstride;
+  int stages;            // A stages in shared memory: 2 (default, 0) or 1 (one K chunk per tile only)
 };
 template <typename T>
 void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhalf, std::vector<uint16_t> &img,
@@ -117,6 +118,9 @@ void launch_tc_gather(const TcArgs<T> &a, cudaStream_t s);
 template <typename T>
 void launch_population(const T *psi, const double *w, const double *vol, int64_t rows, int G, int D,
                        double *partials, int nblocks, double *out, cudaStream_t s);
+template <typename T>
+void launch_population_moments(const T *phi, int M, const double *vol, int64_t rows, int G, double scale,
+                               double *partials, int nblocks, double *out, cudaStream_t s);
 template <typename T>
 void launch_balance_terms(const T *psi, const T *rhs, const T *sigt, const double *w, const double *vol,
                           int64_t rows, int G, int D, double *partials, int nblocks, double *out2, cudaStream_t s);

@@ -42,6 +42,21 @@ __global__ void __launch_bounds__(kRedThreads) population_kernel(const T *__rest
   if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
+// The same count from the moments: sum over (z,g) of scale * phi(0,g,z) * vol(z),
+// with scale = w(d) / ell(0,d) (the quadrature's L has ell(0,d) proportional
+// to w(d), so this equals the sum over d of w(d) psi(d,g,z)).
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) moment_population_kernel(const T *__restrict__ phi, int M,
+                                                                       const double *__restrict__ vol, int64_t rows,
+                                                                       int G, double scale,
+                                                                       double *__restrict__ partials) {
+  double acc = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x)
+    acc += (double)phi[r * M] * vol[r / G];
+  const double b = blockSum(acc);
+  if (threadIdx.x == 0) partials[blockIdx.x] = b * scale;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) balance_kernel(const T *__restrict__ psi, const T *__restrict__ rhs,
                                                              const T *__restrict__ sigt, const double *__restrict__ w,
@@ -119,6 +134,13 @@ void launch_population(const T *psi, const double *w, const double *vol, int64_t
 }
 
 template <typename T>
+void launch_population_moments(const T *phi, int M, const double *vol, int64_t rows, int G, double scale,
+                               double *partials, int nblocks, double *out, cudaStream_t s) {
+  moment_population_kernel<T><<<nblocks, kRedThreads, 0, s>>>(phi, M, vol, rows, G, scale, partials);
+  finish_kernel<<<1, kRedThreads, 0, s>>>(partials, nblocks, 1, 0, out, false);
+}
+
+template <typename T>
 void launch_balance_terms(const T *psi, const T *rhs, const T *sigt, const double *w, const double *vol, int64_t rows,
                           int G, int D, double *partials, int nblocks, double *out2, cudaStream_t s) {
   balance_kernel<T><<<nblocks, kRedThreads, 0, s>>>(psi, rhs, sigt, w, vol, rows, G, D, partials);
@@ -143,6 +165,10 @@ void launch_sum_partials(const double *partials, int64_t n, double *out, cudaStr
 
 template void launch_population<double>(const double *, const double *, const double *, int64_t, int, int, double *, int, double *, cudaStream_t);
 template void launch_population<float>(const float *, const double *, const double *, int64_t, int, int, double *, int, double *, cudaStream_t);
+template void launch_population_moments<double>(const double *, int, const double *, int64_t, int, double, double *,
+                                                int, double *, cudaStream_t);
+template void launch_population_moments<float>(const float *, int, const double *, int64_t, int, double, double *,
+                                               int, double *, cudaStream_t);
 template void launch_balance_terms<double>(const double *, const double *, const double *, const double *, const double *, int64_t, int, int, double *, int, double *, cudaStream_t);
 template void launch_balance_terms<float>(const float *, const float *, const float *, const double *, const double *, int64_t, int, int, double *, int, double *, cudaStream_t);
 template void launch_leakage<double>(const double *, int64_t, int, int, int, int, const double *, const double *, const double *, const double *, double *, int, double *, cudaStream_t);

@@ -496,14 +496,30 @@ constexpr int kPipeWorkers = 16;                       // worker warps
 constexpr int kPipeThreads = (kPipeWorkers + 1) * 32;  // + the MMA warp
 constexpr int kPipeNB = 32;                            // columns per N block
 
+__device__ __forceinline__ uint64_t nowNs() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait for the phase of the given parity: gives up (and raises the
+// CTA's abort flag) after kPipeWaitNs, or as soon as another role has.  A
+// legitimate wait lasts about one tile of work (tens of microseconds).
+constexpr uint64_t kPipeWaitNs = 200000000ull;  // 0.2 s
 __device__ __forceinline__ bool waitParityAbort(uint64_t *bar, uint32_t parity, volatile int *abort) {
   uint32_t done = 0;
-  for (uint32_t it = 0; it < kWaitLimit && !done; ++it) {
+  uint64_t t0 = 0;
+  for (uint32_t it = 0; !done; ++it) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
         : "=r"(done)
         : "r"(smemAddr(bar)), "r"(parity));
-    if (!done && (it & 255u) == 255u && *abort) return false;
+    if (!done && (it & 63u) == 63u) {
+      if (*abort) return false;
+      const uint64_t t = nowNs();
+      if (t0 == 0) t0 = t;
+      else if (t - t0 > kPipeWaitNs) break;
+    }
   }
   if (!done) *abort = 1;
   return done != 0;
@@ -535,12 +551,13 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
   const uint32_t blkBytes = (uint32_t)a.kpad * S * NB * 2;  // B image of one N block
   const int nchunks = a.kpad / kTcChunk;
   const int nb = a.nhalf;
+  const int R = a.stages == 1 ? 1 : 2;  // A stages (1 only when a tile has one K chunk)
 
   const uint32_t base = smemAddr(smem_raw);
   unsigned char *al = smem_raw + (((base + 1023u) & ~1023u) - base);
   unsigned char *sB = al;
   unsigned char *sA = al + ((blkBytes * nb + 1023u) & ~1023u);
-  int *sT = reinterpret_cast<int *>(sA + 2 * kBufBytes);
+  int *sT = reinterpret_cast<int *>(sA + R * kBufBytes);
 
   if (tid == 0) {
     for (int i = 0; i < 2; ++i) {
@@ -699,7 +716,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
       T xn[8];
       loadChunk(0, xn);
       for (int c = 0; c < nchunks; ++c) {
-        const int q = lt * nchunks + c, r = q & 1;
+        const int q = lt * nchunks + c, r = q % R;
         T x[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) x[e] = xn[e];
@@ -713,7 +730,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
           digitPairs<S>(f0, s0, f1, s1, w, e >> 1);
         }
         // the MMAs that last read stage r must be done before it is overwritten
-        if (q >= 2 && !wwait(&empty[r], (uint32_t)((q >> 1) - 1) & 1u)) break;
+        if (q >= R && !wwait(&empty[r], (uint32_t)(q / R - 1) & 1u)) break;
         unsigned char *buf = sA + r * kBufBytes;
         const uint32_t off = part * kLboA + (srow >> 3) * 128 + (srow & 7) * 16;
 #pragma unroll
@@ -723,10 +740,18 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
         __syncwarp();
         if (lane == 0) arriveBar(&full[r]);
       }
-      if (prev_tile >= 0) epilogue(lt - 1, prev_tile);
-      prev_tile = tile;
+      // With two stages the tile lags one behind: the next tile's split waits only for
+      // the stage of the tile before this one, whose items are drained here.  With
+      // one stage the next split waits for every item of this tile, which needs its
+      // own accumulators drained first: drain it now.
+      if (R == 1) {
+        epilogue(lt, tile);
+      } else {
+        if (prev_tile >= 0) epilogue(lt - 1, prev_tile);
+        prev_tile = tile;
+      }
     }
-    if (prev_tile >= 0 && !aborted()) epilogue(lt - 1, prev_tile);
+    if (R == 2 && prev_tile >= 0 && !aborted()) epilogue(lt - 1, prev_tile);
   } else if (lane == 0) {
     // ---------------- MMA issuer ----------------
     int p = 0, lt = 0;
@@ -735,8 +760,8 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
         const int st = p & 1;
         if (p >= 2 && !waitParityAbort(&accempty[st], (uint32_t)((p >> 1) - 1) & 1u, abort)) break;
         for (int c = 0; c < nchunks; ++c) {
-          const int q = lt * nchunks + c, r = q & 1;
-          if (j == 0 && !waitParityAbort(&full[r], (uint32_t)(q >> 1) & 1u, abort)) break;
+          const int q = lt * nchunks + c, r = q % R;
+          if (j == 0 && !waitParityAbort(&full[r], (uint32_t)(q / R) & 1u, abort)) break;
           asm volatile("tcgen05.fence::after_thread_sync;");
           const unsigned char *buf = sA + r * kBufBytes;
 #pragma unroll 1
@@ -760,11 +785,14 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
     // drain: every MMA issued (also on a failed run) must finish before tensor memory is released
     commit(&drain);
     uint32_t done = 0;
-    for (uint32_t it = 0; it < kWaitLimit && !done; ++it)
+    const uint64_t t0 = nowNs();
+    for (uint32_t it = 0; !done; ++it) {
       asm volatile(
           "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
           : "=r"(done)
           : "r"(smemAddr(&drain)));
+      if (!done && (it & 63u) == 63u && nowNs() - t0 > kPipeWaitNs) break;
+    }
     if (!done) *abort = 1;
   }
   if (*abort && tid == 0) atomicExch(a.err, 1);
@@ -777,7 +805,8 @@ template <typename T, int S, bool GATHER>
 void launchPipe(const TcArgs<T> &a, cudaStream_t s) {
   const size_t blkBytes = (size_t)a.kpad * S * kPipeNB * 2;
   const size_t bufBytes = (size_t)S * kTcChunk * kTcRows * 2;
-  const size_t smem = 1024 + ((blkBytes * a.nhalf + 1023) & ~(size_t)1023) + 2 * bufBytes + sizeof(int) * a.nhalf * kPipeNB;
+  const size_t smem = 1024 + ((blkBytes * a.nhalf + 1023) & ~(size_t)1023) + (a.stages == 1 ? 1 : 2) * bufBytes +
+                      sizeof(int) * a.nhalf * kPipeNB;
   cudaFuncSetAttribute(tc_pipe_kernel<T, S, GATHER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int64_t ntiles = (a.rows + kTcRows - 1) / kTcRows;
   const int grid = (int)(ntiles < a.nsm ? ntiles : a.nsm);

@@ -1,11 +1,11 @@
 """Batched problems: one launch per kernel family, the sweeps of every problem
 in one persistent launch, a solve replayed from a CUDA graph.
 
-Parity: each problem's particle counts and psi equal, bit for bit, those of
-the same problem's own context run with the batch's sweep tiles (and the SIMT
-moment kernels when the batch runs its batched SIMT moments), since the
-arithmetic is term for term the same; the particle counts match the CPU
-oracle within 1e-12 (FP64).
+Parity: each problem's psi equals, bit for bit, that of the same problem's
+own context run with the batch's sweep tiles (and the SIMT kernels when the
+batch runs its batched SIMT kernels), since the arithmetic is term for term
+the same; the particle counts agree to 1e-13 (the same sums in another order)
+and match the CPU oracle within 1e-12 (FP64).
 """
 import numpy as np
 import pytest
@@ -58,7 +58,9 @@ def test_batch_equals_single_contexts(kgb, prec, own, tiles):
     psis = [b.context(i).download("psi") for i in range(len(b))]
     for i in range(len(b)):
         want, psi = single_run(kgb, b, i, niter)
-        np.testing.assert_array_equal(parts[:, i], want)
+        # a context's solve counts particles from each iteration's moments, the batch from its
+        # fused sweep partials: the same sums in another order
+        np.testing.assert_allclose(parts[:, i], want, rtol=1e-13)
         np.testing.assert_array_equal(psis[i], psi)
 
 
@@ -96,7 +98,7 @@ def test_batch_autotune_then_parity(kgb):
     parts = b.solve(3)
     for i in range(len(b)):
         want, _ = single_run(kgb, b, i, 3)
-        np.testing.assert_array_equal(parts[:, i], want)
+        np.testing.assert_allclose(parts[:, i], want, rtol=1e-13)
 
 
 @pytest.mark.gpu

@@ -100,8 +100,29 @@ def test_moment_transforms_wide_range(oracle, kgb, tensor, precision, quad):
     p.set("phi_out", phi_out); ctx.upload("phi_out", phi_out)
     p.kconst("rhs", 0.0); ctx.fill("rhs", 0.0)
     p.lplustimes(); ctx.lplustimes()
+    assert ctx.get_option("moments_tensor_lplustimes") == tensor
     want, got = p.get("rhs"), ctx.download("rhs")
     assert np.max(np.abs(got - want)) <= tol * np.abs(want).max()
+
+
+@pytest.mark.parametrize("quad", [(8, 16), (8, 24)])
+def test_moment_transforms_many_tiles_per_sm(oracle, kgb, quad):
+    """More 128-row tiles than SMs, so every CTA of the pipelined tensor-core kernel runs several
+    tiles through its stages: 128 directions (two A stages) and 192 (one stage in FP64)."""
+    p, ctx = pair(oracle, kgb, quad=quad, legendre=4, zones=(20, 20, 10), groups=8)
+    ctx.set_option("moments_tensor", 1)
+    rng = np.random.default_rng(13)
+    psi = rng.standard_normal(ctx.field_bytes("psi") // 8)
+    p.set("psi", psi); ctx.upload("psi", psi)
+    p.kconst("phi", 0.0); ctx.fill("phi", 0.0)
+    p.ltimes(); ctx.ltimes()
+    check(ctx.download("phi"), p.get("phi"), 1e-13)
+    phi_out = rng.standard_normal(ctx.field_bytes("phi_out") // 8)
+    p.set("phi_out", phi_out); ctx.upload("phi_out", phi_out)
+    p.kconst("rhs", 0.0); ctx.fill("rhs", 0.0)
+    p.lplustimes(); ctx.lplustimes()
+    assert ctx.get_option("moments_tensor_lplustimes") == 1
+    check(ctx.download("rhs"), p.get("rhs"), 1e-13)
 
 
 @pytest.mark.parametrize("scatter,gset", [(0, 1), (1, 1), (1, 4)])
