@@ -199,6 +199,25 @@ template <> struct Combine<double, 8> {
     return scale2(scale2((double)h, 28) + (double)l, e0 - 63);  // outside the normal range
   }
 };
+// The same for one K chunk (K <= 32): every diagonal sum is below 8*32*127^2 <
+// 2^22, so each converts to an integer by the 1.5 * 2^23 offset (a float add)
+// instead of a conversion instruction, and digit pairs combine in 32 bits.
+struct CombineSmallK {
+  static __device__ __forceinline__ double value(const float (&dk)[8], int e0) {
+    int32_t d[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) d[k] = __float_as_int(dk[k] + 12582912.0f) - 0x4B400000;
+    const int32_t p01 = d[0] * 128 + d[1], p23 = d[2] * 128 + d[3];
+    const int32_t p45 = d[4] * 128 + d[5], p67 = d[6] * 128 + d[7];
+    const long long h = (long long)p01 * 16384 + p23, l = (long long)p45 * 16384 + p67;
+    bool ok = true;
+    const double hs = exactDouble(h, e0 - 35, ok);
+    const double ls = exactDouble(l, e0 - 63, ok);
+    if (ok) return hs + ls;
+    return scale2(scale2((double)h, 28) + (double)l, e0 - 63);
+  }
+};
+
 template <> struct Combine<float, 4> {
   static __device__ __forceinline__ float value(const float (&dk)[4], int e0) {
     long long x = 0;
@@ -552,6 +571,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
   const int nchunks = a.kpad / kTcChunk;
   const int nb = a.nhalf;
   const int R = a.stages == 1 ? 1 : 2;  // A stages (1 only when a tile has one K chunk)
+  const bool smallk = nchunks == 1;     // diagonal sums below 2^22
 
   const uint32_t base = smemAddr(smem_raw);
   unsigned char *al = smem_raw + (((base + 1023u) & ~1023u) - base);
@@ -638,7 +658,12 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
               float dk[S];
 #pragma unroll
               for (int k = 0; k < S; ++k) dk[k] = __uint_as_float(v[k][u]);
-              const T out = Combine<T, S>::value(dk, oemax + sT[n]);
+              T out;
+              if constexpr (sizeof(T) == 8) {
+                out = smallk ? CombineSmallK::value(dk, oemax + sT[n]) : Combine<T, S>::value(dk, oemax + sT[n]);
+              } else {
+                out = Combine<T, S>::value(dk, oemax + sT[n]);
+              }
               T &dst = crow[(int64_t)n * kstride];
               dst = a.accumulate ? dst + out : out;
             }
