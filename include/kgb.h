@@ -150,7 +150,10 @@ int kgb_source(kgb_ctx *ctx, double source_strength);
 int kgb_sweep_subdomain(kgb_ctx *ctx, int32_t sdom_id);
 /* SweepSolver over all subdomains: zeroes the planes, clears vacuum
  * boundaries, sweeps every subdomain in upwind order (all octants at once)
- * and hands planes to downwind zone sets. */
+ * and hands planes to downwind zone sets.  With the option "block_jacobi" = 1
+ * (--pmethod bj, src/Kripke/ParallelComm/BlockJacobiComm.cpp) every subdomain
+ * is swept at once from the planes as they stood after the zeroing, i.e. from
+ * zero inflow on every face, and no planes are handed on. */
 int kgb_sweep_solver(kgb_ctx *ctx);
 /* Kernel::population: sum over d,g,z of w(d) psi(d,g,z) volume(z), in FP64. */
 int kgb_population(kgb_ctx *ctx, double *out);
@@ -182,7 +185,9 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * the shapes fit; 0 = SIMT kernels; default: tensor for FP64, SIMT for the
  * mixed form); "scattering_tensor" (1 = the single-material zones' scattering on
  * the tensor cores, exact digit products, when groups <= 64; same defaults);
- * "graph" (1 = kgb_solve replays a captured CUDA graph, the default). */
+ * "graph" (1 = kgb_solve replays a captured CUDA graph, the default);
+ * "block_jacobi" (0 = the sweep method, default; 1 = block Jacobi, used by
+ * kgb_sweep_solver and so by every solve, iterate and adjoint call). */
 int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
 /* Current value of a knob: the keys above, plus "moments_tensor_ltimes",
  * "moments_tensor_lplustimes" and "scattering_tensor_active" (1 when that

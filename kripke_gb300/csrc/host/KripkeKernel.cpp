@@ -84,13 +84,17 @@ void kConst(Core::Field<double> &field, double value) {
 }  // namespace Kernel
 
 // src/Kripke/SweepSolver.cpp:23-87: planes zeroed, vacuum boundaries cleared,
-// subdomains swept in upwind order with the plane hand-off between zone sets.
-// The device schedules every subdomain of the list at once (all octants
-// concurrently); a partial list is swept subdomain by subdomain.
+// subdomains swept in upwind order with the plane hand-off between zone sets,
+// or, with block_jacobi (BlockJacobiComm.cpp), every subdomain from the zeroed
+// planes with no hand-off.  The device schedules every subdomain of the list
+// at once (all octants concurrently); a partial list is swept subdomain by
+// subdomain.
 void SweepSolver(Core::DataStore &ds, const std::vector<SdomId> &sdom_list, bool block_jacobi) {
   KRIPKE_TIMER(ds, SweepSolver);
-  if (block_jacobi) throw std::runtime_error("--pmethod bj is not available on the GB300 path (single rank)");
   auto &g = gpu(ds);
+  int64_t bj = 0;
+  g.check(kgb_get_option(g.ctx, "block_jacobi", &bj), "kgb_get_option");
+  if ((bj != 0) != block_jacobi) g.check(kgb_set_option(g.ctx, "block_jacobi", block_jacobi ? 1 : 0), "kgb_set_option");
   int32_t n = 0;
   g.check(kgb_num_subdomains(g.ctx, &n), "kgb_num_subdomains");
   if ((int)sdom_list.size() == n) {

@@ -50,7 +50,10 @@ void usage() {
   printf("  --zset <zx>,<zy>,<zz>  Number of zone-sets in x,y, and z\n                         Default:  --zset 1,1,1\n\n");
   printf("\nSolver Options:\n---------------\n");
   printf("  --niter <NITER>        Number of solver iterations to run\n                         Default:  --niter %d\n\n", def.niter);
-  printf("  --pmethod <method>     sweep (default); bj is not available on one rank\n\n");
+  printf("  --pmethod <method>     Parallel solver method\n");
+  printf("                         sweep: Full up-wind sweep (wavefront algorithm)\n");
+  printf("                         bj: Block Jacobi\n");
+  printf("                         Default: --pmethod sweep\n\n");
   exit(1);
 }
 
@@ -141,10 +144,6 @@ int main(int argc, char **argv) {
     }
   }
   if (vars.checkValues()) return 1;
-  if (vars.parallel_method == PMETHOD_BJ) {
-    printf("Block Jacobi needs more than one zone set per rank exchange; not available on the GB300 path\n");
-    return 1;
-  }
 
   printf("\nInput Parameters\n================\n\n");
   printf("  Problem Size:\n");
@@ -160,7 +159,8 @@ int main(int argc, char **argv) {
   printf("    Geometry:              %s\n", vars.geometry ? "100 cm cube, first duct leg" : "Kobayashi 3i");
   printf("    Scattering matrix:     %s\n", vars.scatter ? "seeded lower-triangular downscatter" : "diagonal P0");
   printf("\n  Solver Options:\n    Number iterations:     %d\n", vars.niter);
-  printf("\n  MPI Decomposition Options:\n    Total MPI tasks:       1\n    Spatial decomp:        1 x 1 x 1 MPI tasks\n    Block solve method:    Sweep\n");
+  printf("\n  MPI Decomposition Options:\n    Total MPI tasks:       1\n    Spatial decomp:        1 x 1 x 1 MPI tasks\n    Block solve method:    %s\n",
+         vars.parallel_method == PMETHOD_BJ ? "Block Jacobi" : "Sweep");
   printf("\n  Per-Task Options:\n");
   printf("    DirSets/Directions:    %d sets, %d directions/set\n", vars.num_dirsets, vars.num_directions / vars.num_dirsets);
   printf("    GroupSet/Groups:       %d sets, %d groups/set\n", vars.num_groupsets, vars.num_groups / vars.num_groupsets);

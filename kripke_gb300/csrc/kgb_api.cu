@@ -206,6 +206,7 @@ struct kgb_ctx {
   };
   std::vector<SolveGraph> solve_graphs;
   bool use_graph = true, graph_active = false;
+  bool block_jacobi = false;  // --pmethod bj: every zone set swept at once from zeroed planes
 };
 
 namespace {
@@ -1001,6 +1002,11 @@ int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
 
 int sweepSolver(kgb_ctx *ctx, bool fused_pop = false) {
   for (int k = 0; k < 3; ++k) CK(cudaMemsetAsync(ctx->plane[k], 0, ctx->plane_chunk[k] * ctx->dc.num() * ctx->tsz, ctx->stream));
+  // Block Jacobi (BlockJacobiComm.cpp:46-98 with SweepSolver.cpp:28-30): the
+  // planes every subdomain receives are the ones saved right after the zeroing
+  // above, so no subdomain waits on another and none hands its outgoing planes
+  // on.  One launch sweeps all of them, each from zero inflow on every face.
+  if (ctx->block_jacobi) return sweepWaveAny(ctx, ctx->levels_d, ctx->dc.num(), fused_pop);
   const int nlev = (int)ctx->level_off.size() - 1;
   const int S[3] = {ctx->dc.Sx, ctx->dc.Sy, ctx->dc.Sz};
   // the reversed (adjoint) orientation visits the zone-set levels last to first
@@ -2227,6 +2233,11 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->dirty_ell = true;
     return KGB_OK;
   }
+  if (!std::strcmp(key, "block_jacobi")) {
+    if (value != 0 && value != 1) return fail(ctx, KGB_ERR_ARG, "block_jacobi must be 0 (sweep) or 1 (bj)");
+    ctx->block_jacobi = value != 0;
+    return KGB_OK;
+  }
   if (!std::strcmp(key, "scattering_tensor")) {
     ctx->allow_tc_sc = value != 0;
     ctx->use_tc_sc = value != 0;
@@ -2344,6 +2355,7 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "scattering_tensor")) *value = ctx->allow_tc_sc ? 1 : 0;
   else if (!std::strcmp(key, "scattering_tensor_active")) *value = (ctx->tc_sc && ctx->use_tc_sc) ? 1 : 0;
   else if (!std::strcmp(key, "graph_active")) *value = ctx->graph_active ? 1 : 0;
+  else if (!std::strcmp(key, "block_jacobi")) *value = ctx->block_jacobi ? 1 : 0;
   else return fail(ctx, KGB_ERR_ARG, std::string("unknown option '") + key + "'");
   return KGB_OK;
 }

@@ -168,6 +168,7 @@ struct orc_problem {
   std::vector<std::array<int, 3>> upwind, downwind;  // per sdom, -1 = boundary
   std::map<std::string, Field> f;
   int threads = 0;
+  bool block_jacobi = false;  // SteadyStateSolver's block_jacobi argument (--pmethod bj)
   double last_solve_s = 0.0;
 
   Field &fld(const char *n) { return f.at(n); }
@@ -739,6 +740,15 @@ void kConstAll(orc_problem &p, const char *name, double value) {
 
 // SweepSolver.cpp:23-87 with the on-rank part of ParallelComm (dependency
 // counts, ready list in queue order, plane copy to the downwind subdomain).
+//
+// With block_jacobi, BlockJacobiComm.cpp:23-98 instead: addSubdomain saves the
+// planes into old_*_plane, and the first workRemaining() sends every queued
+// subdomain's saved planes downwind (ParallelComm.cpp:146-162 copies them into
+// the downwind subdomain's planes and drops its dependency count), after which
+// every subdomain is ready and markComplete only dequeues.  The save follows
+// kCopy's stated direction (old <- current); the reference's kCopy body
+// (Kernel.h:60-72) assigns src = dst, which would instead fill the planes from
+// the freshly allocated, unset old_*_plane storage.
 void sweepSolver(orc_problem &p) {
   kConstAll(p, "i_plane", 0.0);
   kConstAll(p, "j_plane", 0.0);
@@ -751,6 +761,32 @@ void sweepSolver(orc_problem &p) {
     depends.push_back(n);
   }
   const char *planes[3] = {"i_plane", "j_plane", "k_plane"};
+  if (p.block_jacobi) {
+    std::vector<std::vector<double>> old[3];
+    for (int dim = 0; dim < 3; ++dim) old[dim] = p.fld(planes[dim]).d;
+    for (int s : std::vector<int>(queue)) {
+      for (int dim = 0; dim < 3; ++dim) {
+        int dn = p.downwind[s][dim];
+        if (dn < 0) continue;
+        for (size_t i = 0; i < queue.size(); ++i)
+          if (queue[i] == dn) { depends[i]--; break; }
+        Field &pl = p.fld(planes[dim]);
+        pl.d[p.dc.chunkOf(pl.space, dn)] = old[dim][p.dc.chunkOf(pl.space, s)];
+      }
+    }
+    while (!queue.empty()) {
+      size_t idx = 0;
+      while (idx < queue.size() && depends[idx] != 0) ++idx;
+      if (idx == queue.size()) return;  // unreachable: every dependency was met by the sends
+      int s = queue[idx];
+      for (int dim = 0; dim < 3; ++dim)
+        if (p.upwind[s][dim] == -1) zeroChunk(p, planes[dim], s);
+      kSweep(p, s);
+      queue.erase(queue.begin() + idx);
+      depends.erase(depends.begin() + idx);
+    }
+    return;
+  }
   while (!queue.empty()) {
     size_t idx = 0;
     while (idx < queue.size() && depends[idx] != 0) ++idx;
@@ -863,6 +899,8 @@ orc_problem *orc_create(const orc_input *in) {
 
 void orc_destroy(orc_problem *p) { delete p; }
 const char *orc_error(void) { return g_err.c_str(); }
+
+void orc_set_block_jacobi(orc_problem *p, int on) { p->block_jacobi = on != 0; }
 
 void orc_set_threads(orc_problem *p, int n) {
   p->threads = n;

@@ -67,6 +67,10 @@ const char *orc_error(void);
  * n > 0 = OpenMP with n threads (reference OpenMP policies, the timed CPU baseline). */
 void orc_set_threads(orc_problem *p, int n);
 
+/* 1: orc_sweep_solver (and every solve) runs the block Jacobi method
+ * (--pmethod bj, SteadyStateSolver's block_jacobi argument); 0: the sweep. */
+void orc_set_block_jacobi(orc_problem *p, int on);
+
 int32_t orc_num_sdoms(const orc_problem *p);
 /* Element count (all chunks) and element size in bytes of a named field; -1 if unknown. */
 int64_t orc_field_size(const orc_problem *p, const char *name);

@@ -49,6 +49,7 @@ def lib():
         L.orc_destroy.argtypes = [P]
         L.orc_error.restype = ctypes.c_char_p
         L.orc_set_threads.argtypes = [P, ctypes.c_int]
+        L.orc_set_block_jacobi.argtypes = [P, ctypes.c_int]
         L.orc_num_sdoms.argtypes = [P]
         L.orc_num_sdoms.restype = ctypes.c_int32
         L.orc_field_size.argtypes = [P, ctypes.c_char_p]
@@ -114,13 +115,19 @@ def default_input(**kw):
 class Problem:
     """One generated problem held by the oracle (Kripke DataStore equivalent)."""
 
-    def __init__(self, inp=None, threads=0, **kw):
+    def __init__(self, inp=None, threads=0, block_jacobi=False, **kw):
         self.inp = inp if inp is not None else default_input(**kw)
         self.h = lib().orc_create(ctypes.byref(self.inp))
         if not self.h:
             raise ValueError("oracle rejected input: " + lib().orc_error().decode())
         if threads:
             lib().orc_set_threads(self.h, threads)
+        if block_jacobi:
+            self.set_block_jacobi(True)
+
+    def set_block_jacobi(self, on):
+        """--pmethod bj (SteadyStateSolver's block_jacobi) for every later sweep solve."""
+        lib().orc_set_block_jacobi(self.h, 1 if on else 0)
 
     def close(self):
         if self.h:

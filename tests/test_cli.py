@@ -51,6 +51,7 @@ def test_rejects_bad_input(cli, args, msg):
     ([], dict(), 1e-12),
     (["--layout", "GZD", "--gset", "2", "--zset", "2,1,2"], dict(layout="GZD", gset=2, zsets=(2, 1, 2)), 1e-12),
     (["--precision", "mixed", "--autotune"], dict(), 1e-5),
+    (["--pmethod", "bj", "--zset", "2,2,1"], dict(zsets=(2, 2, 1), block_jacobi=True), 1e-12),
 ])
 def test_solve_matches_oracle(cli, oracle, extra, kw, rtol):
     base = ["--zones", "8,8,8", "--groups", "8", "--quad", "4:8", "--legendre", "2", "--niter", "4",
