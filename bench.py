@@ -247,9 +247,20 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     for _ in range(args.warmup):
         ctx.iterate(want_population=False)
     ms = timed_steps(ctx, stream, args.steps)
-    ctx.solve(MIXED_PHI_ITERS)
+    # the fused sweep (rhs formed inside the sweep, no LPlusTimes launch) on the same state
+    ctx.set_option("fused_sweep", 1)
+    for _ in range(args.warmup):
+        ctx.iterate(want_population=False)
+    ms_fused = timed_steps(ctx, stream, args.steps)
+    fused_active = ctx.get_option("fused_sweep_active")
+    parts_fused = ctx.solve(MIXED_PHI_ITERS)
+    phi_fused = ctx.download("phi")
+    ctx.set_option("fused_sweep", 0)
+    parts = ctx.solve(MIXED_PHI_ITERS)
     fp64_ctx.solve(MIXED_PHI_ITERS)
     a, b = fp64_ctx.download("phi"), ctx.download("phi")
+    fused_same = bool(np.array_equal(parts, parts_fused) and np.array_equal(b, phi_fused))
+    del phi_fused
     err = float(np.abs(b - a).max() / np.abs(a).max())
     err_l2 = float(np.linalg.norm(b - a) / np.linalg.norm(a))
     # moment 0 (DGZ host nesting: phi chunks are [M][G][Z], one chunk per group set)
@@ -265,7 +276,11 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
                                  "error of moment 0" % MIXED_PHI_ITERS,
            "autotuned": tuned,
            "kernels": {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "moments_tensor_ltimes",
-                                                      "moments_tensor_lplustimes")}}
+                                                      "moments_tensor_lplustimes")},
+           "fused_sweep": {"ms_per_step": ms_fused, "value": unknowns(w) / (ms_fused * 1e-3),
+                           "speedup_vs_unfused": ms / ms_fused, "active": fused_active,
+                           "identical_to_unfused": fused_same,
+                           "what": "LPlusTimes formed inside the sweep (rhs neither written nor read), same tiles"}}
     ctx.close()
     return out
 

@@ -187,13 +187,19 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * the tensor cores, exact digit products, when groups <= 64; same defaults);
  * "graph" (1 = kgb_solve replays a captured CUDA graph, the default);
  * "block_jacobi" (0 = the sweep method, default; 1 = block Jacobi, used by
- * kgb_sweep_solver and so by every solve, iterate and adjoint call). */
+ * kgb_sweep_solver and so by every solve, iterate and adjoint call);
+ * "fused_sweep" (mixed form, Legendre order <= 4: 1 = the solver loop forms
+ * each cell's rhs inside the sweep from phi_out and ell_plus instead of
+ * running LPlusTimes, with the SIMT kernel's arithmetic, so psi is unchanged;
+ * rhs is then refreshed, as L+ phi_out, only when an entry point reads it --
+ * download, kgb_lplustimes, the sweep entry points, kgb_balance, autotune). */
 int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
 /* Current value of a knob: the keys above, plus "moments_tensor_ltimes",
  * "moments_tensor_lplustimes" and "scattering_tensor_active" (1 when that
  * kernel runs on the tensor cores), "sweep_reciprocals_active" (1 when the
- * sweep uses tabulated reciprocals) and "graph_active" (1 when the last
- * kgb_solve replayed a graph). */
+ * sweep uses tabulated reciprocals), "graph_active" (1 when the last
+ * kgb_solve replayed a graph) and "fused_sweep_active" (1 when the last
+ * iteration formed rhs inside the sweep). */
 int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value);
 /* Autotuner: times every sweep tile shape (footprint 4x4, 4x2, 2x2 x depth
  * 2, 4, 8, 16 zones) and both LTimes / LPlusTimes paths (tensor-core digit

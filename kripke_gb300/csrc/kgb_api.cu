@@ -207,6 +207,9 @@ struct kgb_ctx {
   std::vector<SolveGraph> solve_graphs;
   bool use_graph = true, graph_active = false;
   bool block_jacobi = false;  // --pmethod bj: every zone set swept at once from zeroed planes
+  // mixed form: the solver loop forms rhs inside the sweep (no LPlusTimes launch);
+  // rhs then holds an older value until an entry point that reads it refreshes it
+  bool fuse_sweep = false, fuse_active = false, rhs_stale = false;
 };
 
 namespace {
@@ -936,8 +939,13 @@ int buildTiles(kgb_ctx *ctx) {
 // Kernel drivers
 // ---------------------------------------------------------------------------
 template <typename T>
-int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop) {
+int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool fused_rhs) {
   SweepArgs<T> a{};
+  if (fused_rhs) {
+    a.phiout = as<T>(ctx->phi_out);
+    a.ellp = as<T>(ctx->ellp);
+    a.M = ctx->M;
+  }
   a.rhs = as<T>(ctx->rhs);
   a.psi = as<T>(ctx->psi);
   a.sigt = as<T>(ctx->sigt);
@@ -979,9 +987,9 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop) {
   return KGB_OK;
 }
 
-int sweepWaveAny(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop = false) {
-  return ctx->prec == KGB_FP64 ? sweepWave<double>(ctx, wave_dev, nwave, fused_pop)
-                               : sweepWave<float>(ctx, wave_dev, nwave, fused_pop);
+int sweepWaveAny(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop = false, bool fused_rhs = false) {
+  return ctx->prec == KGB_FP64 ? sweepWave<double>(ctx, wave_dev, nwave, fused_pop, fused_rhs)
+                               : sweepWave<float>(ctx, wave_dev, nwave, fused_pop, fused_rhs);
 }
 
 int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
@@ -1000,13 +1008,13 @@ int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
   return KGB_OK;
 }
 
-int sweepSolver(kgb_ctx *ctx, bool fused_pop = false) {
+int sweepSolver(kgb_ctx *ctx, bool fused_pop = false, bool fused_rhs = false) {
   for (int k = 0; k < 3; ++k) CK(cudaMemsetAsync(ctx->plane[k], 0, ctx->plane_chunk[k] * ctx->dc.num() * ctx->tsz, ctx->stream));
   // Block Jacobi (BlockJacobiComm.cpp:46-98 with SweepSolver.cpp:28-30): the
   // planes every subdomain receives are the ones saved right after the zeroing
   // above, so no subdomain waits on another and none hands its outgoing planes
   // on.  One launch sweeps all of them, each from zero inflow on every face.
-  if (ctx->block_jacobi) return sweepWaveAny(ctx, ctx->levels_d, ctx->dc.num(), fused_pop);
+  if (ctx->block_jacobi) return sweepWaveAny(ctx, ctx->levels_d, ctx->dc.num(), fused_pop, fused_rhs);
   const int nlev = (int)ctx->level_off.size() - 1;
   const int S[3] = {ctx->dc.Sx, ctx->dc.Sy, ctx->dc.Sz};
   // the reversed (adjoint) orientation visits the zone-set levels last to first
@@ -1015,7 +1023,7 @@ int sweepSolver(kgb_ctx *ctx, bool fused_pop = false) {
     const int lv = ctx->flip ? nlev - 1 - step : step;
     const int b = ctx->level_off[lv], e = ctx->level_off[lv + 1];
     if (e == b) continue;
-    int rc = sweepWaveAny(ctx, ctx->levels_d + b, e - b, fused_pop);
+    int rc = sweepWaveAny(ctx, ctx->levels_d + b, e - b, fused_pop, fused_rhs);
     if (rc) return rc;
     // hand the outgoing planes to downwind zone sets (ParallelComm.cpp:146-162)
     for (int x = b; x < e; ++x) {
@@ -1108,6 +1116,7 @@ int doLTimes(kgb_ctx *ctx, bool acc) {
 
 int doLPlusTimes(kgb_ctx *ctx, bool acc) {
   FamScope fs(ctx, "lplustimes");
+  ctx->rhs_stale = false;
   const int64_t rows = ctx->Z * ctx->G;
   if (ctx->tc_lp && ctx->use_tc_lp) {
     if (ctx->prec == KGB_FP64)
@@ -1125,6 +1134,14 @@ int doLPlusTimes(kgb_ctx *ctx, bool acc) {
     launch_lplustimes<float>(as<float>(ctx->phi_out), as<float>(ctx->rhs), as<float>(ctx->ellp), rows, ctx->D, ctx->M, acc, ctx->stream);
   CKN(1);
   return KGB_OK;
+}
+
+// rhs as the last iteration swept it (L+ phi_out), for entry points that read
+// rhs after a solver loop with the fused sweep.
+int ensureRhs(kgb_ctx *ctx) {
+  if (!ctx->rhs_stale) return KGB_OK;
+  int rc = prepare(ctx);
+  return rc ? rc : doLPlusTimes(ctx, false);
 }
 
 template <typename T>
@@ -1239,8 +1256,11 @@ int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot =
   }
   if ((rc = doScattering(ctx, false))) return rc;      // phi_out = S phi    (kConst + scattering)
   if ((rc = doSource(ctx, q))) return rc;              // phi_out += Q
-  if ((rc = doLPlusTimes(ctx, false))) return rc;      // rhs = L+ phi_out   (kConst + LPlusTimes)
-  if ((rc = sweepSolver(ctx, part_slot != nullptr))) return rc;  // psi = H^-1 rhs (+ population partials)
+  // rhs = L+ phi_out (kConst + LPlusTimes), or formed cell by cell inside the sweep
+  ctx->fuse_active = ctx->fuse_sweep && ctx->prec == KGB_MIXED && ctx->M <= kFuseMaxM;
+  if (!ctx->fuse_active && (rc = doLPlusTimes(ctx, false))) return rc;
+  if ((rc = sweepSolver(ctx, part_slot != nullptr, ctx->fuse_active))) return rc;  // psi = H^-1 rhs (+ population)
+  if (ctx->fuse_active) ctx->rhs_stale = true;
   if (part_slot) {
     FamScope fs(ctx, "population");
     launch_sum_partials(ctx->pop_slots, ctx->npop_slots, part_slot, ctx->stream);
@@ -1826,6 +1846,7 @@ int kgb_field_upload(kgb_ctx *ctx, const char *name, const void *host, int64_t n
   const int64_t want = fieldBytes(ctx, f);
   if (nbytes != want)
     return fail(ctx, KGB_ERR_ARG, std::string("field '") + name + "' expects " + std::to_string(want) + " bytes, got " + std::to_string(nbytes));
+  if (!std::strcmp(f->name, "rhs")) ctx->rhs_stale = false;
   CK(cudaSetDevice(ctx->device));
   const int nch = numChunks(ctx, f);
   const int layout = ctx->dims.layout;
@@ -1955,6 +1976,10 @@ int kgb_field_download(kgb_ctx *ctx, const char *name, void *host, int64_t nbyte
   if (nbytes != want)
     return fail(ctx, KGB_ERR_ARG, std::string("field '") + name + "' holds " + std::to_string(want) + " bytes, got " + std::to_string(nbytes));
   CK(cudaSetDevice(ctx->device));
+  if (!std::strcmp(f->name, "rhs")) {
+    int rc = ensureRhs(ctx);
+    if (rc) return rc;
+  }
   const int nch = numChunks(ctx, f);
   if (deviceKind(f->kind)) {
     size_t maxc = 0;
@@ -2054,6 +2079,7 @@ int kgb_field_fill(kgb_ctx *ctx, const char *name, double value) {
   const FieldInfo *f = findField(name);
   if (!f) return fail(ctx, KGB_ERR_ARG, std::string("unknown field '") + (name ? name : "(null)") + "'");
   CK(cudaSetDevice(ctx->device));
+  if (!std::strcmp(f->name, "rhs")) ctx->rhs_stale = false;
   return fillField(ctx, f, value);
 }
 
@@ -2064,6 +2090,7 @@ int kgb_ltimes(kgb_ctx *ctx) {
 
 int kgb_lplustimes(kgb_ctx *ctx) {
   int rc = prepare(ctx);
+  if (!rc) rc = ensureRhs(ctx);
   return rc ? rc : doLPlusTimes(ctx, true);
 }
 
@@ -2081,11 +2108,13 @@ int kgb_sweep_subdomain(kgb_ctx *ctx, int32_t sdom) {
   int rc = prepare(ctx);
   if (rc) return rc;
   if (sdom < 0 || sdom >= ctx->dc.num()) return fail(ctx, KGB_ERR_ARG, "subdomain id out of range");
+  if ((rc = ensureRhs(ctx))) return rc;
   return sweepWaveAny(ctx, ctx->ident_d + sdom, 1);
 }
 
 int kgb_sweep_solver(kgb_ctx *ctx) {
   int rc = prepare(ctx);
+  if (!rc) rc = ensureRhs(ctx);
   return rc ? rc : sweepSolver(ctx);
 }
 
@@ -2102,6 +2131,7 @@ int kgb_population(kgb_ctx *ctx, double *out) {
 int kgb_balance(kgb_ctx *ctx, double out[5]) {
   if (!out) return fail(ctx, KGB_ERR_ARG, "null output");
   int rc = prepare(ctx);
+  if (!rc) rc = ensureRhs(ctx);
   if (rc) return rc;
   const int64_t rows = ctx->Z * ctx->G;
   CK(cudaMemsetAsync(ctx->results, 0, 8 * sizeof(double), ctx->stream));
@@ -2238,6 +2268,10 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->block_jacobi = value != 0;
     return KGB_OK;
   }
+  if (!std::strcmp(key, "fused_sweep")) {
+    ctx->fuse_sweep = value != 0;
+    return KGB_OK;
+  }
   if (!std::strcmp(key, "scattering_tensor")) {
     ctx->allow_tc_sc = value != 0;
     ctx->use_tc_sc = value != 0;
@@ -2254,6 +2288,7 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
 
 int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_z) {
   int rc = prepare(ctx);
+  if (!rc) rc = ensureRhs(ctx);
   if (rc) return rc;
   const int xys[3] = {44, 42, 22};
   const int tzs[4] = {2, 4, 8, 16};
@@ -2356,6 +2391,8 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "scattering_tensor_active")) *value = (ctx->tc_sc && ctx->use_tc_sc) ? 1 : 0;
   else if (!std::strcmp(key, "graph_active")) *value = ctx->graph_active ? 1 : 0;
   else if (!std::strcmp(key, "block_jacobi")) *value = ctx->block_jacobi ? 1 : 0;
+  else if (!std::strcmp(key, "fused_sweep")) *value = ctx->fuse_sweep ? 1 : 0;
+  else if (!std::strcmp(key, "fused_sweep_active")) *value = ctx->fuse_active ? 1 : 0;
   else return fail(ctx, KGB_ERR_ARG, std::string("unknown option '") + key + "'");
   return KGB_OK;
 }

@@ -55,7 +55,15 @@ struct SweepArgs {
   const double *w;            // [D]
   const double *vol;          // [Z]; unused when vol_uniform > 0
   double vol_uniform;
+  // fused LPlusTimes prologue (mixed form): rhs(z,g,d) = sum_m ellp[d][m] * phiout[z][g][m]
+  // formed per cell instead of read, or null: read rhs
+  const T *phiout;            // [Z][G][M]
+  const T *ellp;              // [D][M]
+  int M;
 };
+
+// Largest moment count (Legendre order 4) of the fused LPlusTimes prologue.
+constexpr int kFuseMaxM = 25;
 
 // Sweep tiles: footprint in i and j is a compile-time instance (4x4, 4x2 or
 // 2x2), depth in k is runtime.

@@ -42,6 +42,13 @@
 // volume * psi over its cells (FP64, or compensated FP32 in the mixed form),
 // scales by w(d), and each block writes one partial; a fixed-order reduction
 // over the partials follows the sweep.
+//
+// In the mixed form the LPlusTimes that precedes the sweep
+// (SteadyStateSolver.cpp:69-71) can be fused too (FUSE): a thread keeps its
+// direction's row of ell_plus in registers and forms each cell's rhs from the
+// zone's phi_out moments in the order the SIMT LPlusTimes kernel sums them
+// (ascending moment, one FMA chain), so the swept psi is bit-for-bit that of
+// the unfused iteration while rhs is neither written nor read.
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -92,7 +99,7 @@ __device__ __forceinline__ T ldFace(const T *p) {
 
 // One tile of one subdomain for one block of chains: tile is the index into
 // a.tiles, cb the chain block (chains cb*blockDim.x + threadIdx.x) of ncb.
-template <typename T, int TX, int TY, bool RECIP, bool POP, bool COH>
+template <typename T, int TX, int TY, bool RECIP, bool POP, bool COH, bool FUSE = false>
 __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom, const int tile, const int cb,
                                           const int ncb) {
   const SdomDesc sd = a.sdoms[sdom];
@@ -143,6 +150,11 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
       for (int jj = 0; jj < TY; ++jj)
         bo[ii][jj] = (iv[ii] && jv[jj]) ? ldFace<COH>(kpl + ((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c) : T(0);
 
+    T ep[FUSE ? kFuseMaxM : 1];
+    if constexpr (FUSE) {
+#pragma unroll
+      for (int m = 0; m < kFuseMaxM; ++m) ep[m] = m < a.M ? a.ellp[(int64_t)d * a.M + m] : T(0);
+    }
     const T *__restrict__ rhs = a.rhs;
     T *__restrict__ psi = a.psi;
     const int kend = min(a.tz, a.nzs - kb);
@@ -161,7 +173,19 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
         for (int ii = 0; ii < TX; ++ii) {
           const int64_t z = zrow + iloc[ii];
           if (iv[ii] && jv[jj]) {
-            rv[jj][ii] = rhs[(z * a.G + g) * a.D + d];
+            if constexpr (FUSE) {
+              // unconditional loads (the index is clamped to the row; beyond M the
+              // coefficient is zero and the FMA leaves the sum unchanged) so the
+              // compiler can issue them ahead of the chain
+              const T *__restrict__ ph = a.phiout + (z * a.G + g) * a.M;
+              const int mlast = a.M - 1;
+              T acc = T(0);
+#pragma unroll
+              for (int m = 0; m < kFuseMaxM; ++m) acc += ep[m] * __ldg(ph + min(m, mlast));
+              rv[jj][ii] = acc;
+            } else {
+              rv[jj][ii] = rhs[(z * a.G + g) * a.D + d];
+            }
             if (RECIP) sv[jj][ii] = a.inv[(int64_t)a.cls[z * a.G + g] * a.D + d];
             else sv[jj][ii] = a.sigt[z * a.G + g];
           } else {
@@ -222,9 +246,10 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
   }
 }
 
-template <typename T, int TX, int TY, bool RECIP, bool POP>
+template <typename T, int TX, int TY, bool RECIP, bool POP, bool FUSE = false>
 __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const __grid_constant__ SweepArgs<T> a) {
-  sweepTile<T, TX, TY, RECIP, POP, false>(a, a.wave[blockIdx.z], a.tile_off + blockIdx.y, blockIdx.x, gridDim.x);
+  sweepTile<T, TX, TY, RECIP, POP, false, FUSE>(a, a.wave[blockIdx.z], a.tile_off + blockIdx.y, blockIdx.x,
+                                                gridDim.x);
 }
 
 namespace {
@@ -296,14 +321,22 @@ __global__ void __launch_bounds__(kSweepThreads) batch_sweep_kernel(const SweepA
 }
 
 namespace {
-template <typename T, int TX, int TY>
-void launchTile(const SweepArgs<T> &a, dim3 grid, cudaStream_t s) {
+template <typename T, int TX, int TY, bool FUSE>
+void launchTileAs(const SweepArgs<T> &a, dim3 grid, cudaStream_t s) {
   const bool recip = a.cls != nullptr && a.inv != nullptr;
   const bool pop = a.pop != nullptr;
-  if (recip && pop) sweep_step_kernel<T, TX, TY, true, true><<<grid, kSweepThreads, 0, s>>>(a);
-  else if (recip) sweep_step_kernel<T, TX, TY, true, false><<<grid, kSweepThreads, 0, s>>>(a);
-  else if (pop) sweep_step_kernel<T, TX, TY, false, true><<<grid, kSweepThreads, 0, s>>>(a);
-  else sweep_step_kernel<T, TX, TY, false, false><<<grid, kSweepThreads, 0, s>>>(a);
+  if (recip && pop) sweep_step_kernel<T, TX, TY, true, true, FUSE><<<grid, kSweepThreads, 0, s>>>(a);
+  else if (recip) sweep_step_kernel<T, TX, TY, true, false, FUSE><<<grid, kSweepThreads, 0, s>>>(a);
+  else if (pop) sweep_step_kernel<T, TX, TY, false, true, FUSE><<<grid, kSweepThreads, 0, s>>>(a);
+  else sweep_step_kernel<T, TX, TY, false, false, FUSE><<<grid, kSweepThreads, 0, s>>>(a);
+}
+// the fused LPlusTimes prologue exists for the mixed form only
+template <typename T, int TX, int TY>
+void launchTile(const SweepArgs<T> &a, dim3 grid, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (a.phiout != nullptr) return launchTileAs<T, TX, TY, true>(a, grid, s);
+  }
+  launchTileAs<T, TX, TY, false>(a, grid, s);
 }
 }  // namespace
 

@@ -57,7 +57,7 @@ def test_bj_decouples_zone_sets(oracle):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("zsets,layout,precision", [((2, 2, 1), "DGZ", 0), ((1, 3, 2), "GZD", 0), ((2, 2, 2), "DGZ", 1)])
+@pytest.mark.parametrize("zsets,layout,precision", [((2, 2, 1), "DGZ", 0), ((1, 2, 5), "GZD", 0), ((2, 3, 1), "DGZ", 1)])
 def test_bj_solve_matches_oracle(kgb, oracle, zsets, layout, precision):
     p = oracle.Problem(zsets=zsets, layout=layout, block_jacobi=True, **KW)
     want = p.solve(4)
@@ -74,9 +74,9 @@ def test_bj_solve_matches_oracle(kgb, oracle, zsets, layout, precision):
 
 @pytest.mark.gpu
 def test_bj_sweep_solver_and_graph_switch(kgb, oracle):
-    p = oracle.Problem(zsets=(2, 1, 2), block_jacobi=True, **KW)
+    p = oracle.Problem(zsets=(2, 1, 5), block_jacobi=True, **KW)
     c = kgb.Context()
-    c.generate(zsets=(2, 1, 2), **KW)
+    c.generate(zsets=(2, 1, 5), **KW)
     rhs = random_rhs(p)
     c.upload("rhs", rhs)
     c.set_option("block_jacobi", 1)
@@ -88,7 +88,7 @@ def test_bj_sweep_solver_and_graph_switch(kgb, oracle):
     bj = np.array(c.solve(3))
     c.set_option("block_jacobi", 0)
     sw = np.array(c.solve(3))
-    q = oracle.Problem(zsets=(2, 1, 2), **KW)
+    q = oracle.Problem(zsets=(2, 1, 5), **KW)
     np.testing.assert_allclose(sw, q.solve(3), rtol=1e-12)
     c.set_option("block_jacobi", 1)
     np.testing.assert_array_equal(np.array(c.solve(3)), bj)
@@ -100,13 +100,16 @@ def test_bj_sweep_solver_and_graph_switch(kgb, oracle):
 def test_bj_gradient_matches_finite_differences(kgb):
     # the transpose of block Jacobi's block-diagonal sweep is the reversed sweep of
     # each subdomain from zero inflow: the adjoint solve runs it through the same switch
-    from test_adjoint import BASE, MAXIT, TOL, detector, fd_response, rel_err, solve_gradient
+    # (the zone sets without source stay empty under block Jacobi, so the detector spans the mesh)
+    from test_adjoint import BASE, fd_response, rel_err, solve_gradient
     ctx = kgb.Context()
     inp = ctx.generate(**dict(BASE, zsets=(2, 1, 2)))
     ctx.set_option("block_jacobi", 1)
-    ctx.set_response(detector(*BASE["zones"]))
+    nz = int(np.prod(BASE["zones"]))
+    ctx.set_response(np.linspace(0.5, 1.5, nz))
     st, sg = kgb.material_tables(inp)
     R, dt, ds, dq = solve_gradient(ctx)
+    assert R > 0 and np.abs(dt).max() > 0 and np.abs(ds).max() > 0
     assert abs(R - dq) <= 1e-11 * abs(R)
     fd_t = np.zeros_like(dt)
     for m, g in zip(*np.unravel_index(np.argsort(-np.abs(dt), axis=None)[:3], dt.shape)):
