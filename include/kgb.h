@@ -177,8 +177,9 @@ int kgb_sync(kgb_ctx *ctx);
 /* Run on a caller-owned CUDA stream (a cudaStream_t passed as a pointer)
  * instead of the context's own; NULL restores the context's stream. */
 int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
-/* Tuning knobs: "sweep_tile_z" (tile depth in k, default 4); "sweep_tile_xy"
- * (tile footprint in i and j: 44, 42 or 22, default 44); "sweep_reciprocals"
+/* Tuning knobs: "sweep_tile_z" (tile depth in k, default 8); "sweep_tile_xy"
+ * (tile footprint in i and j: 44, 42 or 22; default 22 in FP64, 42 in the
+ * mixed form); "sweep_reciprocals"
  * (uniform mesh: 1 = tabulate 1/denominator per (sigt value, direction), the
  * FP64 default; 0 = divide in every cell, the mixed default); "moments_tensor"
  * (1 = LTimes and LPlusTimes on the tensor cores with exact digit products when

@@ -35,7 +35,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall", "-I" + 
 CU_SOURCES = ["kgb_api.cu", "sweep.cu", "moments.cu", "scatter.cu", "reduce.cu", "xpose.cu", "noalloc.cu", "tc_moments.cu",
               "adjoint.cu", "batch.cu"]
 CPP_SOURCES = ["generate.cpp"]
-HEADERS = ["kgb_internal.h", "kgb_layout.h"]
+HEADERS = ["kgb_internal.h", "kgb_layout.h", "exact_round.h"]
 
 
 def _nvcc():

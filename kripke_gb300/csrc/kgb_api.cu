@@ -91,6 +91,7 @@ struct kgb_ctx {
   size_t tsz = 8;
   int tz = 4;
   int tx = 4, ty = 4;  // sweep tile footprint
+  bool tiles_set = false;  // the caller chose the tile shape: setup keeps it
 
   // device state (element type T = double or float by precision)
   void *psi = nullptr, *rhs = nullptr, *phi = nullptr, *phi_out = nullptr, *sigt = nullptr;
@@ -152,7 +153,7 @@ struct kgb_ctx {
   uint16_t *tc_lt_img = nullptr, *tc_lp_img = nullptr;
   int *tc_lt_exp = nullptr, *tc_lp_exp = nullptr;
   int tc_lt_kpad = 0, tc_lp_nhalf = 0;
-  int tc_lp_stages = 2;
+  int tc_lp_stages = 2, tc_lp_stage_out = 1;
   int *err_d = nullptr;                     // set by kernels whose bounded waits gave up
   int nsm = 0;
   // fused population partials, one per (tile, subdomain, chain block)
@@ -510,17 +511,44 @@ int buildReciprocalsT(kgb_ctx *ctx) {
     for (double v : ctx->dxyz[k])
       if (v != ctx->dxyz[k][0]) return KGB_OK;
   const int64_t n = ctx->Z * ctx->G;
-  std::vector<T> sig(n);
-  CK(cudaMemcpyAsync(sig.data(), ctx->sigt, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream));
+  // distinct sigt values found on the device (hash table of bit patterns), sorted here
+  const size_t nslot = (size_t)1 << kClassTableBits;
+  unsigned long long *table = nullptr;
+  int *ovf = nullptr;
+  int rc;
+  if ((rc = dmalloc(ctx, &table, nslot)) || (rc = dmalloc(ctx, &ovf, 1))) {
+    cudaFree(table);
+    return rc;
+  }
+  struct Free {
+    void *a, *b;
+    ~Free() { cudaFree(a); cudaFree(b); }
+  } guard{table, ovf};
+  std::vector<unsigned long long> keys(nslot);
+  int overflow = 0;
+  CK(cudaMemsetAsync(table, 0xFF, nslot * sizeof(unsigned long long), ctx->stream));
+  CK(cudaMemsetAsync(ovf, 0, sizeof(int), ctx->stream));
+  launch_class_insert<T>(as<T>(ctx->sigt), n, table, ovf, ctx->stream);
+  CKN(1);
+  CK(cudaMemcpyAsync(keys.data(), table, nslot * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&overflow, ovf, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  std::vector<T> uniq(sig);
+  if (overflow) return KGB_OK;  // not tabulated: the sweep divides per cell
+  std::vector<T> uniq;
+  for (unsigned long long k : keys) {
+    if (k == kClassEmpty) continue;
+    T v;
+    if constexpr (sizeof(T) == 8) std::memcpy(&v, &k, 8);
+    else {
+      const uint32_t b = (uint32_t)k;
+      std::memcpy(&v, &b, 4);
+    }
+    uniq.push_back(v);
+  }
   std::sort(uniq.begin(), uniq.end());
   uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
   const int64_t ncls = (int64_t)uniq.size();
-  if (ncls > 65535 || ncls * ctx->D > (int64_t)16 << 20) return KGB_OK;
-  std::vector<uint16_t> cls(n);
-  for (int64_t e = 0; e < n; ++e)
-    cls[e] = (uint16_t)(std::lower_bound(uniq.begin(), uniq.end(), sig[e]) - uniq.begin());
+  if (ncls == 0 || ncls > 65535 || ncls * ctx->D > (int64_t)16 << 20) return KGB_OK;
   std::vector<T> inv((size_t)ncls * ctx->D);
   for (int64_t c = 0; c < ncls; ++c)
     for (int d = 0; d < ctx->D; ++d) {
@@ -535,12 +563,18 @@ int buildReciprocalsT(kgb_ctx *ctx) {
   if (ctx->inv_d) cudaFree(ctx->inv_d);
   ctx->cls_d = nullptr;
   ctx->inv_d = nullptr;
-  int rc;
-  T *inv_d = nullptr;
+  T *inv_d = nullptr, *uniq_d = nullptr;
   if ((rc = dmalloc(ctx, &ctx->cls_d, n)) || (rc = dmalloc(ctx, &inv_d, inv.size()))) return rc;
   ctx->inv_d = inv_d;
-  CK(cudaMemcpyAsync(ctx->cls_d, cls.data(), n * sizeof(uint16_t), cudaMemcpyHostToDevice, ctx->stream));
+  if ((rc = dmalloc(ctx, &uniq_d, uniq.size()))) return rc;
+  struct FreeU {
+    void *a;
+    ~FreeU() { cudaFree(a); }
+  } guard_u{uniq_d};
+  CK(cudaMemcpyAsync(uniq_d, uniq.data(), uniq.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(inv_d, inv.data(), inv.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+  launch_class_lookup<T>(as<T>(ctx->sigt), n, uniq_d, (int)ncls, ctx->cls_d, ctx->stream);
+  CKN(1);
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->ncls = ncls;
   ctx->use_recip = true;
@@ -609,9 +643,12 @@ int planTensorMomentsFrom(kgb_ctx *ctx, const std::vector<double> &lt_src, const
     const int nhalf = (D + NB - 1) / NB;
     const size_t stage = (size_t)S * 32 * 128 * 2;
     const size_t smem1 = 1024 + (size_t)nhalf * 32 * S * NB * 2 + stage + 4 * nhalf * NB;
-    // + the kernel's static shared memory; a second A stage when it fits (overlap across tiles)
-    ctx->tc_lp_stages = smem1 + stage + 4096 <= 227 * 1024 ? 2 : 1;
-    if (smem1 + 4096 <= 227 * 1024) {
+    // + the kernel's static shared memory; the output staging of 16 warps (32 rows x 5
+    // values each) when it fits, then a second A stage when that fits too (overlap across tiles)
+    const size_t lim = 227 * 1024 - 4096, stg = 16 * 32 * 5 * sizeof(T);
+    ctx->tc_lp_stage_out = smem1 + stg <= lim ? 1 : 0;
+    ctx->tc_lp_stages = smem1 + stage + (ctx->tc_lp_stage_out ? stg : 0) <= lim ? 2 : 1;
+    if (smem1 <= lim) {
       std::vector<double> bt((size_t)M * D);
       for (int d = 0; d < D; ++d)
         for (int m = 0; m < M; ++m) bt[(size_t)m * D + d] = lp_src[(size_t)d * M + m];
@@ -1083,6 +1120,7 @@ void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, i
   a.accumulate = acc;
   a.nsm = ctx->nsm;
   a.stages = multi_n ? ctx->tc_lp_stages : 2;
+  a.stage_out = multi_n ? ctx->tc_lp_stage_out : 1;  // LTimes' B image is at most 64 KB: staging fits
   launch_tc_rows<T>(a, sizeof(T) == 8 ? 8 : 4, 0, multi_n, ctx->stream);
 }
 
@@ -1730,6 +1768,13 @@ int kgb_setup(kgb_ctx *ctx, const kgb_dims *d) {
   // the tabulated reciprocal pays where the divide costs FP64 slots; in FP32 its
   // dependent table load costs more than the divide it saves
   ctx->allow_recip = ctx->prec == KGB_FP64;
+  // default sweep tiles: the autotuner's choice on 32^3 and 64^3 problems (2x2x8 in
+  // FP64, where the FP64 pipe wants the most chains in flight; 4x2x8 in FP32)
+  if (!ctx->tiles_set) {
+    ctx->tx = ctx->prec == KGB_FP64 ? 2 : 4;
+    ctx->ty = 2;
+    ctx->tz = 8;
+  }
   ctx->dc.SP = d->num_groupsets;
   ctx->dc.SQ = d->num_dirsets;
   ctx->dc.Sx = d->num_zonesets[0];
@@ -2247,11 +2292,13 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
   if (!std::strcmp(key, "sweep_tile_z")) {
     if (value < 1 || value > 1024) return fail(ctx, KGB_ERR_ARG, "sweep_tile_z must be in [1, 1024]");
     ctx->tz = (int)value;
+    ctx->tiles_set = true;
     if (ctx->ready) return buildTiles(ctx);
     return KGB_OK;
   }
   if (!std::strcmp(key, "sweep_tile_xy")) {
     if (value != 44 && value != 42 && value != 22) return fail(ctx, KGB_ERR_ARG, "sweep_tile_xy must be 44, 42 or 22");
+    ctx->tiles_set = true;
     ctx->tx = (int)(value / 10);
     ctx->ty = (int)(value % 10);
     if (ctx->ready) return buildTiles(ctx);
@@ -2299,6 +2346,9 @@ int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_
   ctx->timing = false;
   float best = 1e30f;
   int bxy = 44, btz = 4;
+  // the sweep variant the solver runs: fused population partials unless the FP64
+  // count comes from the next iteration's moments
+  const bool pop = !lagPopulation(ctx);
   for (int xy : xys)
     for (int tz : tzs) {
       if (tz > 2 * ctx->nzs && tz != 2) continue;
@@ -2306,10 +2356,10 @@ int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_
       ctx->ty = xy % 10;
       ctx->tz = tz;
       if ((rc = buildTiles(ctx))) break;
-      if ((rc = sweepSolver(ctx, true))) break;  // warm-up
+      if ((rc = sweepSolver(ctx, pop))) break;  // warm-up
       CK(cudaEventRecord(e0, ctx->stream));
       for (int r = 0; r < 2; ++r)
-        if ((rc = sweepSolver(ctx, true))) break;
+        if ((rc = sweepSolver(ctx, pop))) break;
       CK(cudaEventRecord(e1, ctx->stream));
       CK(cudaEventSynchronize(e1));
       float ms = 0.f;

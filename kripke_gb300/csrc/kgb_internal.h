@@ -72,6 +72,18 @@ constexpr int kSweepThreads = 128;
 template <typename T>
 void launch_sweep_step(const SweepArgs<T> &a, int ntiles, int nwave, cudaStream_t s);
 
+// Classes of the distinct sigt values for the sweep's reciprocal tables, on the
+// device: class_insert records every distinct bit pattern of sig in an
+// open-addressing table of 2^kClassTableBits 64-bit keys (kClassEmpty = free;
+// *overflow is set when a value cannot be recorded), class_lookup gives each
+// element the index of its value in the sorted distinct values.
+constexpr int kClassTableBits = 17;
+constexpr unsigned long long kClassEmpty = ~0ull;
+template <typename T>
+void launch_class_insert(const T *sig, int64_t n, unsigned long long *table, int *overflow, cudaStream_t s);
+template <typename T>
+void launch_class_lookup(const T *sig, int64_t n, const T *uniq, int ncls, uint16_t *cls, cudaStream_t s);
+
 template <typename T>
 void launch_ltimes(const T *psi, T *phi, const T *ell_dm, int64_t rows, int D, int M, bool accumulate, cudaStream_t s);
 template <typename T>
@@ -113,6 +125,7 @@ struct TcArgs {
   int nm, m0, ks;
   int64_t zstride;
   int stages;            // A stages in shared memory: 2 (default, 0) or 1 (one K chunk per tile only)
+  int stage_out;         // 1: outputs of contiguous rows are staged in shared memory for wide stores
 };
 template <typename T>
 void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhalf, std::vector<uint16_t> &img,

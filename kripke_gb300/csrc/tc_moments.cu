@@ -30,29 +30,25 @@
 //
 // Shared-memory operand layout: K-major, no swizzle ("interleaved" core
 // matrices of 8 rows x 16 bytes; core matrices adjacent in K are LBO bytes
-// apart, adjacent 8-row groups SBO = 128 bytes apart).  One CTA per SM
-// (persistent over 128-row tiles) of 16 warps: four threads split each row
-// (one 8-element K group of every 32-element chunk each), and in the epilogue
-// warp w reads TMEM lane quarter w%4 (rows 32*(w%4)..) for column group w/4;
-// thread 0 issues the MMAs.  The
-// B image reaches shared memory with one cp.async.bulk.  Every mbarrier wait is
-// bounded; on timeout the CTA records the failure, releases its tensor memory
-// and returns.
+// apart, adjacent 8-row groups SBO = 128 bytes apart).  The kernel
+// (tc_pipe_kernel, below) is warp-specialised and persistent, one CTA per SM;
+// the B image reaches shared memory with one cp.async.bulk; every mbarrier
+// wait is bounded, and on timeout the CTA records the failure, releases its
+// tensor memory and returns.
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cstring>
 
 #include "kgb_internal.h"
+#include "exact_round.h"
 
 namespace kgb {
 
 namespace {
 
-constexpr int kTcThreads = 512;     // 16 warps: 4 threads per row while splitting
 constexpr int kTcRows = 128;            // rows per tile = MMA M
 constexpr int kTcChunk = 32;            // K elements staged per A buffer
-constexpr uint32_t kWaitLimit = 1u << 24;  // mbarrier polls before giving up
 
 __device__ __forceinline__ uint32_t smemAddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -79,18 +75,6 @@ __device__ __forceinline__ void mma(uint32_t tmem, uint64_t da, uint64_t db, uin
 
 __device__ __forceinline__ void commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smemAddr(bar)));
-}
-
-// Bounded wait for the phase with the given parity to complete.
-__device__ __forceinline__ bool waitParity(uint64_t *bar, uint32_t parity) {
-  uint32_t done = 0;
-  for (uint32_t it = 0; it < kWaitLimit && !done; ++it) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(done)
-        : "r"(smemAddr(bar)), "r"(parity));
-  }
-  return done != 0;
 }
 
 __device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&v)[8]) {
@@ -170,22 +154,10 @@ __device__ __forceinline__ float scale2(float x, int e) {
 
 // Combine the S diagonal sums (FP32, exact integers) into the output value.
 template <typename T, int S> struct Combine;
-// Exact double of sign*a*2^sh for 0 < a < 2^53, assembled from its bits (no
-// FP64 instruction); `ok` is cleared when the result is not a normal number.
-__device__ __forceinline__ double exactDouble(long long v, int sh, bool &ok) {
-  if (v == 0) return 0.0;
-  const unsigned long long sgn = v < 0 ? 1ull : 0ull;
-  const unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
-  const int p = 63 - __clzll((long long)a);
-  const int e = p + sh + 1023;
-  if (e < 1 || e > 2046) ok = false;
-  const unsigned long long mant = (a << (52 - p)) & 0xFFFFFFFFFFFFFull;
-  return __longlong_as_double((long long)((sgn << 63) | ((unsigned long long)(e & 0x7FF) << 52) | mant));
-}
-
 template <> struct Combine<double, 8> {
-  // value = (H*2^28 + L) * 2^(e0 - 63) with H, L below 2^47: both terms are
-  // exact doubles, so the one addition is the only rounding
+  // value = (H*2^28 + L) * 2^(e0 - 63) with H, L below 2^47, rounded once to
+  // nearest in integer arithmetic (roundScaled: bit for bit the sum of the two
+  // exact doubles H*2^(e0-35) + L*2^(e0-63), without the FP64 add)
   static __device__ __forceinline__ double value(const float (&dk)[8], int e0) {
     long long h = 0, l = 0;
 #pragma unroll
@@ -193,9 +165,8 @@ template <> struct Combine<double, 8> {
 #pragma unroll
     for (int k = 4; k < 8; ++k) l = l * 128 + (long long)__float2int_rn(dk[k]);
     bool ok = true;
-    const double hs = exactDouble(h, e0 - 35, ok);
-    const double ls = exactDouble(l, e0 - 63, ok);
-    if (ok) return hs + ls;
+    const double r = roundScaled(h, l, e0, ok);
+    if (ok) return r;
     return scale2(scale2((double)h, 28) + (double)l, e0 - 63);  // outside the normal range
   }
 };
@@ -211,9 +182,8 @@ struct CombineSmallK {
     const int32_t p45 = d[4] * 128 + d[5], p67 = d[6] * 128 + d[7];
     const long long h = (long long)p01 * 16384 + p23, l = (long long)p45 * 16384 + p67;
     bool ok = true;
-    const double hs = exactDouble(h, e0 - 35, ok);
-    const double ls = exactDouble(l, e0 - 63, ok);
-    if (ok) return hs + ls;
+    const double r = roundScaled(h, l, e0, ok);
+    if (ok) return r;
     return scale2(scale2((double)h, 28) + (double)l, e0 - 63);
   }
 };
@@ -231,270 +201,9 @@ template <typename T> struct TcBias;
 template <> struct TcBias<double> { static constexpr int v = 1022; };
 template <> struct TcBias<float> { static constexpr int v = 126; };
 
-// GATHER: rows are (zone, moment) pairs of the device nesting [zone][group][moment]
+// GATHER (tc_pipe_kernel): rows are (zone, moment) pairs of the device nesting [zone][group][moment]
 // (the scattering's operand): row r is zone zl[r / nm], moment m0 + r % nm, and
 // its element k (A) or n (C) lies ks elements after the row's base.
-template <typename T, int S, int NB, bool MULTI_N, bool GATHER>
-__global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> a) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  __shared__ uint64_t bars[3];  // 0,1: A buffers (MMA done), 2: B image load / per-block MMA done
-  __shared__ uint32_t tmem_slot;
-  __shared__ int row_emax[kTcRows];
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // split phase: 4 threads per row, part p owns the 8-element K group p of every 32-element chunk
-  const int srow = warp * 8 + (lane & 7);
-  const int part = lane >> 3;
-  // epilogue phase: warp w reads TMEM lane quarter w%4 and column group w/4
-  const int erow = (warp & 3) * 32 + lane;
-  const int cgrp = warp >> 2;
-  constexpr int kCols = NB / 4;      // columns per epilogue column group
-  constexpr int kTmemCols = S * NB;  // power of two: 128, 256 or 512
-  constexpr uint32_t kSliceBytes = kTcChunk * kTcRows * 2;  // one digit slice of one chunk: 8 KB
-  constexpr uint32_t kBufBytes = S * kSliceBytes;
-  constexpr uint32_t kLboA = (kTcRows / 8) * 128;           // 2048: next 8-element K group
-  const uint32_t lboB = (uint32_t)S * NB * 16;               // [kc][S*NB rows] image: next K group
-  const uint32_t halfBytes = (uint32_t)a.kpad * S * NB * 2;  // B image of one N block
-
-  const uint32_t base = smemAddr(smem_raw);
-  unsigned char *al = smem_raw + (((base + 1023u) & ~1023u) - base);
-  unsigned char *sB = al;
-  unsigned char *sA = al + ((halfBytes * a.nhalf + 1023u) & ~1023u);
-  int *sT = reinterpret_cast<int *>(sA + (MULTI_N ? 1 : 2) * kBufBytes);
-
-  // --- set-up: barriers, tensor memory, B image (one bulk copy), column exponents ---
-  if (tid == 0) {
-    for (int i = 0; i < 3; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(&bars[i])), "r"(1));
-    asm volatile("fence.mbarrier_init.release.cluster;");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(&tmem_slot)),
-                 "r"(kTmemCols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  for (int i = tid; i < a.nhalf * NB; i += kTcThreads) sT[i] = a.bexp[i];
-  asm volatile("tcgen05.fence::before_thread_sync;");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  const uint32_t tmem = tmem_slot;
-  const uint32_t bbytes = halfBytes * a.nhalf;
-  if (tid == 0) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(&bars[2])), "r"(bbytes));
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smemAddr(sB)),
-                 "l"(a.bimg), "r"(bbytes), "r"(smemAddr(&bars[2])));
-  }
-  bool ok = __syncthreads_and(waitParity(&bars[2], 0));
-  uint32_t parity2 = 1;  // next phase of bars[2]
-  uint32_t uses[2] = {0, 0};
-
-  const int ntiles = (int)((a.rows + kTcRows - 1) / kTcRows);
-  const int nchunks = a.kpad / kTcChunk;
-  const bool vec = !GATHER && (a.lda * sizeof(T)) % 16 == 0;  // 16-byte loads of row segments
-  // element k of a row at its base + k * kstride
-  const int64_t kstride = GATHER ? a.ks : 1;
-  auto rowBase = [&](int64_t r) -> int64_t {
-    if constexpr (GATHER) {
-      const int64_t q = r / a.nm;
-      return (int64_t)a.zl[q] * a.zstride + a.m0 + (r - q * a.nm);
-    } else {
-      return r * a.lda;
-    }
-  };
-  uint32_t item = 0;
-  for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-    const int64_t row = (int64_t)tile * kTcRows + srow;
-    const bool valid = row < a.rows;
-    const T *arow = a.A + (valid ? rowBase(row) : 0);
-    // row exponent: largest biased exponent of the row, over the 4 threads of the row
-    int emax = 1;
-    if (valid) {
-      if (vec && a.K == a.kpad) {
-        // all of this thread's K groups at once (independent 16-byte loads; the row has kpad elements)
-#pragma unroll 4
-        for (int c = 0; c < nchunks; ++c) {
-          const T *p8 = arow + c * kTcChunk + part * 8;
-          if constexpr (sizeof(T) == 8) {
-            double2 v[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) v[e] = *reinterpret_cast<const double2 *>(p8 + 2 * e);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) emax = max(emax, max(expOf(v[e].x), expOf(v[e].y)));
-          } else {
-            float4 v[2];
-#pragma unroll
-            for (int e = 0; e < 2; ++e) v[e] = *reinterpret_cast<const float4 *>(p8 + 4 * e);
-#pragma unroll
-            for (int e = 0; e < 2; ++e)
-              emax = max(emax, max(max(expOf(v[e].x), expOf(v[e].y)), max(expOf(v[e].z), expOf(v[e].w))));
-          }
-        }
-      } else {
-        for (int c = 0; c < nchunks; ++c) {
-          const int k0 = c * kTcChunk + part * 8;
-#pragma unroll
-          for (int e = 0; e < 8; ++e)
-            if (k0 + e < a.K) emax = max(emax, expOf(arow[(k0 + e) * kstride]));
-        }
-      }
-    }
-    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 8));
-    emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 16));
-    if (part == 0) row_emax[srow] = emax;
-
-    // this thread's 8 elements of chunk c (zero beyond K or the last row)
-    auto loadChunk = [&](int c, T (&x)[8]) {
-      const int k0 = c * kTcChunk + part * 8;
-      if (valid && vec && k0 + 8 <= a.K) {
-        if constexpr (sizeof(T) == 8) {
-#pragma unroll
-          for (int e = 0; e < 8; e += 2) {
-            const double2 v = *reinterpret_cast<const double2 *>(arow + k0 + e);
-            x[e] = v.x;
-            x[e + 1] = v.y;
-          }
-        } else {
-#pragma unroll
-          for (int e = 0; e < 8; e += 4) {
-            const float4 v = *reinterpret_cast<const float4 *>(arow + k0 + e);
-            x[e] = v.x;
-            x[e + 1] = v.y;
-            x[e + 2] = v.z;
-            x[e + 3] = v.w;
-          }
-        }
-      } else {
-#pragma unroll
-        for (int e = 0; e < 8; ++e) x[e] = (valid && k0 + e < a.K) ? arow[(k0 + e) * kstride] : T(0);
-      }
-    };
-    T xn[8];
-    loadChunk(0, xn);
-
-    for (int c = 0; c < nchunks && ok; ++c, ++item) {
-      const int b = MULTI_N ? 0 : (int)(item & 1);
-      if (!MULTI_N && item >= 2) {  // the MMAs that last read this buffer must be done
-        ok = __syncthreads_and(waitParity(&bars[b], (uses[b] - 1) & 1) && ok);
-        if (!ok) break;
-      }
-      unsigned char *buf = sA + b * kBufBytes;
-      // this thread's 8 elements of the chunk (loaded one chunk ahead), split into S digit slices
-      T x[8];
-#pragma unroll
-      for (int e = 0; e < 8; ++e) x[e] = xn[e];
-      if (c + 1 < nchunks) loadChunk(c + 1, xn);
-      uint32_t w[S][4];
-#pragma unroll
-      for (int e = 0; e < 8; e += 2) {
-        uint32_t s0, s1;
-        const uint64_t f0 = Fixed<T, S>::mag(x[e], emax, s0);
-        const uint64_t f1 = Fixed<T, S>::mag(x[e + 1], emax, s1);
-        digitPairs<S>(f0, s0, f1, s1, w, e >> 1);
-      }
-      const uint32_t off = part * kLboA + (srow >> 3) * 128 + (srow & 7) * 16;
-#pragma unroll
-      for (int i = 0; i < S; ++i)
-        *reinterpret_cast<uint4 *>(buf + i * kSliceBytes + off) = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
-      asm volatile("fence.proxy.async.shared::cta;");
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      __syncthreads();
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      if (!MULTI_N && tid == 0) {
-        // accumulate this chunk: slice i against B slices 1..S+1-i, at diagonal offset (i-1)*NB
-#pragma unroll 1
-        for (int i = 1; i <= S; ++i) {
-          const int ncols = NB * (S + 1 - i);
-#pragma unroll 1
-          for (int ks = 0; ks < kTcChunk / 16; ++ks) {
-            const int kg = c * (kTcChunk / 16) + ks;  // global 16-element K step
-            const uint64_t da = matDesc(smemAddr(buf + (i - 1) * kSliceBytes + ks * 2 * kLboA), kLboA, 128);
-            for (int n0 = 0; n0 < ncols; n0 += 256) {
-              const int wd = min(256, ncols - n0);
-              const uint64_t db = matDesc(smemAddr(sB) + kg * 2 * lboB + (n0 / 8) * 128, lboB, 128);
-              // slice 1's first MMA initialises every diagonal block; all later ones accumulate
-              mma(tmem + (uint32_t)((i - 1) * NB + n0), da, db, instrDesc(wd), (c > 0 || ks > 0 || i > 1) ? 1u : 0u);
-            }
-          }
-        }
-        commit(&bars[b]);
-      }
-      if (!MULTI_N) uses[b]++;
-    }
-    if (!ok) break;
-
-    // --- epilogue(s): thread = (row erow, column group cgrp) ---
-    const int64_t orow = (int64_t)tile * kTcRows + erow;
-    const bool ovalid = orow < a.rows;
-    const int oemax = row_emax[erow] - TcBias<T>::v;
-    T *crow = a.C + (ovalid ? (GATHER ? rowBase(orow) : orow * a.ldc) : 0);
-    for (int hf = 0; hf < a.nhalf && ok; ++hf) {
-      if (MULTI_N) {
-        if (tid == 0) {
-          const unsigned char *bh = sB + hf * halfBytes;
-#pragma unroll 1
-          for (int i = 1; i <= S; ++i) {
-            const int ncols = NB * (S + 1 - i);
-#pragma unroll 1
-            for (int ks = 0; ks < a.kpad / 16; ++ks) {
-              const uint64_t da = matDesc(smemAddr(sA + (i - 1) * kSliceBytes + ks * 2 * kLboA), kLboA, 128);
-              for (int n0 = 0; n0 < ncols; n0 += 256) {
-                const int wd = min(256, ncols - n0);
-                const uint64_t db = matDesc(smemAddr(bh) + ks * 2 * lboB + (n0 / 8) * 128, lboB, 128);
-                mma(tmem + (uint32_t)((i - 1) * NB + n0), da, db, instrDesc(wd), (ks > 0 || i > 1) ? 1u : 0u);
-              }
-            }
-          }
-          commit(&bars[2]);
-        }
-        ok = __syncthreads_and(waitParity(&bars[2], parity2) && ok);
-        parity2 ^= 1;
-      } else {
-        const int b = (int)((item - 1) & 1);
-        ok = __syncthreads_and(waitParity(&bars[b], (uses[b] - 1) & 1) && ok);
-      }
-      if (!ok) break;
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t lanebase = (uint32_t)((warp & 3) * 32) << 16;
-#pragma unroll 1
-      for (int c0 = cgrp * kCols; c0 < (cgrp + 1) * kCols; c0 += 8) {
-        uint32_t v[S][8];
-#pragma unroll
-        for (int k = 0; k < S; ++k) ld8(tmem + lanebase + (uint32_t)(k * NB + c0), v[k]);
-        asm volatile("tcgen05.wait::ld.sync.aligned;");
-        T out[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int n = hf * NB + c0 + u;
-          float dk[S];
-#pragma unroll
-          for (int k = 0; k < S; ++k) dk[k] = __uint_as_float(v[k][u]);
-          out[u] = n < a.N ? Combine<T, S>::value(dk, oemax + sT[n]) : T(0);
-        }
-        if (ovalid) {
-          const int nb = hf * NB + c0;
-#pragma unroll
-          for (int u = 0; u < 8; ++u)
-            if (nb + u < a.N) {
-              T &dst = crow[(nb + u) * kstride];
-              dst = a.accumulate ? dst + out[u] : out[u];
-            }
-        }
-      }
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      __syncthreads();
-      asm volatile("tcgen05.fence::after_thread_sync;");
-    }
-  }
-  if (!ok && tid == 0) atomicExch(a.err, 1);
-  // drain: let any committed MMAs finish (bounded) before the tensor memory is released
-  if (!MULTI_N && tid == 0 && ok) {
-    for (int b = 0; b < 2; ++b)
-      if (uses[b] > 0) waitParity(&bars[b], (uses[b] - 1) & 1);
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;");
-  __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
-}
-
 // ---------------------------------------------------------------------------
 // Pipelined row products (the production kernel).
 //
@@ -514,6 +223,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_rows_kernel(const TcArgs<T> 
 constexpr int kPipeWorkers = 16;                       // worker warps
 constexpr int kPipeThreads = (kPipeWorkers + 1) * 32;  // + the MMA warp
 constexpr int kPipeNB = 32;                            // columns per N block
+constexpr int kStagePitch = 5;                         // staged outputs per row: 4 columns + 1 pad
 
 __device__ __forceinline__ uint64_t nowNs() {
   uint64_t t;
@@ -578,6 +288,8 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
   unsigned char *sB = al;
   unsigned char *sA = al + ((blkBytes * nb + 1023u) & ~1023u);
   int *sT = reinterpret_cast<int *>(sA + R * kBufBytes);
+  // per-warp staging of finished outputs (contiguous rows only): [32 rows][kStagePitch]
+  T *sStage = reinterpret_cast<T *>(sT + nb * NB) + warp * (32 * kStagePitch);
 
   if (tid == 0) {
     for (int i = 0; i < 2; ++i) {
@@ -650,23 +362,57 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncwarp();
         if (lane == 0) arriveBar(&accempty[st]);  // the accumulator is in registers: release it
-        if (ovalid) {
+        auto combined = [&](int u, int n) -> T {
+          float dk[S];
+#pragma unroll
+          for (int k = 0; k < S; ++k) dk[k] = __uint_as_float(v[k][u]);
+          if constexpr (sizeof(T) == 8) {
+            return smallk ? CombineSmallK::value(dk, oemax + sT[n]) : Combine<T, S>::value(dk, oemax + sT[n]);
+          } else {
+            return Combine<T, S>::value(dk, oemax + sT[n]);
+          }
+        };
+        if (GATHER || !a.stage_out) {
+          if (ovalid) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int n = j * NB + cgrp * 8 + u;
+              if (n < a.N) {
+                const T out = combined(u, n);
+                T &dst = crow[(int64_t)n * kstride];
+                dst = a.accumulate ? dst + out : out;
+              }
+            }
+          }
+        } else {
+          // A lane holds 8 columns of one row; stored as they are, every store
+          // instruction would touch 32 rows.  Staged through shared memory,
+          // four columns at a time, each instruction writes 8 rows x 4
+          // consecutive columns.
+          T out[8];
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
             const int n = j * NB + cgrp * 8 + u;
-            if (n < a.N) {
-              float dk[S];
+            out[u] = (ovalid && n < a.N) ? combined(u, n) : T(0);
+          }
+          const int64_t rbase = (int64_t)tile * kTcRows + (warp & 3) * 32;
 #pragma unroll
-              for (int k = 0; k < S; ++k) dk[k] = __uint_as_float(v[k][u]);
-              T out;
-              if constexpr (sizeof(T) == 8) {
-                out = smallk ? CombineSmallK::value(dk, oemax + sT[n]) : Combine<T, S>::value(dk, oemax + sT[n]);
-              } else {
-                out = Combine<T, S>::value(dk, oemax + sT[n]);
+          for (int hh = 0; hh < 2; ++hh) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) sStage[lane * kStagePitch + u] = out[hh * 4 + u];
+            __syncwarp();
+            const int n = j * NB + cgrp * 8 + hh * 4 + (lane & 3);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const int rl = (lane >> 2) + 8 * i;
+              const int64_t orow2 = rbase + rl;
+              if (orow2 < a.rows && n < a.N) {
+                const T val = sStage[rl * kStagePitch + (lane & 3)];
+                T &dst = a.C[orow2 * a.ldc + n];
+                dst = a.accumulate ? dst + val : val;
               }
-              T &dst = crow[(int64_t)n * kstride];
-              dst = a.accumulate ? dst + out : out;
             }
+            __syncwarp();
           }
         }
       }
@@ -831,24 +577,12 @@ void launchPipe(const TcArgs<T> &a, cudaStream_t s) {
   const size_t blkBytes = (size_t)a.kpad * S * kPipeNB * 2;
   const size_t bufBytes = (size_t)S * kTcChunk * kTcRows * 2;
   const size_t smem = 1024 + ((blkBytes * a.nhalf + 1023) & ~(size_t)1023) + (a.stages == 1 ? 1 : 2) * bufBytes +
-                      sizeof(int) * a.nhalf * kPipeNB;
+                      sizeof(int) * a.nhalf * kPipeNB +
+                      (GATHER || !a.stage_out ? 0 : kPipeWorkers * 32 * kStagePitch * sizeof(T));
   cudaFuncSetAttribute(tc_pipe_kernel<T, S, GATHER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int64_t ntiles = (a.rows + kTcRows - 1) / kTcRows;
   const int grid = (int)(ntiles < a.nsm ? ntiles : a.nsm);
   tc_pipe_kernel<T, S, GATHER><<<grid, kPipeThreads, smem, s>>>(a);
-}
-
-template <typename T, int S, int NB, bool MULTI_N, bool GATHER = false>
-void launchRows(const TcArgs<T> &a, cudaStream_t s) {
-  const size_t halfBytes = (size_t)a.kpad * S * NB * 2;
-  const size_t bufBytes = (size_t)S * kTcChunk * kTcRows * 2;
-  const size_t smem = 1024 + ((halfBytes * a.nhalf + 1023) & ~(size_t)1023) + (MULTI_N ? 1 : 2) * bufBytes +
-                      sizeof(int) * a.nhalf * NB;
-  cudaFuncSetAttribute(tc_rows_kernel<T, S, NB, MULTI_N, GATHER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
-  const int64_t ntiles = (a.rows + kTcRows - 1) / kTcRows;
-  const int grid = (int)(ntiles < a.nsm ? ntiles : a.nsm);
-  tc_rows_kernel<T, S, NB, MULTI_N, GATHER><<<grid, kTcThreads, smem, s>>>(a);
 }
 
 }  // namespace

@@ -100,4 +100,93 @@ template void launch_download_xpose<float>(const float *, double *, const XposeD
 template void launch_fill<double>(double *, int64_t, double, cudaStream_t);
 template void launch_fill<float>(float *, int64_t, double, cudaStream_t);
 
+// ---------------------------------------------------------------------------
+// sigt classes for the sweep's tabulated reciprocals (set-up only)
+// ---------------------------------------------------------------------------
+namespace {
+template <typename T> struct KeyOf;
+template <> struct KeyOf<double> {
+  static __device__ __forceinline__ unsigned long long of(double v) { return (unsigned long long)__double_as_longlong(v); }
+};
+template <> struct KeyOf<float> {
+  static __device__ __forceinline__ unsigned long long of(float v) { return (unsigned long long)__float_as_uint(v); }
+};
+
+// splitmix64 finaliser
+__device__ __forceinline__ unsigned int hashKey(unsigned long long k) {
+  k ^= k >> 30;
+  k *= 0xbf58476d1ce4e5b9ull;
+  k ^= k >> 27;
+  k *= 0x94d049bb133111ebull;
+  k ^= k >> 31;
+  return (unsigned int)k;
+}
+
+// Every element probes at most the whole table (no waiting on other threads);
+// a key already present is found by a plain load, so the atomics touch only
+// the first arrival of each distinct value.
+template <typename T>
+__global__ void class_insert_kernel(const T *__restrict__ sig, int64_t n, unsigned long long *table, int *overflow) {
+  constexpr unsigned int mask = (1u << kClassTableBits) - 1u;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long key = KeyOf<T>::of(sig[e]);
+    if (key == kClassEmpty) {
+      *overflow = 1;
+      continue;
+    }
+    unsigned int h = hashKey(key) & mask;
+    bool placed = false;
+    for (unsigned int probe = 0; probe <= mask; ++probe, h = (h + 1u) & mask) {
+      const unsigned long long cur = __ldcg(table + h);
+      if (cur == key) {
+        placed = true;
+        break;
+      }
+      if (cur == kClassEmpty) {
+        const unsigned long long prev = atomicCAS(table + h, kClassEmpty, key);
+        if (prev == kClassEmpty || prev == key) {
+          placed = true;
+          break;
+        }
+      }
+    }
+    if (!placed) *overflow = 1;
+  }
+}
+
+// lower bound of sig[e] among the ncls sorted distinct values
+template <typename T>
+__global__ void class_lookup_kernel(const T *__restrict__ sig, int64_t n, const T *__restrict__ uniq, int ncls,
+                                    uint16_t *__restrict__ cls) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const T v = sig[e];
+    int lo = 0, hi = ncls;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (uniq[mid] < v) lo = mid + 1;
+      else hi = mid;
+    }
+    cls[e] = (uint16_t)lo;
+  }
+}
+
+int setupGrid(int64_t n) {
+  const int64_t b = (n + 255) / 256;
+  return (int)(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
+}
+}  // namespace
+
+template <typename T>
+void launch_class_insert(const T *sig, int64_t n, unsigned long long *table, int *overflow, cudaStream_t s) {
+  class_insert_kernel<T><<<setupGrid(n), 256, 0, s>>>(sig, n, table, overflow);
+}
+template <typename T>
+void launch_class_lookup(const T *sig, int64_t n, const T *uniq, int ncls, uint16_t *cls, cudaStream_t s) {
+  class_lookup_kernel<T><<<setupGrid(n), 256, 0, s>>>(sig, n, uniq, ncls, cls);
+}
+template void launch_class_insert<double>(const double *, int64_t, unsigned long long *, int *, cudaStream_t);
+template void launch_class_insert<float>(const float *, int64_t, unsigned long long *, int *, cudaStream_t);
+template void launch_class_lookup<double>(const double *, int64_t, const double *, int, uint16_t *, cudaStream_t);
+template void launch_class_lookup<float>(const float *, int64_t, const float *, int, uint16_t *, cudaStream_t);
+
 }  // namespace kgb
