@@ -1,9 +1,9 @@
 // exact_round.h -- correctly rounded double of an exact integer combination,
 // in integer arithmetic only.
 //
-// The tensor-core digit products end with v = h * 2^28 + l, an exact integer
-// (|h|, |l| < 2^47), to be scaled by 2^(e0 - 63) and rounded once to the
-// nearest double (ties to even).  Splitting v into two exact doubles and
+// The tensor-core digit products end with v = h * 2^32 + l, an exact integer
+// (|h| < 2^41, |l| < 2^49), to be scaled by a power of two and rounded once to
+// the nearest double (ties to even).  Splitting v into two exact doubles and
 // adding them rounds correctly too, but costs an FP64 add per output, which
 // GB300 issues at 1/64 of its integer rate; here the 128-bit value is
 // normalised and rounded with 64-bit integer operations.  Host and device
@@ -40,28 +40,30 @@ KGB_HD double bitsToDouble(uint64_t b) {
 #endif
 }
 
-// (h * 2^28 + l) * 2^(e0 - 63) rounded to nearest, ties to even, for
-// |h|, |l| < 2^62.  `ok` is cleared (and 0 returned) when the result is not a
-// normal double; the caller then takes a slower path.
-KGB_HD double roundScaled(int64_t h, int64_t l, int e0, bool &ok) {
+// (h * 2^SHIFT + l) * 2^scale rounded to nearest, ties to even, for
+// |h| < 2^(63 - SHIFT), |l| < 2^62.  `ok` is cleared (and 0 returned) when the
+// result is not a normal double; the caller then takes a slower path.
+template <int SHIFT>
+KGB_HD double roundScaled(int64_t h, int64_t l, int scale, bool &ok) {
+  static_assert(SHIFT > 0 && SHIFT < 64, "shift of the high part");
   // v as a 128-bit two's-complement pair (hi, lo)
-  const uint64_t hl = (uint64_t)h << 28;
+  const uint64_t hl = (uint64_t)h << SHIFT;
   uint64_t lo = hl + (uint64_t)l;
-  int64_t hi = (h >> 36) + (l >> 63) + (lo < hl ? 1 : 0);
+  int64_t hi = (h >> (64 - SHIFT)) + (l >> 63) + (lo < hl ? 1 : 0);
   if (hi == 0 && lo == 0) return 0.0;
   const bool neg = hi < 0;
   if (neg) {  // magnitude
     lo = ~lo + 1u;
     hi = ~hi + (lo == 0 ? 1 : 0);
   }
-  const uint64_t uh = (uint64_t)hi;  // below 2^14
+  const uint64_t uh = (uint64_t)hi;
   int p = uh ? 127 - clz64(uh) : 63 - clz64(lo);  // leading bit
   uint64_t mant;
   if (p <= 52) {
     mant = lo << (52 - p);
   } else {
-    const int sh = p - 52;  // 1 .. 77
-    mant = (lo >> sh) | (uh << (64 - sh));
+    const int sh = p - 52;  // below 64 for the stated ranges
+    mant = (lo >> sh) | (sh == 0 ? 0u : uh << (64 - sh));
     const uint64_t rem = lo & ((1ull << sh) - 1u), half = 1ull << (sh - 1);
     if (rem > half || (rem == half && (mant & 1u))) ++mant;
     if (mant >> 53) {
@@ -69,7 +71,7 @@ KGB_HD double roundScaled(int64_t h, int64_t l, int e0, bool &ok) {
       ++p;
     }
   }
-  const int e = p + e0 - 63 + 1023;
+  const int e = p + scale + 1023;
   if (e < 1 || e > 2046) {
     ok = false;
     return 0.0;

@@ -599,7 +599,7 @@ int planTensorMomentsFrom(kgb_ctx *ctx, const std::vector<double> &lt_src, const
   *lt_ok = *lp_ok = false;
   if (!ctx->allow_tc) return KGB_OK;
   const bool f64 = sizeof(T) == 8;
-  const int S = f64 ? 8 : 4;
+  const int S = tcDigits<T>();
   const int D = ctx->D, M = ctx->M;
   auto upload = [&](uint16_t **img_d, int **exp_d, const std::vector<uint16_t> &img, const std::vector<int> &ex) {
     if (*img_d) cudaFree(*img_d);
@@ -618,11 +618,13 @@ int planTensorMomentsFrom(kgb_ctx *ctx, const std::vector<double> &lt_src, const
   std::vector<int> ex;
   int rc;
   // LTimes: B[d][m] = ell(m,d), K = D, N = M (one 32-wide block).  Exact diagonal
-  // sums hold for at most 128 (FP64) / 256 (mixed) directions, so larger D runs in
-  // K chunks of equal width kc (a multiple of 32), each with its own digit image,
-  // the chunk results added in the output precision.  *lt_kpad = kc.
+  // sums (at most S digit pairs of magnitude 128^2 per direction, below 2^24) hold
+  // for at most 128 directions, so larger D runs in K chunks of equal width kc (a
+  // multiple of 32), each with its own digit image, the chunk results added in the
+  // output precision.  *lt_kpad = kc.
   if (M <= 32) {
-    const int kmax = f64 ? 128 : 256;
+    const int kmax = 128;
+    static_assert(tcDigits<double>() * 128 * 128 * 128 < (1 << 24), "exact FP32 diagonal sums");
     const int nk = (D + kmax - 1) / kmax;
     const int kc = ((D + nk - 1) / nk + 31) / 32 * 32;
     std::vector<uint16_t> all;
@@ -674,7 +676,7 @@ int planTensorMoments(kgb_ctx *ctx) {
 template <typename T>
 int planTensorScatter(kgb_ctx *ctx) {
   ctx->tc_sc = false;
-  const int G = ctx->G, L1 = ctx->L + 1, S = sizeof(T) == 8 ? 8 : 4, NB = 32;
+  const int G = ctx->G, L1 = ctx->L + 1, S = tcDigits<T>(), NB = 32;
   if (!ctx->allow_tc_sc || G > 64) return KGB_OK;
   // zone lists from the device mixing tables
   std::vector<int> zs(ctx->Z), zc(ctx->Z), mm(std::max<int64_t>(ctx->nmix, 1));
@@ -1121,7 +1123,7 @@ void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, i
   a.nsm = ctx->nsm;
   a.stages = multi_n ? ctx->tc_lp_stages : 2;
   a.stage_out = multi_n ? ctx->tc_lp_stage_out : 1;  // LTimes' B image is at most 64 KB: staging fits
-  launch_tc_rows<T>(a, sizeof(T) == 8 ? 8 : 4, 0, multi_n, ctx->stream);
+  launch_tc_rows<T>(a, tcDigits<T>(), 0, multi_n, ctx->stream);
 }
 
 int doLTimes(kgb_ctx *ctx, bool acc) {
@@ -1129,7 +1131,7 @@ int doLTimes(kgb_ctx *ctx, bool acc) {
   const int64_t rows = ctx->Z * ctx->G;
   if (ctx->tc_lt && ctx->use_tc_lt) {
     // one launch per K chunk of kc directions (one chunk up to 128 FP64 / 256 FP32 directions)
-    const int kc = ctx->tc_lt_kpad, S = ctx->prec == KGB_FP64 ? 8 : 4;
+    const int kc = ctx->tc_lt_kpad, S = ctx->prec == KGB_FP64 ? tcDigits<double>() : tcDigits<float>();
     for (int k0 = 0, c = 0; k0 < ctx->D; k0 += kc, ++c) {
       const int K = std::min(kc, ctx->D - k0);
       const uint16_t *img = ctx->tc_lt_img + (size_t)c * kc * S * 32;
@@ -1184,7 +1186,7 @@ int ensureRhs(kgb_ctx *ctx) {
 
 template <typename T>
 int scatterTensor(kgb_ctx *ctx, bool acc) {
-  const int G = ctx->G, L1 = ctx->L + 1, S = sizeof(T) == 8 ? 8 : 4, kpad = ctx->tc_sc_kpad;
+  const int G = ctx->G, L1 = ctx->L + 1, S = tcDigits<T>(), kpad = ctx->tc_sc_kpad;
   for (int m = 0; m < 3; ++m) {
     const int64_t nz = ctx->pure_off[m + 1] - ctx->pure_off[m];
     if (nz == 0) continue;

@@ -127,6 +127,12 @@ struct TcArgs {
   int stages;            // A stages in shared memory: 2 (default, 0) or 1 (one K chunk per tile only)
   int stage_out;         // 1: outputs of contiguous rows are staged in shared memory for wide stores
 };
+// Digits per operand of the exact tensor-core products: 7 balanced 8-bit digits
+// (54 bits) for FP64, 4 (30 bits) for the FP32 of the mixed form.
+template <typename T>
+constexpr int tcDigits() {
+  return sizeof(T) == 8 ? 7 : 4;
+}
 template <typename T>
 void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhalf, std::vector<uint16_t> &img,
                 std::vector<int> &texp);

@@ -10,17 +10,18 @@
 // Exact products from bf16 digits (the Ozaki splitting, Ozaki et al. 2012,
 // "Error-free transformations of matrix multiplication by using fast
 // routines of matrix multiplication"): every A row is scaled by a power of two
-// taken from its largest element and written as S signed 7-bit digits,
-//   |A[r][k]| = 2^s_r * sum_i a_i * 2^-7i   (truncated after 7*S bits),
-// and every B column likewise with 2^t_n and digits b_j (done on the host).
-// A digit is an integer below 128, exact in bf16; a digit product is an
-// integer below 2^14, and for every anti-diagonal i+j the sum over k of the
-// products stays below 2^24, so tcgen05.mma with FP32 accumulation in tensor
+// taken from its largest element and written as S balanced 8-bit digits,
+//   |A[r][k]| = 2^s_r * sum_i a_i * 2^-8i   (truncated after 8S-2 bits),
+// a_i in [-128, 127] times the element's sign, and every B column likewise
+// with 2^t_n and digits b_j (done on the host).  A digit has at most 8
+// significant bits, so it is exact in bf16; a digit product is below 2^14 in
+// magnitude, and for every anti-diagonal i+j the sum over k <= 128 of at most
+// S products stays below 2^24, so tcgen05.mma with FP32 accumulation in tensor
 // memory computes each diagonal sum D_{i+j} exactly.  The diagonals are
-// recombined in integer arithmetic and scaled once:
-//   C = 2^(s_r + t_n) * sum_{k=2..S+1} D_k * 2^-7k.
-// Pairs with i+j > S+1 are dropped: their weight is below 2^-7(S+1) of the
-// leading term.  S = 8 (56 bits) gives the FP64 form, S = 4 (28 bits) the
+// recombined in integer arithmetic and rounded once:
+//   C = 2^(s_r + t_n) * sum_{m=2..S+1} D_m * 2^-8m.
+// Pairs with i+j > S+1 are dropped: their weight is below 2^-8(S+1) of the
+// leading term.  S = 7 (54 bits) gives the FP64 form, S = 4 (30 bits) the
 // mixed form.
 //
 // Tensor-memory layout: D_k occupies columns [(k-2)*NB, (k-1)*NB).  The B digit
@@ -83,28 +84,33 @@ __device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&v)[8]) {
                : "r"(taddr));
 }
 
-// The S 7-bit digits (most significant first) of two 7S-bit magnitudes as bf16
-// pairs: element 0 in the low half, element 1 in the high half, each with its
-// sign.  The magnitudes are cut into 28-bit words so every digit comes from
-// one 32-bit shift-and-mask; a digit d < 128 becomes the float d through the
-// 2^23 offset trick and two of them pack into bf16x2 exactly.
+// The S balanced 8-bit digits (most significant first) of two (8S-2)-bit
+// magnitudes as bf16 pairs: element 0 in the low half, element 1 in the high
+// half, each multiplied by its element's sign.  Adding 0x80 to every byte of
+// the magnitude (the carries ripple upward and stay inside its 8S bits,
+// since the magnitude is below 2^(8S-2))
+// turns byte b into the digit b - 128 in [-128, 127]; one byte permute places
+// b under the exponent of 2^23, a float add subtracts 2^23 + 128 exactly, and
+// two digits pack into bf16x2 exactly (|d| <= 128 has at most 8 significant
+// bits); a sign flip applies the element's sign.
 template <int S>
 __device__ __forceinline__ void digitPairs(uint64_t f0, uint32_t s0, uint64_t f1, uint32_t s1, uint32_t (&w)[S][4],
                                            int col) {
-  static_assert(S == 4 || S == 8, "7S-bit magnitudes of 28 or 56 bits");
+  static_assert(S == 4 || S == 7, "30-bit (FP32) or 54-bit (FP64) magnitudes");
+  constexpr uint64_t kBias = S == 7 ? 0x0080808080808080ull : 0x80808080ull;
   const uint32_t sg = (s0 << 15) | (s1 << 31);
-  uint32_t a[2], b[2];  // [0]: digits 0..3, [1]: digits 4..7
-  a[0] = (uint32_t)(f0 >> (S == 8 ? 28 : 0)) & 0x0FFFFFFFu;
-  b[0] = (uint32_t)(f1 >> (S == 8 ? 28 : 0)) & 0x0FFFFFFFu;
-  a[1] = (uint32_t)f0 & 0x0FFFFFFFu;
-  b[1] = (uint32_t)f1 & 0x0FFFFFFFu;
+  const uint64_t y0 = f0 + kBias, y1 = f1 + kBias;
+  const uint32_t lo0 = (uint32_t)y0, hi0 = (uint32_t)(y0 >> 32), lo1 = (uint32_t)y1, hi1 = (uint32_t)(y1 >> 32);
 #pragma unroll
   for (int i = 0; i < S; ++i) {
-    const int wd = i >> 2, sh = 7 * (3 - (i & 3));
-    const float v0 = __uint_as_float(0x4B000000u | ((a[wd] >> sh) & 127u)) - 8388608.0f;
-    const float v1 = __uint_as_float(0x4B000000u | ((b[wd] >> sh) & 127u)) - 8388608.0f;
+    const int byte = S - 1 - i;  // digit i is byte S-1-i of the biased magnitude
+    const uint32_t x0 = byte >= 4 ? hi0 : lo0, x1 = byte >= 4 ? hi1 : lo1;
+    // bytes: [b, 0, 0, 0x4B] = the float 2^23 + b
+    const uint32_t sel = (uint32_t)(byte & 3) | 0x7440u;
+    const float v0 = __uint_as_float(__byte_perm(x0, 0x4B000000u, sel)) - 8388736.0f;
+    const float v1 = __uint_as_float(__byte_perm(x1, 0x4B000000u, sel)) - 8388736.0f;
     const __nv_bfloat162 p = __floats2bfloat162_rn(v0, v1);
-    w[i][col] = *reinterpret_cast<const uint32_t *>(&p) | sg;
+    w[i][col] = *reinterpret_cast<const uint32_t *>(&p) ^ sg;
   }
 }
 
@@ -118,8 +124,9 @@ __device__ __forceinline__ int expOf(float x) {
   return e > 0 ? e : 1;
 }
 
-// Digit source: the 7*S-bit fixed-point magnitude of x relative to the row's
-// largest exponent emax, and its sign.
+// Digit source: the (8S-2)-bit fixed-point magnitude of x relative to the
+// row's largest exponent emax (the largest element's leading bit at 8S-3), and
+// its sign.
 template <typename T, int S> struct Fixed;
 template <int S> struct Fixed<double, S> {
   static __device__ __forceinline__ uint64_t mag(double x, int emax, uint32_t &sign) {
@@ -127,7 +134,7 @@ template <int S> struct Fixed<double, S> {
     sign = (uint32_t)(b >> 63);
     const int e = (int)((b >> 52) & 0x7FF);
     const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
-    const int sh = (e > 0 ? e : 1) - emax + (7 * S - 53);  // left shift; at most 7S-53
+    const int sh = (e > 0 ? e : 1) - emax + (8 * S - 2 - 53);  // left shift; at most 8S-55
     if (sh >= 0) return m << sh;
     return -sh >= 64 ? 0ull : m >> (-sh);
   }
@@ -138,7 +145,7 @@ template <int S> struct Fixed<float, S> {
     sign = b >> 31;
     const int e = (int)((b >> 23) & 0xFF);
     const uint64_t m = (uint64_t)((b & 0x7FFFFFu) | (e ? (1u << 23) : 0u));
-    const int sh = (e > 0 ? e : 1) - emax + (7 * S - 24);
+    const int sh = (e > 0 ? e : 1) - emax + (8 * S - 2 - 24);
     if (sh >= 0) return m << sh;
     return -sh >= 64 ? 0ull : m >> (-sh);
   }
@@ -153,47 +160,53 @@ __device__ __forceinline__ float scale2(float x, int e) {
 }
 
 // Combine the S diagonal sums (FP32, exact integers) into the output value.
+// With A = 2^(emax-1076) sum_i a_i 2^(8(7-i)) and B likewise (FP64, S = 7),
+// the kept diagonals D_m (m = i+j = 2..8) give
+//   C = 2^(e0-60) * V,  V = sum_m D_m 2^(8(8-m)) = H*2^32 + L,
+//   H = D2*2^16 + D3*2^8 + D4,  L = D5*2^24 + D6*2^16 + D7*2^8 + D8,
+// with e0 = (emax - 1022) + (column exponent - 1022).
 template <typename T, int S> struct Combine;
-template <> struct Combine<double, 8> {
-  // value = (H*2^28 + L) * 2^(e0 - 63) with H, L below 2^47, rounded once to
-  // nearest in integer arithmetic (roundScaled: bit for bit the sum of the two
-  // exact doubles H*2^(e0-35) + L*2^(e0-63), without the FP64 add)
-  static __device__ __forceinline__ double value(const float (&dk)[8], int e0) {
-    long long h = 0, l = 0;
+template <> struct Combine<double, 7> {
+  // V rounded once to nearest in integer arithmetic (roundScaled: bit for bit
+  // the sum of the two exact doubles H*2^(e0-28) + L*2^(e0-60), without the FP64 add)
+  static __device__ __forceinline__ double value(const float (&dk)[7], int e0) {
+    long long d[7];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) h = h * 128 + (long long)__float2int_rn(dk[k]);
-#pragma unroll
-    for (int k = 4; k < 8; ++k) l = l * 128 + (long long)__float2int_rn(dk[k]);
+    for (int k = 0; k < 7; ++k) d[k] = (long long)__float2int_rn(dk[k]);
+    const long long h = (d[0] * 256 + d[1]) * 256 + d[2];
+    const long long l = ((d[3] * 256 + d[4]) * 256 + d[5]) * 256 + d[6];
     bool ok = true;
-    const double r = roundScaled(h, l, e0, ok);
+    const double r = roundScaled<32>(h, l, e0 - 60, ok);
     if (ok) return r;
-    return scale2(scale2((double)h, 28) + (double)l, e0 - 63);  // outside the normal range
+    return scale2(scale2((double)h, 32) + (double)l, e0 - 60);  // outside the normal range
   }
 };
-// The same for one K chunk (K <= 32): every diagonal sum is below 8*32*127^2 <
+// The same for one K chunk (K <= 32): every diagonal sum is below 7*32*128^2 <
 // 2^22, so each converts to an integer by the 1.5 * 2^23 offset (a float add)
 // instead of a conversion instruction, and digit pairs combine in 32 bits.
 struct CombineSmallK {
-  static __device__ __forceinline__ double value(const float (&dk)[8], int e0) {
-    int32_t d[8];
+  static __device__ __forceinline__ double value(const float (&dk)[7], int e0) {
+    int32_t d[7];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) d[k] = __float_as_int(dk[k] + 12582912.0f) - 0x4B400000;
-    const int32_t p01 = d[0] * 128 + d[1], p23 = d[2] * 128 + d[3];
-    const int32_t p45 = d[4] * 128 + d[5], p67 = d[6] * 128 + d[7];
-    const long long h = (long long)p01 * 16384 + p23, l = (long long)p45 * 16384 + p67;
+    for (int k = 0; k < 7; ++k) d[k] = __float_as_int(dk[k] + 12582912.0f) - 0x4B400000;
+    const int32_t p01 = d[0] * 256 + d[1], p34 = d[3] * 256 + d[4], p56 = d[5] * 256 + d[6];
+    const long long h = (long long)p01 * 256 + d[2], l = (long long)p34 * 65536 + p56;
     bool ok = true;
-    const double r = roundScaled(h, l, e0, ok);
+    const double r = roundScaled<32>(h, l, e0 - 60, ok);
     if (ok) return r;
-    return scale2(scale2((double)h, 28) + (double)l, e0 - 63);
+    return scale2(scale2((double)h, 32) + (double)l, e0 - 60);
   }
 };
 
+// FP32 (S = 4): A = 2^(emax-156) sum_i a_i 2^(8(4-i)), B = 2^(t-1052) sum_j
+// b_j 2^(8(4-j)) (B from doubles), kept diagonals m = 2..5:
+//   C = 2^(e0-36) * sum_m D_m 2^(8(5-m)),  e0 = (emax - 126) + (t - 1022).
 template <> struct Combine<float, 4> {
   static __device__ __forceinline__ float value(const float (&dk)[4], int e0) {
     long long x = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) x = x * 128 + (long long)__float2int_rn(dk[k]);
-    return scale2((float)x, e0 - 35);
+    for (int k = 0; k < 4; ++k) x = x * 256 + (long long)__float2int_rn(dk[k]);
+    return scale2((float)x, e0 - 36);
   }
 };
 
@@ -275,7 +288,9 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
   constexpr uint32_t kBufBytes = S * kSliceBytes;
   constexpr uint32_t kLboA = (kTcRows / 8) * 128;
   constexpr uint32_t kAccCols = S * NB;             // one accumulator
-  constexpr uint32_t kTmemCols = 2 * kAccCols;      // 512 (FP64) or 256 (mixed)
+  // tensor memory is allocated in powers of two: 2 x 224 columns (FP64) take 512
+  constexpr uint32_t kTmemCols = 2 * kAccCols <= 256 ? 256u : 512u;
+  static_assert(2 * kAccCols <= 512, "two accumulators must fit tensor memory");
   const uint32_t lboB = (uint32_t)S * NB * 16;
   const uint32_t blkBytes = (uint32_t)a.kpad * S * NB * 2;  // B image of one N block
   const int nchunks = a.kpad / kTcChunk;
@@ -593,10 +608,11 @@ void launchPipe(const TcArgs<T> &a, cudaStream_t s) {
 template <typename T>
 void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhalf, std::vector<uint16_t> &img,
                 std::vector<int> &texp) {
-  const int W = 7 * S;
-  const int bias = sizeof(T) == 8 ? 1022 : 126;
+  const int W = 8 * S - 2;  // fixed-point bits: below 2^(8S-2), so adding 0x80 per byte cannot carry out
   img.assign((size_t)nhalf * kpad * S * NB, 0);
   texp.assign((size_t)nhalf * NB, 0);
+  uint64_t bias = 0;
+  for (int j = 0; j < S; ++j) bias |= 0x80ull << (8 * j);
   for (int n = 0; n < N; ++n) {
     int emax = 1;
     for (int k = 0; k < K; ++k) {
@@ -606,25 +622,25 @@ void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhal
       const int e = (int)((bits >> 52) & 0x7FF);
       emax = std::max(emax, e > 0 ? e : 1);
     }
-    // column exponent in the output precision's convention: |B| < 2^(emax-1022)
+    // column exponent: |B| < 2^(emax-1022)
     texp[n] = emax - 1022;
-    (void)bias;
     const int h = n / NB, nl = n % NB;
     for (int k = 0; k < K; ++k) {
       const double x = b[(size_t)k * N + n];
       uint64_t bits;
       std::memcpy(&bits, &x, 8);
-      const uint32_t sign = (uint32_t)(bits >> 63);
+      const bool neg = (bits >> 63) != 0;
       const int e = (int)((bits >> 52) & 0x7FF);
       const uint64_t m = (bits & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
       const int sh = (e > 0 ? e : 1) - emax + (W - 53);
       const uint64_t f = sh >= 0 ? (m << sh) : (-sh >= 64 ? 0ull : (m >> (-sh)));
+      const uint64_t y = f + bias;  // balanced digits: byte - 128
       for (int j = 1; j <= S; ++j) {
-        const uint32_t dg = (uint32_t)(f >> (7 * (S - j))) & 127u;
-        float fv = (float)dg;
+        const int dg = (int)((y >> (8 * (S - j))) & 0xFFu) - 128;
+        const float fv = (float)(neg ? -dg : dg);  // |dg| <= 128: exact in bf16
         uint32_t fb;
         std::memcpy(&fb, &fv, 4);
-        const uint16_t bf = (uint16_t)((fb >> 16) | (sign << 15));
+        const uint16_t bf = (uint16_t)(fb >> 16);
         const int rowi = (j - 1) * NB + nl;
         const size_t off = (size_t)h * kpad * S * NB + (size_t)(k / 8) * (S * NB * 8) + (size_t)(rowi / 8) * 64 +
                            (size_t)(rowi % 8) * 8 + (k % 8);
@@ -637,8 +653,7 @@ void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhal
 template <typename T>
 void launch_tc_rows(const TcArgs<T> &a, int S, int NB, bool multi_n, cudaStream_t s) {
   // the pipelined kernel covers both shapes (N blocks of 32 columns)
-  if constexpr (sizeof(T) == 8) launchPipe<T, 8, false>(a, s);
-  else launchPipe<T, 4, false>(a, s);
+  launchPipe<T, tcDigits<T>(), false>(a, s);
   (void)S;
   (void)NB;
   (void)multi_n;
@@ -648,8 +663,7 @@ void launch_tc_rows(const TcArgs<T> &a, int S, int NB, bool multi_n, cudaStream_
 // gathered as (zone, moment) pairs, B = the material's order-l matrix transposed.
 template <typename T>
 void launch_tc_gather(const TcArgs<T> &a, cudaStream_t s) {
-  if constexpr (sizeof(T) == 8) launchPipe<T, 8, true>(a, s);
-  else launchPipe<T, 4, true>(a, s);
+  launchPipe<T, tcDigits<T>(), true>(a, s);
 }
 
 template void tc_build_b<double>(const double *, int, int, int, int, int, int, std::vector<uint16_t> &, std::vector<int> &);
