@@ -276,7 +276,7 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
                                  "error of moment 0" % MIXED_PHI_ITERS,
            "autotuned": tuned,
            "kernels": {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "moments_tensor_ltimes",
-                                                      "moments_tensor_lplustimes")},
+                                                      "moments_tensor_lplustimes", "scattering_tensor_active")},
            "fused_sweep": {"ms_per_step": ms_fused, "value": unknowns(w) / (ms_fused * 1e-3),
                            "speedup_vs_unfused": ms / ms_fused, "active": fused_active,
                            "identical_to_unfused": fused_same,
@@ -418,7 +418,7 @@ def run_gpu(args, world, rank, local):
     ctx.iterate(want_population=False)
     tuned = ctx.autotune() if not args.no_autotune else None
     active = {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "sweep_reciprocals_active",
-                                             "moments_tensor_ltimes", "moments_tensor_lplustimes")}
+                                             "moments_tensor_ltimes", "moments_tensor_lplustimes", "scattering_tensor_active")}
 
     # warm-up (the solve starts from psi = 0, like SteadyStateSolver)
     ctx.fill("psi", 0.0)
