@@ -176,7 +176,7 @@ template <> struct Combine<double, 7> {
     const long long h = (d[0] * 256 + d[1]) * 256 + d[2];
     const long long l = ((d[3] * 256 + d[4]) * 256 + d[5]) * 256 + d[6];
     bool ok = true;
-    const double r = roundScaled<32>(h, l, e0 - 60, ok);
+    const double r = roundScaled32(h, l, e0 - 60, ok);
     if (ok) return r;
     return scale2(scale2((double)h, 32) + (double)l, e0 - 60);  // outside the normal range
   }
@@ -192,7 +192,7 @@ struct CombineSmallK {
     const int32_t p01 = d[0] * 256 + d[1], p34 = d[3] * 256 + d[4], p56 = d[5] * 256 + d[6];
     const long long h = (long long)p01 * 256 + d[2], l = (long long)p34 * 65536 + p56;
     bool ok = true;
-    const double r = roundScaled<32>(h, l, e0 - 60, ok);
+    const double r = roundScaled32(h, l, e0 - 60, ok);
     if (ok) return r;
     return scale2(scale2((double)h, 32) + (double)l, e0 - 60);
   }

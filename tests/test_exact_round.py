@@ -1,8 +1,9 @@
 """The tensor-core combine's integer rounding (kripke_gb300/csrc/exact_round.h).
 
-roundScaled<SHIFT>(h, l, scale) must equal, bit for bit, the two-double sum
-h*2^(scale+SHIFT) + l*2^scale, both terms exact doubles, added once in IEEE
-round-to-nearest-even (the kernels use SHIFT = 32 with |h| < 2^41, |l| < 2^49).  The header compiles for the host too; this test builds
+roundScaled32(h, l, scale) must equal, bit for bit, the two-double sum
+h*2^(scale+32) + l*2^scale, both terms exact doubles, added once in IEEE
+round-to-nearest-even (the kernels pass |h| < 2^41, |l| < 2^49; the test also
+covers wider h, up to 2^52, where the significand lies in the high word alone).  The header compiles for the host too; this test builds
 a small driver with g++ and checks random and constructed cases (ties, carries
 across the 64-bit boundary, sign changes, mantissa overflow on rounding up).
 """
@@ -26,7 +27,7 @@ static int check(int64_t h, int64_t l, int e0, long long &n) {
   const double want = hs + ls;
   if (want != 0.0 && std::fabs(want) < 2.2250738585072014e-308) return 0;
   bool ok = true;
-  const double got = kgb::roundScaled<SHIFT>(h, l, e0, ok);
+  const double got = kgb::roundScaled32(h, l, e0, ok);
   ++n;
   uint64_t a, b;
   std::memcpy(&a, &got, 8);
@@ -76,7 +77,7 @@ static int run(int hbits, int lbits, long long &n) {
 
 int main() {
   long long n = 0;
-  int bad = run<32>(41, 49, n) + run<28>(47, 47, n);
+  int bad = run<32>(41, 49, n) + run<32>(52, 49, n) + run<32>(20, 49, n);
   std::printf("checked %lld mismatches %d\n", n, bad);
   return bad != 0;
 }
