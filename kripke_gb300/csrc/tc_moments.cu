@@ -438,6 +438,20 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
       const int64_t row = (int64_t)tile * kTcRows + srow;
       const bool valid = row < a.rows;
       const T *arow = a.A + (valid ? rowBase(row) : 0);
+      if constexpr (!GATHER) {
+        // the CTA's next tile of A rows (contiguous) into L2 while this one is split:
+        // its row-exponent pass then waits on L2 instead of DRAM
+        const int64_t r1 = (int64_t)(tile + gridDim.x) * kTcRows;
+        if (tid == 0 && r1 < a.rows) {
+          const int64_t nr = a.rows - r1 < kTcRows ? a.rows - r1 : kTcRows;
+          const T *p = a.A + r1 * a.lda;
+          // up to the last row's K-th element (A may be a K chunk inside wider rows),
+          // rounded down to whole 16-byte units: nothing past the operand is touched
+          const uint64_t bytes = ((uint64_t)((nr - 1) * a.lda + a.K) * sizeof(T)) & ~(uint64_t)15u;
+          if (((uintptr_t)p & 15u) == 0 && bytes > 0 && bytes < (1ull << 31))
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"((uint32_t)bytes) : "memory");
+        }
+      }
       int emax = 1;
       if (valid) {
         if (vec && a.K == a.kpad) {
