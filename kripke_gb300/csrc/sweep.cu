@@ -166,13 +166,23 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
     const T *__restrict__ rhs = a.rhs;
     T *__restrict__ psi = a.psi;
     const int kend = min(a.tz, a.nzs - kb);
-    // FP64: rhs of the next k-slice streams into shared memory (each thread its
-    // own slots) while this slice is swept, so a slice's first cell does not wait
-    // on DRAM (measured 34.0 -> 32.8 ms per 64^3 sweep; the FP32 sweep, bound by
-    // its chain latency rather than the FP64 pipe, ran slower with it)
-    constexpr bool PF = !FUSE && sizeof(T) == 8;
-    __shared__ T rbuf[PF ? 2 : 1][PF ? TX * TY : 1][kSweepThreads];
-    auto prefetchRhs = [&](int kk2, int buf) {
+    // FP64 per-step launches: the next k-slice's operands stream into shared
+    // memory (each thread its own slots) while this slice is swept, so a slice's
+    // first cell does not wait on memory (measured 34.0 -> 32.8 ms per 64^3 sweep
+    // with rhs alone; the FP32 sweep, bound by its chain latency rather than the
+    // FP64 pipe, ran slower with it; the persistent batched sweep instantiates
+    // both table variants in one kernel and keeps plain loads)
+    constexpr bool PF = !FUSE && !COH && sizeof(T) == 8;
+    // slots per slice: rhs of every cell, then, for footprints up to 4x2 (the
+    // buffers stay within 48 KB of static shared memory), the incoming j- and
+    // i-faces (faces written in an earlier launch only, not COH) and sigt when
+    // it is not tabulated
+    constexpr bool PFX = PF && TX * TY <= 8;
+    constexpr int kFaces = PFX && !COH ? TX + TY : 0, kSig = PFX && !RECIP ? TX * TY : 0;
+    constexpr int kSlots = TX * TY + kFaces + kSig;
+    __shared__ T rbuf[PF ? 2 : 1][PF ? kSlots : 1][kSweepThreads];
+    int cn[TY][TX];  // RECIP: the next slice's sigt classes, loaded a slice ahead
+    auto prefetchSlice = [&](int kk2, int buf) {
       const int kq2 = kb + kk2;
       const int k2 = skd > 0 ? kq2 : a.nzs - 1 - kq2;
       const int64_t zs2 = (int64_t)(sd.ko + k2) * a.ny;
@@ -181,18 +191,38 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
         const int64_t zrow2 = (zs2 + (sd.jo + jloc[jj])) * a.nx + sd.io;
 #pragma unroll
         for (int ii = 0; ii < TX; ++ii)
-          if (iv[ii] && jv[jj])
-            cpAsync(&rbuf[buf][jj * TX + ii][threadIdx.x], rhs + ((zrow2 + iloc[ii]) * a.G + g) * a.D + d);
+          if (iv[ii] && jv[jj]) {
+            const int64_t zg = (zrow2 + iloc[ii]) * a.G + g;
+            cpAsync(&rbuf[buf][jj * TX + ii][threadIdx.x], rhs + zg * a.D + d);
+            if constexpr (RECIP) cn[jj][ii] = a.cls[zg];
+            else if constexpr (kSig > 0) cpAsync(&rbuf[buf][TX * TY + kFaces + jj * TX + ii][threadIdx.x], a.sigt + zg);
+          }
+      }
+      if constexpr (kFaces > 0) {
+#pragma unroll
+        for (int ii = 0; ii < TX; ++ii)
+          if (iv[ii]) cpAsync(&rbuf[buf][TX * TY + ii][threadIdx.x], jpl + ((int64_t)k2 * a.nxs + iloc[ii]) * nchain + c);
+#pragma unroll
+        for (int jj = 0; jj < TY; ++jj)
+          if (jv[jj])
+            cpAsync(&rbuf[buf][TX * TY + TX + jj][threadIdx.x], ipl + ((int64_t)k2 * a.nys + jloc[jj]) * nchain + c);
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    if constexpr (PF) prefetchRhs(0, 0);
+    if constexpr (PF) prefetchSlice(0, 0);
     for (int kk = 0; kk < kend; ++kk) {
       const int kq = kb + kk;
       const int k = skd > 0 ? kq : a.nzs - 1 - kq;
+      int cc[TY][TX];  // RECIP: this slice's sigt classes
+      if constexpr (PF && RECIP) {
+#pragma unroll
+        for (int jj = 0; jj < TY; ++jj)
+#pragma unroll
+          for (int ii = 0; ii < TX; ++ii) cc[jj][ii] = cn[jj][ii];
+      }
       if constexpr (PF) {
         if (kk + 1 < kend) {
-          prefetchRhs(kk + 1, (kk + 1) & 1);
+          prefetchSlice(kk + 1, (kk + 1) & 1);
           asm volatile("cp.async.wait_group 1;" ::: "memory");  // this slice's copies have landed
         } else {
           asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -225,8 +255,15 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
             } else {
               rv[jj][ii] = rhs[(z * a.G + g) * a.D + d];
             }
-            if (RECIP) sv[jj][ii] = a.inv[(int64_t)a.cls[z * a.G + g] * a.D + d];
-            else sv[jj][ii] = a.sigt[z * a.G + g];
+            if constexpr (PF) {
+              if constexpr (RECIP) sv[jj][ii] = a.inv[(int64_t)cc[jj][ii] * a.D + d];
+              else if constexpr (kSig > 0) sv[jj][ii] = rbuf[kk & 1][TX * TY + kFaces + jj * TX + ii][threadIdx.x];
+              else sv[jj][ii] = a.sigt[z * a.G + g];
+            } else if (RECIP) {
+              sv[jj][ii] = a.inv[(int64_t)a.cls[z * a.G + g] * a.D + d];
+            } else {
+              sv[jj][ii] = a.sigt[z * a.G + g];
+            }
           } else {
             rv[jj][ii] = T(0);
             sv[jj][ii] = T(1);
@@ -235,13 +272,18 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
       }
       T fr[TX];
 #pragma unroll
-      for (int ii = 0; ii < TX; ++ii) fr[ii] = iv[ii] ? ldFace<COH>(jpl + ((int64_t)k * a.nxs + iloc[ii]) * nchain + c) : T(0);
+      for (int ii = 0; ii < TX; ++ii) {
+        if constexpr (kFaces > 0) fr[ii] = iv[ii] ? rbuf[kk & 1][TX * TY + ii][threadIdx.x] : T(0);
+        else fr[ii] = iv[ii] ? ldFace<COH>(jpl + ((int64_t)k * a.nxs + iloc[ii]) * nchain + c) : T(0);
+      }
 #pragma unroll
       for (int jj = 0; jj < TY; ++jj) {
         if (!jv[jj]) continue;
         const int j = jloc[jj];
         T *const lfp = ipl + ((int64_t)k * a.nys + j) * nchain + c;
-        T lf = ldFace<COH>(lfp);
+        T lf;
+        if constexpr (kFaces > 0) lf = rbuf[kk & 1][TX * TY + TX + jj][threadIdx.x];
+        else lf = ldFace<COH>(lfp);
         const int64_t zrow = (zslice + (sd.jo + j)) * a.nx + sd.io;
 #pragma unroll
         for (int ii = 0; ii < TX; ++ii) {
