@@ -323,7 +323,7 @@ int kgb_batch_profile(kgb_batch *b, double ms[5]);
 /* Kernels the batch has launched (graph replays included). */
 int kgb_batch_launch_count(kgb_batch *b, int64_t *out);
 
-/* Allocation-free population edit.  No counterpart in the reference: it/* Allocation-free population edit.  No counterpart in the reference: it
+/* Allocation-free population edit.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory at the point they
  * need the particle count -- code recorded into a CUDA graph, frameworks that
  * own all device memory through their own pool, latency-bound loops.  Same

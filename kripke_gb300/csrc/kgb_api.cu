@@ -598,7 +598,6 @@ int planTensorMomentsFrom(kgb_ctx *ctx, const std::vector<double> &lt_src, const
                           int **lp_exp, int *lp_nhalf) {
   *lt_ok = *lp_ok = false;
   if (!ctx->allow_tc) return KGB_OK;
-  const bool f64 = sizeof(T) == 8;
   const int S = tcDigits<T>();
   const int D = ctx->D, M = ctx->M;
   auto upload = [&](uint16_t **img_d, int **exp_d, const std::vector<uint16_t> &img, const std::vector<int> &ex) {
