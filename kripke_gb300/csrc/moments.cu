@@ -128,6 +128,50 @@ __device__ __forceinline__ void lplusRow(const T *__restrict__ src, const T *sel
   }
 }
 
+// LTimes, two rows per thread (FP32, whole 16-byte vectors, up to 28 moments):
+// every L vector read from shared memory feeds both rows, halving the
+// shared-memory traffic per multiply-add; each row's sums run in the same order
+// as above.  (LPlusTimes measured slower both paired and with 8 threads per
+// row: 6.0 -> 7.2 / 7.4 ms at 64^3.)
+template <typename T, int MB>
+__device__ __forceinline__ void ltimesRow2(const T *__restrict__ p0, const T *__restrict__ p1, const T *sell, int D,
+                                           T *o0, T *o1, int mc, bool accumulate) {
+  constexpr int V = Vec16<T>::n;
+  T a0[MB], a1[MB];
+#pragma unroll
+  for (int m = 0; m < MB; ++m) a0[m] = a1[m] = T(0);
+  for (int d0 = 0; d0 < D; d0 += V) {
+    T pv0[V], pv1[V];
+    load16(pv0, p0 + d0);
+    load16(pv1, p1 + d0);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+      const T *e = sell + (d0 + v) * MB;
+#pragma unroll
+      for (int m = 0; m < MB; m += V) {
+        T ev[V];
+        load16(ev, e + m);
+#pragma unroll
+        for (int u = 0; u < V; ++u) {
+          a0[m + u] += ev[u] * pv0[v];
+          a1[m + u] += ev[u] * pv1[v];
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < MB; ++m)
+    if (m < mc) {
+      o0[m] = accumulate ? o0[m] + a0[m] : a0[m];
+      o1[m] = accumulate ? o1[m] + a1[m] : a1[m];
+    }
+}
+
+template <typename T, int MB, bool VEC>
+constexpr bool pairRows() {
+  return sizeof(T) == 4 && VEC && MB <= 28;
+}
+
 template <typename T, int MB, bool VEC>
 __global__ void __launch_bounds__(kMomThreads) ltimes_kernel(const T *__restrict__ psi, T *__restrict__ phi,
                                                             const T *__restrict__ ell_dm, int64_t rows, int D,
@@ -136,8 +180,19 @@ __global__ void __launch_bounds__(kMomThreads) ltimes_kernel(const T *__restrict
   T *sell = reinterpret_cast<T *>(smem_raw);  // [D][MB]
   loadRows<T, MB>(sell, ell_dm, D, M, m0, mc);
   __syncthreads();
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x)
-    ltimesRow<T, MB, VEC>(psi + r * D, sell, D, phi + r * M + m0, mc, accumulate);
+  if constexpr (pairRows<T, MB, VEC>()) {
+    for (int64_t r = 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x); r < rows;
+         r += 2 * (int64_t)gridDim.x * blockDim.x) {
+      if (r + 1 < rows)
+        ltimesRow2<T, MB>(psi + r * D, psi + (r + 1) * D, sell, D, phi + r * M + m0, phi + (r + 1) * M + m0, mc,
+                          accumulate);
+      else
+        ltimesRow<T, MB, VEC>(psi + r * D, sell, D, phi + r * M + m0, mc, accumulate);
+    }
+  } else {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x)
+      ltimesRow<T, MB, VEC>(psi + r * D, sell, D, phi + r * M + m0, mc, accumulate);
+  }
 }
 
 template <typename T, int MB, bool VEC>
@@ -227,7 +282,8 @@ struct LTimesLaunch {
     const size_t smem = sizeof(T) * (size_t)D * MB;
     if (vec) {
       setSmem(ltimes_kernel<T, MB, true>, smem);
-      ltimes_kernel<T, MB, true><<<gridFor(rows), kMomThreads, smem, s>>>(psi, phi, ell, rows, D, M, 0, M, acc);
+      const int64_t units = pairRows<T, MB, true>() ? (rows + 1) / 2 : rows;
+      ltimes_kernel<T, MB, true><<<gridFor(units), kMomThreads, smem, s>>>(psi, phi, ell, rows, D, M, 0, M, acc);
     } else {
       setSmem(ltimes_kernel<T, MB, false>, smem);
       ltimes_kernel<T, MB, false><<<gridFor(rows), kMomThreads, smem, s>>>(psi, phi, ell, rows, D, M, 0, M, acc);
