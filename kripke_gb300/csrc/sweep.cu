@@ -107,9 +107,20 @@ __device__ __forceinline__ void cpAsync(T *dst, const T *src) {
 
 // One tile of one subdomain for one block of chains: tile is the index into
 // a.tiles, cb the chain block (chains cb*blockDim.x + threadIdx.x) of ncb.
-template <typename T, int TX, int TY, bool RECIP, bool POP, bool COH, bool FUSE = false>
+// Shared-memory slots per k-slice of the operand streaming (PFM 0: none,
+// 1: rhs only, 2: rhs, the incoming faces of per-step launches and sigt for
+// footprints up to 4x2, which keeps the buffers within 48 KB of static
+// shared memory); the buffers hold two slices.
+template <int TX, int TY, bool RECIP, bool COH, int PFM>
+constexpr int sweepSlots() {
+  return PFM == 0 ? 0
+                  : TX * TY + (PFM == 2 && TX * TY <= 8 && !COH ? TX + TY : 0) +
+                        (PFM == 2 && TX * TY <= 8 && !RECIP ? TX * TY : 0);
+}
+
+template <typename T, int TX, int TY, bool RECIP, bool POP, bool COH, bool FUSE = false, int PFM = 0>
 __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom, const int tile, const int cb,
-                                          const int ncb) {
+                                          const int ncb, T (*rbuf)[kSweepThreads] = nullptr) {
   const SdomDesc sd = a.sdoms[sdom];
   // the adjoint sweep (transposed operator) runs every direction in its reversed orientation
   const int sid = a.flip ? -sd.id : sd.id, sjd = a.flip ? -sd.jd : sd.jd, skd = a.flip ? -sd.kd : sd.kd;
@@ -166,21 +177,21 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
     const T *__restrict__ rhs = a.rhs;
     T *__restrict__ psi = a.psi;
     const int kend = min(a.tz, a.nzs - kb);
-    // FP64 per-step launches: the next k-slice's operands stream into shared
-    // memory (each thread its own slots) while this slice is swept, so a slice's
-    // first cell does not wait on memory (measured 34.0 -> 32.8 ms per 64^3 sweep
-    // with rhs alone; the FP32 sweep, bound by its chain latency rather than the
-    // FP64 pipe, ran slower with it; the persistent batched sweep instantiates
-    // both table variants in one kernel and keeps plain loads)
-    constexpr bool PF = !FUSE && !COH && sizeof(T) == 8;
-    // slots per slice: rhs of every cell, then, for footprints up to 4x2 (the
-    // buffers stay within 48 KB of static shared memory), the incoming j- and
-    // i-faces (faces written in an earlier launch only, not COH) and sigt when
-    // it is not tabulated
-    constexpr bool PFX = PF && TX * TY <= 8;
+    // FP64: the next k-slice's operands stream into shared memory (each thread
+    // its own slots, rbuf[2 * kSlots][threads] from the kernel) while this slice
+    // is swept, so a slice's first cell does not wait on memory (measured 34.0 ->
+    // 32.8 ms per 64^3 sweep with rhs alone, 32.1 with faces and sigt classes;
+    // the FP32 sweep, bound by its chain latency rather than the FP64 pipe, ran
+    // slower with it).  Faces only in per-step launches: in the persistent
+    // batched sweep a face address is rewritten by other SMs within the launch
+    // and must be read through L2.
+    static_assert(PFM == 0 || !FUSE, "the fused prologue forms rhs itself");
+    constexpr bool PF = PFM > 0;
+    constexpr bool PFX = PFM == 2 && TX * TY <= 8;
     constexpr int kFaces = PFX && !COH ? TX + TY : 0, kSig = PFX && !RECIP ? TX * TY : 0;
-    constexpr int kSlots = TX * TY + kFaces + kSig;
-    __shared__ T rbuf[PF ? 2 : 1][PF ? kSlots : 1][kSweepThreads];
+    constexpr int kSlots = sweepSlots<TX, TY, RECIP, COH, PFM>();
+    static_assert(kSlots == TX * TY + kFaces + kSig || !PF, "slot layout");
+    auto slot = [&](int buf, int i) -> T & { return rbuf[buf * kSlots + i][threadIdx.x]; };
     int cn[TY][TX];  // RECIP: the next slice's sigt classes, loaded a slice ahead
     auto prefetchSlice = [&](int kk2, int buf) {
       const int kq2 = kb + kk2;
@@ -193,19 +204,19 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
         for (int ii = 0; ii < TX; ++ii)
           if (iv[ii] && jv[jj]) {
             const int64_t zg = (zrow2 + iloc[ii]) * a.G + g;
-            cpAsync(&rbuf[buf][jj * TX + ii][threadIdx.x], rhs + zg * a.D + d);
+            cpAsync(&slot(buf, jj * TX + ii), rhs + zg * a.D + d);
             if constexpr (RECIP) cn[jj][ii] = a.cls[zg];
-            else if constexpr (kSig > 0) cpAsync(&rbuf[buf][TX * TY + kFaces + jj * TX + ii][threadIdx.x], a.sigt + zg);
+            else if constexpr (kSig > 0) cpAsync(&slot(buf, TX * TY + kFaces + jj * TX + ii), a.sigt + zg);
           }
       }
       if constexpr (kFaces > 0) {
 #pragma unroll
         for (int ii = 0; ii < TX; ++ii)
-          if (iv[ii]) cpAsync(&rbuf[buf][TX * TY + ii][threadIdx.x], jpl + ((int64_t)k2 * a.nxs + iloc[ii]) * nchain + c);
+          if (iv[ii]) cpAsync(&slot(buf, TX * TY + ii), jpl + ((int64_t)k2 * a.nxs + iloc[ii]) * nchain + c);
 #pragma unroll
         for (int jj = 0; jj < TY; ++jj)
           if (jv[jj])
-            cpAsync(&rbuf[buf][TX * TY + TX + jj][threadIdx.x], ipl + ((int64_t)k2 * a.nys + jloc[jj]) * nchain + c);
+            cpAsync(&slot(buf, TX * TY + TX + jj), ipl + ((int64_t)k2 * a.nys + jloc[jj]) * nchain + c);
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
     };
@@ -251,13 +262,13 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
               for (int m = 0; m < kFuseMaxM; ++m) acc += ep[m] * __ldg(ph + min(m, mlast));
               rv[jj][ii] = acc;
             } else if constexpr (PF) {
-              rv[jj][ii] = rbuf[kk & 1][jj * TX + ii][threadIdx.x];
+              rv[jj][ii] = slot(kk & 1, jj * TX + ii);
             } else {
               rv[jj][ii] = rhs[(z * a.G + g) * a.D + d];
             }
             if constexpr (PF) {
               if constexpr (RECIP) sv[jj][ii] = a.inv[(int64_t)cc[jj][ii] * a.D + d];
-              else if constexpr (kSig > 0) sv[jj][ii] = rbuf[kk & 1][TX * TY + kFaces + jj * TX + ii][threadIdx.x];
+              else if constexpr (kSig > 0) sv[jj][ii] = slot(kk & 1, TX * TY + kFaces + jj * TX + ii);
               else sv[jj][ii] = a.sigt[z * a.G + g];
             } else if (RECIP) {
               sv[jj][ii] = a.inv[(int64_t)a.cls[z * a.G + g] * a.D + d];
@@ -273,7 +284,7 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
       T fr[TX];
 #pragma unroll
       for (int ii = 0; ii < TX; ++ii) {
-        if constexpr (kFaces > 0) fr[ii] = iv[ii] ? rbuf[kk & 1][TX * TY + ii][threadIdx.x] : T(0);
+        if constexpr (kFaces > 0) fr[ii] = iv[ii] ? slot(kk & 1, TX * TY + ii) : T(0);
         else fr[ii] = iv[ii] ? ldFace<COH>(jpl + ((int64_t)k * a.nxs + iloc[ii]) * nchain + c) : T(0);
       }
 #pragma unroll
@@ -282,7 +293,7 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
         const int j = jloc[jj];
         T *const lfp = ipl + ((int64_t)k * a.nys + j) * nchain + c;
         T lf;
-        if constexpr (kFaces > 0) lf = rbuf[kk & 1][TX * TY + TX + jj][threadIdx.x];
+        if constexpr (kFaces > 0) lf = slot(kk & 1, TX * TY + TX + jj);
         else lf = ldFace<COH>(lfp);
         const int64_t zrow = (zslice + (sd.jo + j)) * a.nx + sd.io;
 #pragma unroll
@@ -329,8 +340,11 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
 
 template <typename T, int TX, int TY, bool RECIP, bool POP, bool FUSE = false>
 __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const __grid_constant__ SweepArgs<T> a) {
-  sweepTile<T, TX, TY, RECIP, POP, false, FUSE>(a, a.wave[blockIdx.z], a.tile_off + blockIdx.y, blockIdx.x,
-                                                gridDim.x);
+  constexpr int PFM = (sizeof(T) == 8 && !FUSE) ? 2 : 0;
+  constexpr int kSlots = sweepSlots<TX, TY, RECIP, false, PFM>();
+  __shared__ T rbuf[kSlots > 0 ? 2 * kSlots : 1][kSweepThreads];
+  sweepTile<T, TX, TY, RECIP, POP, false, FUSE, PFM>(a, a.wave[blockIdx.z], a.tile_off + blockIdx.y, blockIdx.x,
+                                                     gridDim.x, rbuf);
 }
 
 namespace {
@@ -381,6 +395,12 @@ __device__ __forceinline__ void gridBarrier(unsigned int *bar, unsigned int nblo
 template <typename T, int TX, int TY>
 __global__ void __launch_bounds__(kSweepThreads) batch_sweep_kernel(const SweepArgs<T> *__restrict__ inst,
                                                                    const BatchSweepPlan p) {
+  // FP64: rhs of the next slice streamed into shared memory (read-only in the launch);
+  // one buffer serves both sigt variants (their slot counts agree for rhs only)
+  constexpr int PFM = sizeof(T) == 8 ? 1 : 0;
+  constexpr int kSlots = sweepSlots<TX, TY, true, true, PFM>();
+  static_assert(kSlots == sweepSlots<TX, TY, false, true, PFM>(), "one buffer for both variants");
+  __shared__ T rbuf[kSlots > 0 ? 2 * kSlots : 1][kSweepThreads];
   const unsigned int nb = gridDim.x;
   for (int i = blockIdx.x; i < p.nzero; i += gridDim.x) {
     const BatchZero z = p.zero[i];
@@ -394,8 +414,8 @@ __global__ void __launch_bounds__(kSweepThreads) batch_sweep_kernel(const SweepA
       const int4 w = p.items[i];
       const SweepArgs<T> &a = inst[w.x];
       const int ncb = (a.Ds * a.Gs + kSweepThreads - 1) / kSweepThreads;
-      if (a.cls != nullptr) sweepTile<T, TX, TY, true, true, true>(a, w.y, w.z, w.w, ncb);
-      else sweepTile<T, TX, TY, false, true, true>(a, w.y, w.z, w.w, ncb);
+      if (a.cls != nullptr) sweepTile<T, TX, TY, true, true, true, false, PFM>(a, w.y, w.z, w.w, ncb, rbuf);
+      else sweepTile<T, TX, TY, false, true, true, false, PFM>(a, w.y, w.z, w.w, ncb, rbuf);
     }
     gridBarrier(p.bar, nb, p.err);
   }
