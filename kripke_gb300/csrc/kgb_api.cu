@@ -79,6 +79,11 @@ struct TimerFam {
 struct kgb_ctx {
   int device = 0;
   cudaStream_t own_stream = nullptr;
+  // second stream for half of each sweep step's subdomains: the two halves' step
+  // launches overlap, so one half's wave tail runs beside the other's blocks
+  cudaStream_t aux = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  int sweep_streams = 2;
   cudaStream_t stream = nullptr;
   std::string err;
   bool ready = false;
@@ -1015,12 +1020,27 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool
     a.vol_uniform = ctx->vol_uniform;
   }
   FamScope fs(ctx, "sweep");
+  const int split = (ctx->sweep_streams > 1 && ctx->aux && nwave >= 2) ? nwave / 2 : 0;
+  SweepArgs<T> b = a;
+  b.wave = wave_dev + split;
+  if (split) {
+    CK(cudaEventRecord(ctx->fork_ev, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->aux, ctx->fork_ev, 0));
+  }
   for (int s = 0; s < ctx->nsteps; ++s) {
-    a.tile_off = ctx->tile_off[s];
+    a.tile_off = b.tile_off = ctx->tile_off[s];
     const int nt = ctx->tile_off[s + 1] - ctx->tile_off[s];
     if (nt == 0) continue;
-    launch_sweep_step<T>(a, nt, nwave, ctx->stream);
+    launch_sweep_step<T>(a, nt, split ? split : nwave, ctx->stream);
     CKN(1);
+    if (split) {
+      launch_sweep_step<T>(b, nt, nwave - split, ctx->aux);
+      CKN(1);
+    }
+  }
+  if (split) {
+    CK(cudaEventRecord(ctx->join_ev, ctx->aux));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0));
   }
   return KGB_OK;
 }
@@ -1720,6 +1740,12 @@ int kgb_ctx_create(int device, kgb_ctx **out) {
     return KGB_ERR_CUDA;
   }
   c->stream = c->own_stream;
+  if (cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();  // one stream only: sweeps stay on the context's stream
+    c->sweep_streams = 1;
+  }
   *out = c;
   return KGB_OK;
 }
@@ -1735,6 +1761,9 @@ int kgb_ctx_destroy(kgb_ctx *ctx) {
     }
   freeAll(ctx);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  if (ctx->aux) cudaStreamDestroy(ctx->aux);
+  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+  if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
   delete ctx;
   return KGB_OK;
 }
@@ -2316,6 +2345,11 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->block_jacobi = value != 0;
     return KGB_OK;
   }
+  if (!std::strcmp(key, "sweep_streams")) {
+    if (value != 1 && value != 2) return fail(ctx, KGB_ERR_ARG, "sweep_streams must be 1 or 2");
+    ctx->sweep_streams = (int)value;
+    return KGB_OK;
+  }
   if (!std::strcmp(key, "fused_sweep")) {
     ctx->fuse_sweep = value != 0;
     return KGB_OK;
@@ -2443,6 +2477,7 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "graph_active")) *value = ctx->graph_active ? 1 : 0;
   else if (!std::strcmp(key, "block_jacobi")) *value = ctx->block_jacobi ? 1 : 0;
   else if (!std::strcmp(key, "fused_sweep")) *value = ctx->fuse_sweep ? 1 : 0;
+  else if (!std::strcmp(key, "sweep_streams")) *value = ctx->sweep_streams;
   else if (!std::strcmp(key, "fused_sweep_active")) *value = ctx->fuse_active ? 1 : 0;
   else return fail(ctx, KGB_ERR_ARG, std::string("unknown option '") + key + "'");
   return KGB_OK;
