@@ -187,8 +187,9 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * mixed form); "scattering_tensor" (1 = the single-material zones' scattering on
  * the tensor cores, exact digit products, when groups <= 64; same defaults);
  * "graph" (1 = kgb_solve replays a captured CUDA graph, the default);
- * "sweep_streams" (2 = each sweep step launches half of its subdomains on a
- * second stream so the halves' wave tails overlap, the default; 1 = one launch);
+ * "sweep_streams" (1 to 4: each sweep step launches its subdomains in that
+ * many parts on as many streams, so one part's wave tail overlaps the others'
+ * blocks; default 2);
  * "block_jacobi" (0 = the sweep method, default; 1 = block Jacobi, used by
  * kgb_sweep_solver and so by every solve, iterate and adjoint call);
  * "fused_sweep" (mixed form, Legendre order <= 4: 1 = the solver loop forms

@@ -79,11 +79,12 @@ struct TimerFam {
 struct kgb_ctx {
   int device = 0;
   cudaStream_t own_stream = nullptr;
-  // second stream for half of each sweep step's subdomains: the two halves' step
-  // launches overlap, so one half's wave tail runs beside the other's blocks
-  cudaStream_t aux = nullptr;
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
-  int sweep_streams = 2;
+  // further streams for parts of each sweep step's subdomains: the parts' step
+  // launches overlap, so one part's wave tail runs beside the others' blocks
+  static constexpr int kMaxSweepStreams = 4;
+  cudaStream_t aux[kMaxSweepStreams - 1] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kMaxSweepStreams - 1] = {};
+  int sweep_streams = 2, max_streams = kMaxSweepStreams;
   cudaStream_t stream = nullptr;
   std::string err;
   bool ready = false;
@@ -1020,27 +1021,33 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool
     a.vol_uniform = ctx->vol_uniform;
   }
   FamScope fs(ctx, "sweep");
-  const int split = (ctx->sweep_streams > 1 && ctx->aux && nwave >= 2) ? nwave / 2 : 0;
-  SweepArgs<T> b = a;
-  b.wave = wave_dev + split;
-  if (split) {
+  // parts of the wave's subdomain list, one per stream
+  const int np = std::max(1, std::min(ctx->sweep_streams, nwave));
+  SweepArgs<T> part[kgb_ctx::kMaxSweepStreams];
+  int pn[kgb_ctx::kMaxSweepStreams];
+  for (int i = 0, off = 0; i < np; ++i) {
+    pn[i] = nwave / np + (i < nwave % np ? 1 : 0);
+    part[i] = a;
+    part[i].wave = wave_dev + off;
+    off += pn[i];
+  }
+  auto streamOf = [&](int i) { return i == 0 ? ctx->stream : ctx->aux[i - 1]; };
+  if (np > 1) {
     CK(cudaEventRecord(ctx->fork_ev, ctx->stream));
-    CK(cudaStreamWaitEvent(ctx->aux, ctx->fork_ev, 0));
+    for (int i = 1; i < np; ++i) CK(cudaStreamWaitEvent(ctx->aux[i - 1], ctx->fork_ev, 0));
   }
   for (int s = 0; s < ctx->nsteps; ++s) {
-    a.tile_off = b.tile_off = ctx->tile_off[s];
     const int nt = ctx->tile_off[s + 1] - ctx->tile_off[s];
     if (nt == 0) continue;
-    launch_sweep_step<T>(a, nt, split ? split : nwave, ctx->stream);
-    CKN(1);
-    if (split) {
-      launch_sweep_step<T>(b, nt, nwave - split, ctx->aux);
+    for (int i = 0; i < np; ++i) {
+      part[i].tile_off = ctx->tile_off[s];
+      launch_sweep_step<T>(part[i], nt, pn[i], streamOf(i));
       CKN(1);
     }
   }
-  if (split) {
-    CK(cudaEventRecord(ctx->join_ev, ctx->aux));
-    CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev, 0));
+  for (int i = 1; i < np; ++i) {
+    CK(cudaEventRecord(ctx->join_ev[i - 1], ctx->aux[i - 1]));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev[i - 1], 0));
   }
   return KGB_OK;
 }
@@ -1740,11 +1747,14 @@ int kgb_ctx_create(int device, kgb_ctx **out) {
     return KGB_ERR_CUDA;
   }
   c->stream = c->own_stream;
-  if (cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess) {
+  bool streams_ok = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; i < kgb_ctx::kMaxSweepStreams - 1 && streams_ok; ++i)
+    streams_ok = cudaStreamCreateWithFlags(&c->aux[i], cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming) == cudaSuccess;
+  if (!streams_ok) {
     cudaGetLastError();  // one stream only: sweeps stay on the context's stream
     c->sweep_streams = 1;
+    c->max_streams = 1;
   }
   *out = c;
   return KGB_OK;
@@ -1761,9 +1771,11 @@ int kgb_ctx_destroy(kgb_ctx *ctx) {
     }
   freeAll(ctx);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
-  if (ctx->aux) cudaStreamDestroy(ctx->aux);
+  for (int i = 0; i < kgb_ctx::kMaxSweepStreams - 1; ++i) {
+    if (ctx->aux[i]) cudaStreamDestroy(ctx->aux[i]);
+    if (ctx->join_ev[i]) cudaEventDestroy(ctx->join_ev[i]);
+  }
   if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
-  if (ctx->join_ev) cudaEventDestroy(ctx->join_ev);
   delete ctx;
   return KGB_OK;
 }
@@ -2346,8 +2358,8 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     return KGB_OK;
   }
   if (!std::strcmp(key, "sweep_streams")) {
-    if (value != 1 && value != 2) return fail(ctx, KGB_ERR_ARG, "sweep_streams must be 1 or 2");
-    ctx->sweep_streams = (int)value;
+    if (value < 1 || value > kgb_ctx::kMaxSweepStreams) return fail(ctx, KGB_ERR_ARG, "sweep_streams must be 1 to 4");
+    ctx->sweep_streams = (int)std::min<int64_t>(value, ctx->max_streams);
     return KGB_OK;
   }
   if (!std::strcmp(key, "fused_sweep")) {
