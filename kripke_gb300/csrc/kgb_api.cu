@@ -1213,6 +1213,14 @@ int ensureRhs(kgb_ctx *ctx) {
 template <typename T>
 int scatterTensor(kgb_ctx *ctx, bool acc) {
   const int G = ctx->G, L1 = ctx->L + 1, S = tcDigits<T>(), kpad = ctx->tc_sc_kpad;
+  // the (material, order) launches write disjoint outputs: alternate them over two
+  // streams so each launch's tail overlaps the next one's tiles
+  const bool two = ctx->sweep_streams > 1 && ctx->aux[0] != nullptr;
+  if (two) {
+    CK(cudaEventRecord(ctx->fork_ev, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0));
+  }
+  int nl = 0;
   for (int m = 0; m < 3; ++m) {
     const int64_t nz = ctx->pure_off[m + 1] - ctx->pure_off[m];
     if (nz == 0) continue;
@@ -1237,7 +1245,7 @@ int scatterTensor(kgb_ctx *ctx, bool acc) {
       a.ks = ctx->M;
       a.zstride = (int64_t)G * ctx->M;
       a.stages = 2;  // both K chunks of a tile stay resident across its N blocks
-      launch_tc_gather<T>(a, ctx->stream);
+      launch_tc_gather<T>(a, two && (nl++ & 1) ? ctx->aux[0] : ctx->stream);
       CKN(1);
     }
   }
@@ -1245,8 +1253,13 @@ int scatterTensor(kgb_ctx *ctx, bool acc) {
     ScatterArgsBase a = scatterArgs(ctx);
     a.Z = ctx->nmixed_z;
     a.zlist = ctx->mixed_z;
-    launch_scattering<T>(as<T>(ctx->phi), as<T>(ctx->phi_out), as<T>(ctx->sigsT), a, acc, ctx->stream);
+    launch_scattering<T>(as<T>(ctx->phi), as<T>(ctx->phi_out), as<T>(ctx->sigsT), a, acc,
+                         two && (nl++ & 1) ? ctx->aux[0] : ctx->stream);
     CKN(1);
+  }
+  if (two) {
+    CK(cudaEventRecord(ctx->join_ev[0], ctx->aux[0]));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->join_ev[0], 0));
   }
   return KGB_OK;
 }
