@@ -1149,7 +1149,7 @@ void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, i
   a.nsm = ctx->nsm;
   a.stages = multi_n ? ctx->tc_lp_stages : 2;
   a.stage_out = multi_n ? ctx->tc_lp_stage_out : 1;  // LTimes' B image is at most 64 KB: staging fits
-  launch_tc_rows<T>(a, tcDigits<T>(), 0, multi_n, ctx->stream);
+  launch_tc_rows<T>(a, ctx->stream);
 }
 
 int doLTimes(kgb_ctx *ctx, bool acc) {

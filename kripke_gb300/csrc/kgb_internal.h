@@ -137,7 +137,7 @@ template <typename T>
 void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhalf, std::vector<uint16_t> &img,
                 std::vector<int> &texp);
 template <typename T>
-void launch_tc_rows(const TcArgs<T> &a, int S, int NB, bool multi_n, cudaStream_t s);
+void launch_tc_rows(const TcArgs<T> &a, cudaStream_t s);
 template <typename T>
 void launch_tc_gather(const TcArgs<T> &a, cudaStream_t s);
 

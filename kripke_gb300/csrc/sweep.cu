@@ -10,8 +10,10 @@
 // Schedule: a subdomain's zone set is cut into tiles of tx x ty x tz
 // zones.  In the sweep's own orientation a tile (a,b,c) depends only on
 // (a-1,b,c), (a,b-1,c), (a,b,c-1), so all tiles with a+b+c = step form a
-// hyperplane that runs concurrently; one launch sweeps one tile hyperplane of
-// every subdomain in the wave (all eight octants at once).  Inside a tile each
+// hyperplane that runs concurrently; one step sweeps one tile hyperplane of
+// every subdomain in the wave (all eight octants at once), launched in parts
+// on separate streams so one part's last partial wave of blocks runs beside
+// the other parts' blocks (the caller's choice).  Inside a tile each
 // thread owns one (group, direction) chain and walks the tile's cells in
 // upwind order; its upwind faces stay in registers (psi_lf one value, psi_fr
 // one per tile column, psi_bo one per tile column x row).  The reference's

@@ -665,12 +665,8 @@ void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhal
 }
 
 template <typename T>
-void launch_tc_rows(const TcArgs<T> &a, int S, int NB, bool multi_n, cudaStream_t s) {
-  // the pipelined kernel covers both shapes (N blocks of 32 columns)
+void launch_tc_rows(const TcArgs<T> &a, cudaStream_t s) {
   launchPipe<T, tcDigits<T>(), false>(a, s);
-  (void)S;
-  (void)NB;
-  (void)multi_n;
 }
 
 // Scattering of pure zones on the tensor cores: K = N = groups (<= 64), rows
@@ -682,8 +678,8 @@ void launch_tc_gather(const TcArgs<T> &a, cudaStream_t s) {
 
 template void tc_build_b<double>(const double *, int, int, int, int, int, int, std::vector<uint16_t> &, std::vector<int> &);
 template void tc_build_b<float>(const double *, int, int, int, int, int, int, std::vector<uint16_t> &, std::vector<int> &);
-template void launch_tc_rows<double>(const TcArgs<double> &, int, int, bool, cudaStream_t);
-template void launch_tc_rows<float>(const TcArgs<float> &, int, int, bool, cudaStream_t);
+template void launch_tc_rows<double>(const TcArgs<double> &, cudaStream_t);
+template void launch_tc_rows<float>(const TcArgs<float> &, cudaStream_t);
 template void launch_tc_gather<double>(const TcArgs<double> &, cudaStream_t);
 template void launch_tc_gather<float>(const TcArgs<float> &, cudaStream_t);
 
