@@ -185,7 +185,8 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * (1 = LTimes and LPlusTimes on the tensor cores with exact digit products when
  * the shapes fit; 0 = SIMT kernels; default: tensor for FP64, SIMT for the
  * mixed form); "scattering_tensor" (1 = the single-material zones' scattering on
- * the tensor cores, exact digit products, when groups <= 64; same defaults);
+ * the tensor cores, exact digit products, when groups <= 64; the default in both
+ * forms);
  * "graph" (1 = kgb_solve replays a captured CUDA graph, the default);
  * "sweep_streams" (1 to 4: each sweep step launches its subdomains in that
  * many parts on as many streams, so one part's wave tail overlaps the others'

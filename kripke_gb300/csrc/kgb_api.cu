@@ -1816,10 +1816,12 @@ int kgb_setup(kgb_ctx *ctx, const kgb_dims *d) {
   ctx->dims = *d;
   ctx->prec = d->precision;
   ctx->tsz = ctx->prec == KGB_FP64 ? 8 : 4;
-  // measured defaults: the digit-product tensor path wins for FP64, SIMT for the mixed form;
-  // kgb_autotune re-measures both on the actual problem
+  // measured defaults: the digit-product tensor path wins for FP64 and for the
+  // single-material zones' scattering in both forms (FP32 at 64^3: 4.6 against 6.5
+  // ms); the mixed form's LTimes / LPlusTimes stay SIMT; kgb_autotune re-measures
+  // every choice on the actual problem
   ctx->use_tc_lt = ctx->use_tc_lp = ctx->prec == KGB_FP64;
-  ctx->use_tc_sc = ctx->prec == KGB_FP64;
+  ctx->use_tc_sc = true;
   // the tabulated reciprocal pays where the divide costs FP64 slots; in FP32 its
   // dependent table load costs more than the divide it saves
   ctx->allow_recip = ctx->prec == KGB_FP64;
