@@ -49,3 +49,22 @@ def test_graph_follows_changes(kgb, oracle):
     a = np.array(c.solve(3, 2.0))
     b = np.array(c.solve(3, 1.0))
     np.testing.assert_allclose(a, 2.0 * b, rtol=1e-13)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_stream_split_is_bitwise_neutral(kgb, precision):
+    # sweep steps launched in 1, 2 or 4 parts on separate streams (and the scattering's
+    # launches alternating over two streams) compute the same values in the same order
+    c = kgb.Context()
+    c.generate(precision=precision, zsets=(2, 1, 1), **KW)
+    out = []
+    for n in (1, 2, 4):
+        c.set_option("sweep_streams", n)
+        assert c.get_option("sweep_streams") == n
+        out.append((np.array(c.solve(4)), c.download("psi")))
+    for parts, psi in out[1:]:
+        np.testing.assert_array_equal(parts, out[0][0])
+        np.testing.assert_array_equal(psi, out[0][1])
+    with pytest.raises(kgb.KgbError):
+        c.set_option("sweep_streams", 5)
