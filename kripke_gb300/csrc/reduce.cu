@@ -27,15 +27,21 @@ __device__ __forceinline__ double blockSum(double v) {
   return r;
 }
 
+// One warp per (zone, group) row at a time, lanes over directions, so every
+// load of the warp is one contiguous run of the row; each lane keeps its own
+// volume-weighted partial, summed in the block's fixed order at the end.
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) population_kernel(const T *__restrict__ psi, const double *__restrict__ w,
                                                                 const double *__restrict__ vol, int64_t rows, int G,
                                                                 int D, double *__restrict__ partials) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   double acc = 0.0;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t r = warp0; r < rows; r += nwarps) {
     const T *p = psi + r * D;
     double s = 0.0;
-    for (int d = 0; d < D; ++d) s += w[d] * (double)p[d];
+    for (int d = lane; d < D; d += 32) s += w[d] * (double)p[d];
     acc += s * vol[r / G];
   }
   const double b = blockSum(acc);
