@@ -313,9 +313,10 @@ int kgb_batch_context(kgb_batch *b, int32_t index, kgb_ctx **ctx);
  * "kernels_per_iteration". */
 int kgb_batch_set_option(kgb_batch *b, const char *key, int64_t value);
 int kgb_batch_get_option(kgb_batch *b, const char *key, int64_t *value);
-/* Times every sweep tile shape (4x4, 4x2, 2x2 x depth 2, 4, 8, 16) and row
- * item size (256, 1024, 4096) on the batch and keeps the fastest; overwrites
- * the problems' state. */
+/* Times every sweep tile shape (4x4, 4x2, 2x2 x depth 2, 4, 8, 16), row item
+ * size (256, 1024, 4096) and, unless "per_problem_kernels" was set, both
+ * transform modes on the batch and keeps the fastest; overwrites the
+ * problems' state. */
 int kgb_batch_autotune(kgb_batch *b, double *best_ms);
 /* niter source iterations from psi = 0 for every problem (SteadyStateSolver
  * each); part (may be NULL) receives the particle counts [niter][n]. */

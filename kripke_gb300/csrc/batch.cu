@@ -679,6 +679,22 @@ int kgb_batch_autotune(kgb_batch *b, double *best_ms) {
     }
   }
   b->rows_per_item = brows;
+  // batched SIMT transforms or each problem's own kernels (tensor-core scattering,
+  // the problems' moment-path choices), unless the caller fixed the choice
+  if (b->own_mode < 0) {
+    int bmode = perProblem(b) ? 1 : 0;
+    for (int mode : {0, 1}) {
+      b->own_mode = mode;
+      if ((rc = plan(b)) || (rc = ensurePop(b, 1))) return rc;
+      float ms = 0.f;
+      if ((rc = timeIteration(b, &ms))) return rc;
+      if (ms < best) {
+        best = ms;
+        bmode = mode;
+      }
+    }
+    b->own_mode = bmode;
+  }
   if ((rc = plan(b))) return rc;
   if (best_ms) *best_ms = best;
   return KGB_OK;
