@@ -122,13 +122,18 @@ __device__ __forceinline__ unsigned int hashKey(unsigned long long k) {
   return (unsigned int)k;
 }
 
-// Every element probes at most the whole table (no waiting on other threads);
+// Every element probes at most kMaxProbe slots (no waiting on other threads);
 // a key already present is found by a plain load, so the atomics touch only
-// the first arrival of each distinct value.
+// the first arrival of each distinct value.  A probe run that long means the
+// table is far fuller than the 65535 classes the sweep can index: the
+// overflow flag is raised and every thread stops inserting.
+constexpr unsigned int kMaxProbe = 4096;
 template <typename T>
 __global__ void class_insert_kernel(const T *__restrict__ sig, int64_t n, unsigned long long *table, int *overflow) {
   constexpr unsigned int mask = (1u << kClassTableBits) - 1u;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+  const volatile int *ovf = overflow;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n && !*ovf;
+       e += (int64_t)gridDim.x * blockDim.x) {
     const unsigned long long key = KeyOf<T>::of(sig[e]);
     if (key == kClassEmpty) {
       *overflow = 1;
@@ -136,7 +141,7 @@ __global__ void class_insert_kernel(const T *__restrict__ sig, int64_t n, unsign
     }
     unsigned int h = hashKey(key) & mask;
     bool placed = false;
-    for (unsigned int probe = 0; probe <= mask; ++probe, h = (h + 1u) & mask) {
+    for (unsigned int probe = 0; probe < kMaxProbe; ++probe, h = (h + 1u) & mask) {
       const unsigned long long cur = __ldcg(table + h);
       if (cur == key) {
         placed = true;

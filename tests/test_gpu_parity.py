@@ -216,6 +216,29 @@ def test_sweep_reciprocal_table_and_divide(oracle, kgb, recip):
     check(ctx.download("psi"), p.get("psi"), 1e-12)
 
 
+@pytest.mark.parametrize("distinct,tabulated", [(40, 1), (60000, 1), (None, 0)])
+def test_sweep_reciprocal_classes(oracle, kgb, distinct, tabulated):
+    """The reciprocal table's sigt classes come from a device hash of the distinct
+    values: a few dozen or 60000 distinct values are tabulated; with every one of the
+    153600 values distinct (more than the 65535 classes, and more than the hash table
+    holds) the sweep divides per cell; all sweep as the oracle does."""
+    p, ctx = pair(oracle, kgb, zones=(48, 40, 40), quad=(4, 8), groups=2, scatter=1, geometry=1)
+    n = ctx.field_bytes("sigt_zonal") // 8
+    rng = np.random.default_rng(12)
+    if distinct is None:
+        sig = rng.permutation(np.linspace(0.05, 2.0, n))
+    else:
+        vals = rng.uniform(0.05, 2.0, distinct)
+        sig = np.concatenate([vals, vals[rng.integers(0, distinct, n - distinct)]])
+        rng.shuffle(sig)
+    p.set("sigt_zonal", sig); ctx.upload("sigt_zonal", sig)
+    rhs = rng.uniform(0.0, 1.0, ctx.field_bytes("rhs") // 8)
+    p.set("rhs", rhs); ctx.upload("rhs", rhs)
+    p.sweep_solver(); ctx.sweep_solver()
+    assert ctx.get_option("sweep_reciprocals_active") == tabulated
+    check(ctx.download("psi"), p.get("psi"), 1e-12)
+
+
 def test_nonuniform_mesh(oracle, kgb):
     """Zone widths that vary along each axis (the sweep then divides per cell)."""
     p, ctx = pair(oracle, kgb, zones=(7, 6, 5), quad=16, groups=3, geometry=1)
