@@ -167,8 +167,9 @@ __device__ __forceinline__ float scale2(float x, int e) {
 // with e0 = (emax - 1022) + (column exponent - 1022).
 template <typename T, int S> struct Combine;
 template <> struct Combine<double, 7> {
-  // V rounded once to nearest in integer arithmetic (roundScaled: bit for bit
-  // the sum of the two exact doubles H*2^(e0-28) + L*2^(e0-60), without the FP64 add)
+  // V rounded once to nearest in integer arithmetic (roundScaledOdd: bit for bit
+  // the sum of the two exact doubles H*2^(e0-28) + L*2^(e0-60), without the FP64 add).
+  // For K <= 128, |D_m| <= (m-1) * 128 * 2^14, so |H| < 2^38 and |L| < 2^48.
   static __device__ __forceinline__ double value(const float (&dk)[7], int e0) {
     long long d[7];
 #pragma unroll
@@ -176,7 +177,7 @@ template <> struct Combine<double, 7> {
     const long long h = (d[0] * 256 + d[1]) * 256 + d[2];
     const long long l = ((d[3] * 256 + d[4]) * 256 + d[5]) * 256 + d[6];
     bool ok = true;
-    const double r = roundScaled32(h, l, e0 - 60, ok);
+    const double r = roundScaledOdd(h, l, e0 - 60, ok);
     if (ok) return r;
     return scale2(scale2((double)h, 32) + (double)l, e0 - 60);  // outside the normal range
   }
@@ -192,7 +193,7 @@ struct CombineSmallK {
     const int32_t p01 = d[0] * 256 + d[1], p34 = d[3] * 256 + d[4], p56 = d[5] * 256 + d[6];
     const long long h = (long long)p01 * 256 + d[2], l = (long long)p34 * 65536 + p56;
     bool ok = true;
-    const double r = roundScaled32(h, l, e0 - 60, ok);
+    const double r = roundScaledOdd(h, l, e0 - 60, ok);
     if (ok) return r;
     return scale2(scale2((double)h, 32) + (double)l, e0 - 60);
   }
