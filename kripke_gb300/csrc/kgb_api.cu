@@ -160,6 +160,11 @@ struct kgb_ctx {
   int *tc_lt_exp = nullptr, *tc_lp_exp = nullptr;
   int tc_lt_kpad = 0, tc_lp_nhalf = 0;
   int tc_lp_stages = 2, tc_lp_stage_out = 1;
+  // row exponents of psi for the tensor-core LTimes (FP64), written by the solver's sweep:
+  // while psi_exp_valid, psi_exp[z*G + g] is the largest biased exponent in psi's row (z, g)
+  int *psi_exp = nullptr;
+  bool psi_exp_valid = false;
+  bool allow_psi_exp = true;  // option "psi_row_exponents"
   int *err_d = nullptr;                     // set by kernels whose bounded waits gave up
   int nsm = 0;
   // fused population partials, one per (tile, subdomain, chain block)
@@ -414,10 +419,13 @@ void freeAll(kgb_ctx *c) {
                   c->tc_lp_img, c->tc_lt_exp, c->tc_lp_exp, c->err_d, c->lam, c->phi_prev, c->sigsT_adj,
                   c->gp_lo_adj, c->gp_hi_adj, c->colsum_d, c->e0_d, c->det_d, c->norm_d, c->resp_part, c->resp_d,
                   c->tc_lt_img_adj, c->tc_lp_img_adj, c->tc_lt_exp_adj, c->tc_lp_exp_adj, c->tc_sc_img,
-                  c->tc_sc_img_adj, c->tc_sc_exp, c->tc_sc_exp_adj, c->pure_z};  // mixed_z lies inside pure_z
+                  c->tc_sc_img_adj, c->tc_sc_exp, c->tc_sc_exp_adj, c->pure_z,  // mixed_z lies inside pure_z
+                  c->psi_exp};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->psi = c->rhs = c->phi = c->phi_out = c->sigt = nullptr;
+  c->psi_exp = nullptr;
+  c->psi_exp_valid = false;
   c->plane[0] = c->plane[1] = c->plane[2] = nullptr;
   c->ell = c->ellp = c->sigsT = c->cx = c->cy = c->cz = nullptr;
   c->w_d = c->vol_d = nullptr;
@@ -938,6 +946,10 @@ int prepareT(kgb_ctx *ctx) {
     ctx->dirty_sigt = false;
     ++ctx->gen;
   }
+  if (sizeof(T) == 8 && !ctx->psi_exp) {
+    if ((rc = dmalloc(ctx, &ctx->psi_exp, (size_t)(ctx->Z * ctx->G)))) return rc;
+    ctx->psi_exp_valid = false;
+  }
   return KGB_OK;
 }
 
@@ -982,9 +994,34 @@ int buildTiles(kgb_ctx *ctx) {
 // ---------------------------------------------------------------------------
 // Kernel drivers
 // ---------------------------------------------------------------------------
+// Lanes of one group in the sweep's chain order (chains run over a direction
+// set's directions fastest), for the sweep's row-exponent reduction; 0 when a
+// warp's groups are not aligned runs of a power-of-two length.
+int psiExpWidth(const kgb_ctx *ctx) {
+  const int ds = ctx->Ds;
+  if (ds % 32 == 0) return 32;
+  return (ds > 0 && ds < 32 && (ds & (ds - 1)) == 0) ? ds : 0;
+}
+
+// The solver's sweep records psi's row exponents for the next tensor-core
+// LTimes (FP64, every direction in one K chunk), which then skips its own pass
+// over each row.
+bool psiExpUsable(const kgb_ctx *ctx) {
+  return ctx->prec == KGB_FP64 && ctx->allow_psi_exp && ctx->psi_exp && ctx->tc_lt && ctx->use_tc_lt &&
+         ctx->D <= ctx->tc_lt_kpad && psiExpWidth(ctx) > 0;
+}
+
+// rowexp: record psi's row exponents there (the caller zeroed it); null: psi
+// changes without them, so the recorded ones no longer hold.
 template <typename T>
-int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool fused_rhs) {
+int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool fused_rhs, int *rowexp) {
   SweepArgs<T> a{};
+  if (rowexp) {
+    a.rowexp = rowexp;
+    a.rexp_w = psiExpWidth(ctx);
+  } else {
+    ctx->psi_exp_valid = false;
+  }
   if (fused_rhs) {
     a.phiout = as<T>(ctx->phi_out);
     a.ellp = as<T>(ctx->ellp);
@@ -1052,12 +1089,14 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool
   return KGB_OK;
 }
 
-int sweepWaveAny(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop = false, bool fused_rhs = false) {
-  return ctx->prec == KGB_FP64 ? sweepWave<double>(ctx, wave_dev, nwave, fused_pop, fused_rhs)
-                               : sweepWave<float>(ctx, wave_dev, nwave, fused_pop, fused_rhs);
+int sweepWaveAny(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop = false, bool fused_rhs = false,
+                 int *rowexp = nullptr) {
+  return ctx->prec == KGB_FP64 ? sweepWave<double>(ctx, wave_dev, nwave, fused_pop, fused_rhs, rowexp)
+                               : sweepWave<float>(ctx, wave_dev, nwave, fused_pop, fused_rhs, nullptr);
 }
 
 int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
+  ctx->psi_exp_valid = false;
   void *p = deviceArray(ctx, f);
   const int64_t n = deviceElems(ctx, f);
   if (!p) return fail(ctx, KGB_ERR_ARG, std::string("field '") + f->name + "' cannot be filled");
@@ -1073,13 +1112,15 @@ int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
   return KGB_OK;
 }
 
-int sweepSolver(kgb_ctx *ctx, bool fused_pop = false, bool fused_rhs = false) {
+// rowexp (FP64, optional): zeroed here and filled with psi's row exponents.
+int sweepSolver(kgb_ctx *ctx, bool fused_pop = false, bool fused_rhs = false, int *rowexp = nullptr) {
   for (int k = 0; k < 3; ++k) CK(cudaMemsetAsync(ctx->plane[k], 0, ctx->plane_chunk[k] * ctx->dc.num() * ctx->tsz, ctx->stream));
+  if (rowexp) CK(cudaMemsetAsync(rowexp, 0, ctx->Z * ctx->G * sizeof(int), ctx->stream));
   // Block Jacobi (BlockJacobiComm.cpp:46-98 with SweepSolver.cpp:28-30): the
   // planes every subdomain receives are the ones saved right after the zeroing
   // above, so no subdomain waits on another and none hands its outgoing planes
   // on.  One launch sweeps all of them, each from zero inflow on every face.
-  if (ctx->block_jacobi) return sweepWaveAny(ctx, ctx->levels_d, ctx->dc.num(), fused_pop, fused_rhs);
+  if (ctx->block_jacobi) return sweepWaveAny(ctx, ctx->levels_d, ctx->dc.num(), fused_pop, fused_rhs, rowexp);
   const int nlev = (int)ctx->level_off.size() - 1;
   const int S[3] = {ctx->dc.Sx, ctx->dc.Sy, ctx->dc.Sz};
   // the reversed (adjoint) orientation visits the zone-set levels last to first
@@ -1088,7 +1129,7 @@ int sweepSolver(kgb_ctx *ctx, bool fused_pop = false, bool fused_rhs = false) {
     const int lv = ctx->flip ? nlev - 1 - step : step;
     const int b = ctx->level_off[lv], e = ctx->level_off[lv + 1];
     if (e == b) continue;
-    int rc = sweepWaveAny(ctx, ctx->levels_d + b, e - b, fused_pop, fused_rhs);
+    int rc = sweepWaveAny(ctx, ctx->levels_d + b, e - b, fused_pop, fused_rhs, rowexp);
     if (rc) return rc;
     // hand the outgoing planes to downwind zone sets (ParallelComm.cpp:146-162)
     for (int x = b; x < e; ++x) {
@@ -1131,8 +1172,9 @@ ScatterArgsBase scatterArgs(kgb_ctx *ctx) {
 
 template <typename T>
 void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, int N, int nhalf, const uint16_t *img,
-            const int *ex, bool acc, bool multi_n) {
+            const int *ex, bool acc, bool multi_n, const int *rowexp = nullptr) {
   TcArgs<T> a{};
+  a.rowexp = rowexp;
   a.A = A;
   a.C = C;
   a.rows = ctx->Z * ctx->G;
@@ -1152,7 +1194,9 @@ void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, i
   launch_tc_rows<T>(a, ctx->stream);
 }
 
-int doLTimes(kgb_ctx *ctx, bool acc) {
+// rowexp: psi's row exponents recorded by the sweep that wrote it (FP64 tensor
+// path with one K chunk), or null.
+int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr) {
   FamScope fs(ctx, "ltimes");
   const int64_t rows = ctx->Z * ctx->G;
   if (ctx->tc_lt && ctx->use_tc_lt) {
@@ -1164,7 +1208,7 @@ int doLTimes(kgb_ctx *ctx, bool acc) {
       const int *ex = ctx->tc_lt_exp + (size_t)c * 32;
       if (ctx->prec == KGB_FP64)
         tcRows<double>(ctx, as<double>(ctx->psi) + k0, as<double>(ctx->phi), ctx->D, ctx->M, K, kc, ctx->M, 1, img,
-                       ex, acc || c > 0, false);
+                       ex, acc || c > 0, false, ctx->D <= kc ? rowexp : nullptr);
       else
         tcRows<float>(ctx, as<float>(ctx->psi) + k0, as<float>(ctx->phi), ctx->D, ctx->M, K, kc, ctx->M, 1, img, ex,
                       acc || c > 0, false);
@@ -1317,7 +1361,11 @@ int checkDeviceError(kgb_ctx *ctx) {
 // a solve counts every iterate that way and the last one after its loop.
 int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot = nullptr) {
   int rc;
-  if ((rc = doLTimes(ctx, false))) return rc;          // phi = L psi        (kConst + LTimes)
+  // psi's row exponents, when the sweep that wrote psi recorded them
+  const bool px = psiExpUsable(ctx);
+  const int *rx = px && ctx->psi_exp_valid ? ctx->psi_exp : nullptr;
+  ctx->psi_exp_valid = false;
+  if ((rc = doLTimes(ctx, false, rx))) return rc;      // phi = L psi        (kConst + LTimes)
   if (prev_slot) {
     FamScope fs(ctx, "population");
     const int64_t rows = ctx->Z * ctx->G;
@@ -1338,7 +1386,9 @@ int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot =
   // rhs = L+ phi_out (kConst + LPlusTimes), or formed cell by cell inside the sweep
   ctx->fuse_active = ctx->fuse_sweep && ctx->prec == KGB_MIXED && ctx->M <= kFuseMaxM;
   if (!ctx->fuse_active && (rc = doLPlusTimes(ctx, false))) return rc;
-  if ((rc = sweepSolver(ctx, part_slot != nullptr, ctx->fuse_active))) return rc;  // psi = H^-1 rhs (+ population)
+  if ((rc = sweepSolver(ctx, part_slot != nullptr, ctx->fuse_active, px ? ctx->psi_exp : nullptr)))
+    return rc;  // psi = H^-1 rhs (+ population, + row exponents)
+  ctx->psi_exp_valid = px;
   if (ctx->fuse_active) ctx->rhs_stale = true;
   if (part_slot) {
     FamScope fs(ctx, "population");
@@ -1464,6 +1514,7 @@ struct AdjointView {
   AdjointView(const AdjointView &) = delete;
   AdjointView &operator=(const AdjointView &) = delete;
   void swap() {
+    c->psi_exp_valid = false;  // the row exponents were psi's
     std::swap(c->psi, c->lam);
     std::swap(c->ell, c->ellp);
     std::swap(c->sigsT, c->sigsT_adj);
@@ -1509,11 +1560,15 @@ int convergeLoop(kgb_ctx *ctx, bool adjoint, double q, double tol, int max_iter,
   const int64_t rows = ctx->Z * ctx->G;
   CK(cudaMemsetAsync(ctx->psi, 0, rows * ctx->D * ctx->tsz, ctx->stream));
   CK(cudaMemsetAsync(ctx->phi_prev, 0, rows * sizeof(double), ctx->stream));
+  // psi = 0 has row exponents 0; each sweep records the next ones
+  ctx->psi_exp_valid = false;
+  int *const rx = psiExpUsable(ctx) ? ctx->psi_exp : nullptr;
+  if (rx) CK(cudaMemsetAsync(rx, 0, rows * sizeof(int), ctx->stream));
   double ch = std::numeric_limits<double>::infinity(), best = ch;
   int it = 0, stall = 0;
   while (it < max_iter) {
     ++it;
-    if ((rc = doLTimes(ctx, false))) return rc;
+    if ((rc = doLTimes(ctx, false, rx))) return rc;
     CK(cudaMemsetAsync(ctx->norm_d, 0, 2 * sizeof(unsigned long long), ctx->stream));
     {
       FamScope fs(ctx, "convergence");
@@ -1526,7 +1581,7 @@ int convergeLoop(kgb_ctx *ctx, bool adjoint, double q, double tol, int max_iter,
     if ((rc = doScattering(ctx, false))) return rc;
     if ((rc = adjoint ? doAdjointSource(ctx) : doSource(ctx, q))) return rc;
     if ((rc = doLPlusTimes(ctx, false))) return rc;
-    if ((rc = sweepSolver(ctx, false))) return rc;
+    if ((rc = sweepSolver(ctx, false, false, rx))) return rc;
     unsigned long long h[2] = {0ull, 0ull};
     CK(cudaMemcpyAsync(h, ctx->norm_d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -1624,6 +1679,15 @@ namespace {
 // form keeps the compensated sum fused into its (latency-bound) sweep.
 bool lagPopulation(const kgb_ctx *ctx) { return ctx->prec == KGB_FP64 && ctx->pop_scale != 0.0; }
 
+// After psi = 0: its row exponents are 0.
+int resetPsiExp(kgb_ctx *ctx) {
+  ctx->psi_exp_valid = false;
+  if (!psiExpUsable(ctx)) return KGB_OK;
+  CK(cudaMemsetAsync(ctx->psi_exp, 0, ctx->Z * ctx->G * sizeof(int), ctx->stream));
+  ctx->psi_exp_valid = true;
+  return KGB_OK;
+}
+
 // niter iterations from the current psi with their particle counts.
 int solveIterations(kgb_ctx *ctx, int niter, double q) {
   int rc;
@@ -1672,7 +1736,8 @@ int solveGraph(kgb_ctx *ctx, int niter, double q, const kgb_ctx::SolveGraph **ou
   const std::string err0 = ctx->err;
   int rc = cudaMemsetAsync(ctx->psi, 0, ctx->Z * ctx->G * ctx->D * ctx->tsz, ctx->stream) == cudaSuccess
                ? KGB_OK : KGB_ERR_CUDA;
-  rc = solveIterations(ctx, niter, q);
+  if (!rc) rc = resetPsiExp(ctx);
+  if (!rc) rc = solveIterations(ctx, niter, q);
   cudaGraph_t g = nullptr;
   const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
   const int64_t captured = ctx->launches - l0;
@@ -1694,6 +1759,7 @@ namespace kgb {
 int instance_view(kgb_ctx *ctx, InstanceView *v) {
   int rc = prepare(ctx);
   if (rc) return rc;
+  ctx->psi_exp_valid = false;  // a batched solve writes psi through the view
   InstanceView x{};
   x.prec = ctx->prec;
   x.Z = ctx->Z;
@@ -1945,6 +2011,7 @@ int kgb_field_upload(kgb_ctx *ctx, const char *name, const void *host, int64_t n
   if (!f) return fail(ctx, KGB_ERR_ARG, std::string("unknown field '") + (name ? name : "(null)") + "'");
   if (!host && nbytes > 0) return fail(ctx, KGB_ERR_ARG, "null host pointer");
   ctx->have_lam = false;  // an adjoint state belongs to the inputs it was computed for
+  ctx->psi_exp_valid = false;
   const int64_t want = fieldBytes(ctx, f);
   if (nbytes != want)
     return fail(ctx, KGB_ERR_ARG, std::string("field '") + name + "' expects " + std::to_string(want) + " bytes, got " + std::to_string(nbytes));
@@ -2318,7 +2385,9 @@ int kgb_solve(kgb_ctx *ctx, int32_t niter, double q, double *part) {
   }
   if (!ctx->graph_active) {
     CK(cudaMemsetAsync(ctx->psi, 0, ctx->Z * ctx->G * ctx->D * ctx->tsz, ctx->stream));  // kConst(psi, 0)
-    if ((rc = solveIterations(ctx, niter, q))) return rc;
+    if ((rc = resetPsiExp(ctx)) || (rc = solveIterations(ctx, niter, q))) return rc;
+  } else {
+    ctx->psi_exp_valid = psiExpUsable(ctx);  // the replayed solve ended with a recording sweep
   }
   if (part) CK(cudaMemcpyAsync(part, ctx->parts_dev, niter * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -2379,6 +2448,11 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
   }
   if (!std::strcmp(key, "fused_sweep")) {
     ctx->fuse_sweep = value != 0;
+    return KGB_OK;
+  }
+  if (!std::strcmp(key, "psi_row_exponents")) {
+    ctx->allow_psi_exp = value != 0;
+    ctx->psi_exp_valid = false;
     return KGB_OK;
   }
   if (!std::strcmp(key, "scattering_tensor")) {
@@ -2506,6 +2580,9 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "fused_sweep")) *value = ctx->fuse_sweep ? 1 : 0;
   else if (!std::strcmp(key, "sweep_streams")) *value = ctx->sweep_streams;
   else if (!std::strcmp(key, "fused_sweep_active")) *value = ctx->fuse_active ? 1 : 0;
+  else if (!std::strcmp(key, "psi_row_exponents")) *value = ctx->allow_psi_exp ? 1 : 0;
+  else if (!std::strcmp(key, "psi_row_exponents_active")) *value = psiExpUsable(ctx) ? 1 : 0;
+  else if (!std::strcmp(key, "psi_row_exponents_valid")) *value = ctx->psi_exp_valid ? 1 : 0;
   else return fail(ctx, KGB_ERR_ARG, std::string("unknown option '") + key + "'");
   return KGB_OK;
 }

@@ -60,6 +60,12 @@ struct SweepArgs {
   const T *phiout;            // [Z][G][M]
   const T *ellp;              // [D][M]
   int M;
+  // row exponents for the next LTimes (FP64): rowexp[z*G + g] = max over the
+  // row's swept psi of the biased exponent (atomic max, zeroed before the
+  // sweep), or null.  rexp_w lanes share a group (a power of two <= 32 that
+  // divides Ds, or 32 when 32 divides Ds).
+  int *rowexp;
+  int rexp_w;
 };
 
 // Largest moment count (Legendre order 4) of the fused LPlusTimes prologue.
@@ -126,6 +132,9 @@ struct TcArgs {
   int64_t zstride;
   int stages;            // A stages in shared memory: 2 (default, 0) or 1 (one K chunk per tile only)
   int stage_out;         // 1: outputs of contiguous rows are staged in shared memory for wide stores
+  // per-row bound of the biased exponents of A (max over the row, 0 for a zero
+  // row), written by the sweep that produced A; null: the kernel finds it
+  const int *rowexp;
 };
 // Digits per operand of the exact tensor-core products: 7 balanced 8-bit digits
 // (54 bits) for FP64, 4 (30 bits) for the FP32 of the mixed form.

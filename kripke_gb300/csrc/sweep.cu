@@ -105,6 +105,21 @@ __device__ __forceinline__ void cpAsync(T *dst, const T *src) {
                : "memory");
 }
 
+// Row exponent bound for the next LTimes: the largest biased exponent of the
+// row's psi among the rexp_w lanes that share this group (the lanes of one
+// group and direction set are consecutive chains, aligned to rexp_w), folded
+// into rowexp by one lane with an atomic max.  One warp reduction per run of
+// rexp_w lanes (each run names only its own lanes); four shuffle steps
+// instead cost the FP64 sweep of a 64^3-zone, 64-group, 128-direction
+// problem 1.1 ms per iteration, this 0.3.
+__device__ __forceinline__ void rowExpMax(int *rowexp, int w, unsigned mask, double ps, int64_t row) {
+  const unsigned ex = (unsigned)((__double_as_longlong(ps) >> 52) & 0x7FFu);
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned run = w >= 32 ? mask : (((1u << w) - 1u) << (lane & ~(unsigned)(w - 1))) & mask;
+  const unsigned m = __reduce_max_sync(run, ex);
+  if ((lane & (unsigned)(w - 1)) == 0) atomicMax(rowexp + row, (int)m);
+}
+
 }  // namespace
 
 // One tile of one subdomain for one block of chains: tile is the index into
@@ -132,6 +147,9 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
   typename AccOf<T>::type pop;
   double wd = 0.0;
   if (c < nchain) {
+    // this warp's lanes with a chain (whole groups of rexp_w lanes)
+    const int nlive = nchain - (c - (int)(threadIdx.x & 31u));
+    const unsigned rmask = nlive >= 32 ? 0xffffffffu : ((1u << nlive) - 1u);
     const int gl = c / a.Ds;
     const int dl = c - gl * a.Ds;
     const int g = sd.glo + gl;
@@ -312,6 +330,9 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
             ps = num / den;
           }
           psi[e] = ps;
+          if constexpr (sizeof(T) == 8) {
+            if (a.rowexp) rowExpMax(a.rowexp, a.rexp_w, rmask, ps, z * a.G + g);
+          }
           lf = T(2) * ps - lf;
           fr[ii] = T(2) * ps - fr[ii];
           bo[ii][jj] = T(2) * ps - bo[ii][jj];

@@ -454,7 +454,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
         }
       }
       int emax = 1;
-      if (valid) {
+      if (a.rowexp) {
+        // bound written by the sweep that produced A: no pass over the row
+        if (valid) emax = max(emax, a.rowexp[row]);
+      } else if (valid) {
         if (vec && a.K == a.kpad) {
 #pragma unroll 4
           for (int c = 0; c < nchunks; ++c) {

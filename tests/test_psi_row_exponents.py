@@ -1,0 +1,126 @@
+"""Row exponents of psi recorded by the sweep for the next tensor-core LTimes.
+
+With "psi_row_exponents" (FP64, tensor-core LTimes) the solver loop's sweep
+records, for every (zone, group) row of psi, the largest biased exponent
+(an atomic max over the lanes of each group), and the next LTimes scales its
+digit split of the row by it instead of reading the row once more to find it.
+The recorded value is exactly what the kernel would find, so every iterate is
+bit for bit that of the option off.  Any other write of psi drops the record:
+the tests below write psi in each of those ways -- with values far outside
+the swept ones, so a stale record would overflow the digit split -- and check
+that the next iteration still matches a context that never records.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+KW = dict(zones=(10, 9, 8), groups=8, quad=(4, 8), legendre=3, geometry=1, scatter=1, gset=2, dset=8)
+
+
+def pair(kgb, **kw):
+    out = []
+    for on in (0, 1):
+        c = kgb.Context()
+        c.generate(precision=kgb.FP64, **dict(KW, **kw))
+        c.set_option("psi_row_exponents", on)
+        out.append(c)
+    return out
+
+
+def same(a, b, fields=("psi", "phi", "phi_out", "rhs")):
+    for f in fields:
+        np.testing.assert_array_equal(a.download(f), b.download(f), err_msg=f)
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(quad=(8, 16)), dict(quad=(8, 8)), dict(zsets=(2, 1, 2)),
+                                dict(zsets=(5, 3, 1), block_jacobi=True)])
+def test_iterates_bitwise(kgb, kw):
+    bj = kw.pop("block_jacobi", False)
+    a, b = pair(kgb, **kw)
+    for c in (a, b):
+        c.set_option("block_jacobi", int(bj))
+    pa = [a.iterate() for _ in range(4)]
+    pb = [b.iterate() for _ in range(4)]
+    assert b.get_option("psi_row_exponents_active") == 1 and a.get_option("psi_row_exponents_active") == 0
+    assert b.get_option("psi_row_exponents_valid") == 1
+    assert pa == pb
+    same(a, b)
+    # graph-replayed solves (psi = 0 first: its record is zeroed with it)
+    np.testing.assert_array_equal(a.solve(5), b.solve(5))
+    assert b.get_option("graph_active") == 1 and b.get_option("psi_row_exponents_valid") == 1
+    same(a, b)
+    np.testing.assert_array_equal(a.solve(5), b.solve(5))  # replay
+    same(a, b)
+
+
+def test_unaligned_direction_sets_fall_back(kgb):
+    # 3 directions per set: a warp's groups are not power-of-two runs, nothing is recorded
+    a, b = pair(kgb, quad=(4, 6))
+    assert [a.iterate() for _ in range(3)] == [b.iterate() for _ in range(3)]
+    assert b.get_option("psi_row_exponents_active") == 0 and b.get_option("moments_tensor_ltimes") == 1
+    same(a, b)
+
+
+def test_converged_solve_bitwise(kgb):
+    a, b = pair(kgb)
+    ra, rb = a.solve_converged(1.0, 1e-10, 200), b.solve_converged(1.0, 1e-10, 200)
+    assert ra == rb
+    same(a, b, ("psi", "phi"))
+
+
+def _wild(shape, seed):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal(shape) * np.exp2(rng.integers(-40, 60, size=shape))
+
+
+@pytest.mark.parametrize("how", ["upload", "fill", "sweep_subdomain", "sweep_solver", "adjoint", "ltimes_api"])
+def test_other_psi_writes_drop_the_record(kgb, how):
+    a, b = pair(kgb)
+    for c in (a, b):
+        c.iterate()
+        c.iterate()
+    assert b.get_option("psi_row_exponents_valid") == 1
+    for c in (a, b):
+        if how == "upload":
+            c.upload("psi", _wild(c.download("psi").shape, 1))
+        elif how == "fill":
+            c.fill("psi", 3.0e80)
+        elif how in ("sweep_subdomain", "sweep_solver"):
+            c.upload("rhs", _wild(c.download("rhs").shape, 2))
+            if how == "sweep_subdomain":
+                c.sweep_subdomain(c.num_subdomains - 1)
+            else:
+                c.sweep_solver()
+        elif how == "adjoint":
+            # the adjoint state takes psi's place while it runs
+            c.set_response(np.linspace(0.0, 1.0, 10 * 9 * 8))
+            c.adjoint_solve(1e-8, 50)
+        elif how == "ltimes_api":
+            c.ltimes()  # reads psi only: the record stays
+    if how == "ltimes_api":
+        assert b.get_option("psi_row_exponents_valid") == 1
+    else:
+        assert b.get_option("psi_row_exponents_valid") == 0
+    assert a.iterate() == b.iterate()
+    same(a, b)
+    assert a.iterate() == b.iterate()
+    same(a, b)
+
+
+def test_batched_solve_drops_the_record(kgb):
+    bt = kgb.Batch(precision=kgb.FP64)
+    bt.add(**KW)
+    solo = kgb.Context()
+    solo.generate(precision=kgb.FP64, **KW)
+    solo.set_option("psi_row_exponents", 0)
+    c = bt.context(0)
+    c.iterate()
+    c.iterate()
+    assert c.get_option("psi_row_exponents_valid") == 1
+    bt.solve(3)  # writes the problem's psi through the batch's own kernels
+    solo.solve(3)
+    assert c.get_option("psi_row_exponents_valid") == 0
+    np.testing.assert_array_equal(c.download("psi"), solo.download("psi"))
+    assert c.iterate() == solo.iterate()
+    np.testing.assert_array_equal(c.download("phi"), solo.download("phi"))
