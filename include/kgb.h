@@ -198,21 +198,24 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * running LPlusTimes, with the SIMT kernel's arithmetic, so psi is unchanged;
  * rhs is then refreshed, as L+ phi_out, only when an entry point reads it --
  * download, kgb_lplustimes, the sweep entry points, kgb_balance, autotune);
- * "psi_row_exponents" (FP64 with the tensor-core LTimes: 1 = the solver loop's
+ * "row_exponents" (FP64 with the tensor-core LTimes: 1 = the solver loop's
  * sweep records the largest exponent of every (zone, group) row of psi, and
  * the next iteration's LTimes scales its digit split by it instead of reading
- * each row twice; the results are bit for bit those of 0; default 1; any other
- * write of psi -- upload, fill, kgb_sweep_subdomain, kgb_sweep_solver, the
- * adjoint, a batched solve -- drops the record). */
+ * each row twice, and that LTimes records phi's largest exponent per (zone,
+ * moment) for the tensor-core scattering's gathered rows likewise; the
+ * results are bit for bit those of 0; default 1; any other write of psi --
+ * upload, fill, kgb_sweep_subdomain, kgb_sweep_solver, the adjoint, a batched
+ * solve -- drops psi's record). */
 int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
 /* Current value of a knob: the keys above, plus "moments_tensor_ltimes",
  * "moments_tensor_lplustimes" and "scattering_tensor_active" (1 when that
  * kernel runs on the tensor cores), "sweep_reciprocals_active" (1 when the
  * sweep uses tabulated reciprocals), "graph_active" (1 when the last
  * kgb_solve replayed a graph), "fused_sweep_active" (1 when the last
- * iteration formed rhs inside the sweep), "psi_row_exponents_active" (1 when
- * the solver loop records them on this problem) and "psi_row_exponents_valid"
- * (1 when the record matches the current psi). */
+ * iteration formed rhs inside the sweep), "psi_row_exponents_active" and
+ * "phi_row_exponents_active" (1 when the solver loop records them on this
+ * problem) and "psi_row_exponents_valid" (1 when psi's record matches the
+ * current psi). */
 int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value);
 /* Autotuner: times every sweep tile shape (footprint 4x4, 4x2, 2x2 x depth
  * 2, 4, 8, 16 zones) and both LTimes / LPlusTimes paths (tensor-core digit

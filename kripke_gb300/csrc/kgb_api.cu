@@ -164,7 +164,10 @@ struct kgb_ctx {
   // while psi_exp_valid, psi_exp[z*G + g] is the largest biased exponent in psi's row (z, g)
   int *psi_exp = nullptr;
   bool psi_exp_valid = false;
-  bool allow_psi_exp = true;  // option "psi_row_exponents"
+  bool allow_row_exp = true;  // option "row_exponents"
+  // phi's exponents per (zone, moment) over the groups, recorded by the tensor-core
+  // LTimes for the tensor-core scattering that follows it in the same iteration
+  int *phi_exp = nullptr;
   int *err_d = nullptr;                     // set by kernels whose bounded waits gave up
   int nsm = 0;
   // fused population partials, one per (tile, subdomain, chain block)
@@ -420,11 +423,11 @@ void freeAll(kgb_ctx *c) {
                   c->gp_lo_adj, c->gp_hi_adj, c->colsum_d, c->e0_d, c->det_d, c->norm_d, c->resp_part, c->resp_d,
                   c->tc_lt_img_adj, c->tc_lp_img_adj, c->tc_lt_exp_adj, c->tc_lp_exp_adj, c->tc_sc_img,
                   c->tc_sc_img_adj, c->tc_sc_exp, c->tc_sc_exp_adj, c->pure_z,  // mixed_z lies inside pure_z
-                  c->psi_exp};
+                  c->psi_exp, c->phi_exp};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->psi = c->rhs = c->phi = c->phi_out = c->sigt = nullptr;
-  c->psi_exp = nullptr;
+  c->psi_exp = c->phi_exp = nullptr;
   c->psi_exp_valid = false;
   c->plane[0] = c->plane[1] = c->plane[2] = nullptr;
   c->ell = c->ellp = c->sigsT = c->cx = c->cy = c->cz = nullptr;
@@ -950,6 +953,7 @@ int prepareT(kgb_ctx *ctx) {
     if ((rc = dmalloc(ctx, &ctx->psi_exp, (size_t)(ctx->Z * ctx->G)))) return rc;
     ctx->psi_exp_valid = false;
   }
+  if (sizeof(T) == 8 && !ctx->phi_exp && (rc = dmalloc(ctx, &ctx->phi_exp, (size_t)(ctx->Z * ctx->M)))) return rc;
   return KGB_OK;
 }
 
@@ -1007,8 +1011,25 @@ int psiExpWidth(const kgb_ctx *ctx) {
 // LTimes (FP64, every direction in one K chunk), which then skips its own pass
 // over each row.
 bool psiExpUsable(const kgb_ctx *ctx) {
-  return ctx->prec == KGB_FP64 && ctx->allow_psi_exp && ctx->psi_exp && ctx->tc_lt && ctx->use_tc_lt &&
+  return ctx->prec == KGB_FP64 && ctx->allow_row_exp && ctx->psi_exp && ctx->tc_lt && ctx->use_tc_lt &&
          ctx->D <= ctx->tc_lt_kpad && psiExpWidth(ctx) > 0;
+}
+
+// Lanes of one zone in the tensor-core LTimes' epilogue (one lane per (zone,
+// group) row): 32 when the group count is a multiple of 32, the group count
+// when it is a smaller power of two, else 0.
+int phiExpWidth(const kgb_ctx *ctx) {
+  const int g = ctx->G;
+  if (g % 32 == 0) return 32;
+  return (g > 0 && g < 32 && (g & (g - 1)) == 0) ? g : 0;
+}
+
+// The tensor-core LTimes (FP64, one K chunk) records phi's exponents per
+// (zone, moment) for the tensor-core scattering of the same iteration, which
+// then skips its own pass over each gathered row.
+bool phiExpUsable(const kgb_ctx *ctx) {
+  return ctx->prec == KGB_FP64 && ctx->allow_row_exp && ctx->phi_exp && ctx->tc_lt && ctx->use_tc_lt &&
+         ctx->D <= ctx->tc_lt_kpad && ctx->tc_sc && ctx->use_tc_sc && phiExpWidth(ctx) > 0;
 }
 
 // rowexp: record psi's row exponents there (the caller zeroed it); null: psi
@@ -1172,9 +1193,14 @@ ScatterArgsBase scatterArgs(kgb_ctx *ctx) {
 
 template <typename T>
 void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, int N, int nhalf, const uint16_t *img,
-            const int *ex, bool acc, bool multi_n, const int *rowexp = nullptr) {
+            const int *ex, bool acc, bool multi_n, const int *rowexp = nullptr, int *outexp = nullptr) {
   TcArgs<T> a{};
   a.rowexp = rowexp;
+  if (outexp) {  // LTimes only: its outputs are staged
+    a.outexp = outexp;
+    a.outexp_w = phiExpWidth(ctx);
+    a.outexp_rows = ctx->G;
+  }
   a.A = A;
   a.C = C;
   a.rows = ctx->Z * ctx->G;
@@ -1195,8 +1221,9 @@ void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, i
 }
 
 // rowexp: psi's row exponents recorded by the sweep that wrote it (FP64 tensor
-// path with one K chunk), or null.
-int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr) {
+// path with one K chunk), or null.  outexp: zeroed and filled with phi's
+// exponents per (zone, moment) for the tensor-core scattering, or null.
+int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr, int *outexp = nullptr) {
   FamScope fs(ctx, "ltimes");
   const int64_t rows = ctx->Z * ctx->G;
   if (ctx->tc_lt && ctx->use_tc_lt) {
@@ -1206,16 +1233,21 @@ int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr) {
       const int K = std::min(kc, ctx->D - k0);
       const uint16_t *img = ctx->tc_lt_img + (size_t)c * kc * S * 32;
       const int *ex = ctx->tc_lt_exp + (size_t)c * 32;
-      if (ctx->prec == KGB_FP64)
+      if (ctx->prec == KGB_FP64) {
+        const bool one = ctx->D <= kc && !acc;  // the records hold for a whole, fresh phi only
+        if (outexp && !one) return fail(ctx, KGB_ERR_STATE, "phi exponent record needs one fresh LTimes launch");
+        if (outexp) CK(cudaMemsetAsync(outexp, 0, ctx->Z * ctx->M * sizeof(int), ctx->stream));
         tcRows<double>(ctx, as<double>(ctx->psi) + k0, as<double>(ctx->phi), ctx->D, ctx->M, K, kc, ctx->M, 1, img,
-                       ex, acc || c > 0, false, ctx->D <= kc ? rowexp : nullptr);
-      else
+                       ex, acc || c > 0, false, one ? rowexp : nullptr, outexp);
+      } else {
         tcRows<float>(ctx, as<float>(ctx->psi) + k0, as<float>(ctx->phi), ctx->D, ctx->M, K, kc, ctx->M, 1, img, ex,
                       acc || c > 0, false);
+      }
       CKN(1);
     }
     return KGB_OK;
   }
+  if (outexp) return fail(ctx, KGB_ERR_STATE, "phi exponent record needs the tensor-core LTimes");
   if (ctx->prec == KGB_FP64)
     launch_ltimes<double>(as<double>(ctx->psi), as<double>(ctx->phi), as<double>(ctx->ell), rows, ctx->D, ctx->M, acc, ctx->stream);
   else
@@ -1255,7 +1287,7 @@ int ensureRhs(kgb_ctx *ctx) {
 }
 
 template <typename T>
-int scatterTensor(kgb_ctx *ctx, bool acc) {
+int scatterTensor(kgb_ctx *ctx, bool acc, const int *rowexp) {
   const int G = ctx->G, L1 = ctx->L + 1, S = tcDigits<T>(), kpad = ctx->tc_sc_kpad;
   // the (material, order) launches write disjoint outputs: alternate them over two
   // streams so each launch's tail overlaps the next one's tiles
@@ -1289,6 +1321,7 @@ int scatterTensor(kgb_ctx *ctx, bool acc) {
       a.ks = ctx->M;
       a.zstride = (int64_t)G * ctx->M;
       a.stages = 2;  // both K chunks of a tile stay resident across its N blocks
+      a.rowexp = rowexp;
       launch_tc_gather<T>(a, two && (nl++ & 1) ? ctx->aux[0] : ctx->stream);
       CKN(1);
     }
@@ -1308,10 +1341,12 @@ int scatterTensor(kgb_ctx *ctx, bool acc) {
   return KGB_OK;
 }
 
-int doScattering(kgb_ctx *ctx, bool acc) {
+// rowexp (FP64 tensor path): phi's exponents per (zone, moment) recorded by the
+// LTimes that wrote phi, or null.
+int doScattering(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr) {
   FamScope fs(ctx, "scattering");
   if (ctx->tc_sc && ctx->use_tc_sc)
-    return ctx->prec == KGB_FP64 ? scatterTensor<double>(ctx, acc) : scatterTensor<float>(ctx, acc);
+    return ctx->prec == KGB_FP64 ? scatterTensor<double>(ctx, acc, rowexp) : scatterTensor<float>(ctx, acc, nullptr);
   ScatterArgsBase a = scatterArgs(ctx);
   if (ctx->prec == KGB_FP64)
     launch_scattering<double>(as<double>(ctx->phi), as<double>(ctx->phi_out), as<double>(ctx->sigsT), a, acc, ctx->stream);
@@ -1365,7 +1400,8 @@ int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot =
   const bool px = psiExpUsable(ctx);
   const int *rx = px && ctx->psi_exp_valid ? ctx->psi_exp : nullptr;
   ctx->psi_exp_valid = false;
-  if ((rc = doLTimes(ctx, false, rx))) return rc;      // phi = L psi        (kConst + LTimes)
+  int *const pe = phiExpUsable(ctx) ? ctx->phi_exp : nullptr;  // phi's, for the scattering
+  if ((rc = doLTimes(ctx, false, rx, pe))) return rc;  // phi = L psi        (kConst + LTimes)
   if (prev_slot) {
     FamScope fs(ctx, "population");
     const int64_t rows = ctx->Z * ctx->G;
@@ -1381,7 +1417,7 @@ int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot =
       return rc;
     }
   }
-  if ((rc = doScattering(ctx, false))) return rc;      // phi_out = S phi    (kConst + scattering)
+  if ((rc = doScattering(ctx, false, pe))) return rc;  // phi_out = S phi    (kConst + scattering)
   if ((rc = doSource(ctx, q))) return rc;              // phi_out += Q
   // rhs = L+ phi_out (kConst + LPlusTimes), or formed cell by cell inside the sweep
   ctx->fuse_active = ctx->fuse_sweep && ctx->prec == KGB_MIXED && ctx->M <= kFuseMaxM;
@@ -1564,11 +1600,12 @@ int convergeLoop(kgb_ctx *ctx, bool adjoint, double q, double tol, int max_iter,
   ctx->psi_exp_valid = false;
   int *const rx = psiExpUsable(ctx) ? ctx->psi_exp : nullptr;
   if (rx) CK(cudaMemsetAsync(rx, 0, rows * sizeof(int), ctx->stream));
+  int *const pe = phiExpUsable(ctx) ? ctx->phi_exp : nullptr;
   double ch = std::numeric_limits<double>::infinity(), best = ch;
   int it = 0, stall = 0;
   while (it < max_iter) {
     ++it;
-    if ((rc = doLTimes(ctx, false, rx))) return rc;
+    if ((rc = doLTimes(ctx, false, rx, pe))) return rc;
     CK(cudaMemsetAsync(ctx->norm_d, 0, 2 * sizeof(unsigned long long), ctx->stream));
     {
       FamScope fs(ctx, "convergence");
@@ -1578,7 +1615,7 @@ int convergeLoop(kgb_ctx *ctx, bool adjoint, double q, double tol, int max_iter,
         launch_change_norm<float>(as<float>(ctx->phi), ctx->M, ctx->phi_prev, rows, ctx->norm_d, ctx->stream);
       CKN(1);
     }
-    if ((rc = doScattering(ctx, false))) return rc;
+    if ((rc = doScattering(ctx, false, pe))) return rc;
     if ((rc = adjoint ? doAdjointSource(ctx) : doSource(ctx, q))) return rc;
     if ((rc = doLPlusTimes(ctx, false))) return rc;
     if ((rc = sweepSolver(ctx, false, false, rx))) return rc;
@@ -2450,8 +2487,8 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->fuse_sweep = value != 0;
     return KGB_OK;
   }
-  if (!std::strcmp(key, "psi_row_exponents")) {
-    ctx->allow_psi_exp = value != 0;
+  if (!std::strcmp(key, "row_exponents")) {
+    ctx->allow_row_exp = value != 0;
     ctx->psi_exp_valid = false;
     return KGB_OK;
   }
@@ -2580,7 +2617,8 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "fused_sweep")) *value = ctx->fuse_sweep ? 1 : 0;
   else if (!std::strcmp(key, "sweep_streams")) *value = ctx->sweep_streams;
   else if (!std::strcmp(key, "fused_sweep_active")) *value = ctx->fuse_active ? 1 : 0;
-  else if (!std::strcmp(key, "psi_row_exponents")) *value = ctx->allow_psi_exp ? 1 : 0;
+  else if (!std::strcmp(key, "row_exponents")) *value = ctx->allow_row_exp ? 1 : 0;
+  else if (!std::strcmp(key, "phi_row_exponents_active")) *value = phiExpUsable(ctx) ? 1 : 0;
   else if (!std::strcmp(key, "psi_row_exponents_active")) *value = psiExpUsable(ctx) ? 1 : 0;
   else if (!std::strcmp(key, "psi_row_exponents_valid")) *value = ctx->psi_exp_valid ? 1 : 0;
   else return fail(ctx, KGB_ERR_ARG, std::string("unknown option '") + key + "'");

@@ -133,8 +133,16 @@ struct TcArgs {
   int stages;            // A stages in shared memory: 2 (default, 0) or 1 (one K chunk per tile only)
   int stage_out;         // 1: outputs of contiguous rows are staged in shared memory for wide stores
   // per-row bound of the biased exponents of A (max over the row, 0 for a zero
-  // row), written by the sweep that produced A; null: the kernel finds it
+  // row), written by the kernel that produced A; null: the kernel finds it.
+  // Row r's entry is rowexp[r]; gathered rows: rowexp[zone * ks + moment].
   const int *rowexp;
+  // record of C's exponents for a gathered consumer (FP64, staged outputs):
+  // outexp[(r / outexp_rows) * N + n] = max biased exponent of column n over
+  // the outexp_rows consecutive rows of r's zone (atomic max; zeroed by the
+  // caller), reduced over runs of outexp_w lanes (32, or outexp_rows when that
+  // is a power of two below 32); null: none
+  int *outexp;
+  int outexp_w, outexp_rows;
 };
 // Digits per operand of the exact tensor-core products: 7 balanced 8-bit digits
 // (54 bits) for FP64, 4 (30 bits) for the FP32 of the mixed form.

@@ -411,6 +411,27 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
             const int n = j * NB + cgrp * 8 + u;
             out[u] = (ovalid && n < a.N) ? combined(u, n) : T(0);
           }
+          if constexpr (sizeof(T) == 8) {
+            if (a.outexp) {
+              // exponent record for the gathered consumer: one warp reduction per
+              // column over each run of rows of one zone, one atomic per run
+              const unsigned live = __ballot_sync(0xffffffffu, ovalid);
+              const unsigned w = (unsigned)a.outexp_w;
+              const unsigned run = (w >= 32u ? 0xffffffffu : (((1u << w) - 1u) << (lane & ~(w - 1u)))) & live;
+              if (ovalid) {
+                const int64_t zbase = (orow / a.outexp_rows) * (int64_t)a.N;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                  const int n = j * NB + cgrp * 8 + u;
+                  if (n < a.N) {
+                    const unsigned ex = (unsigned)((__double_as_longlong(out[u]) >> 52) & 0x7FF);
+                    const unsigned m = __reduce_max_sync(run, ex);
+                    if ((lane & (w - 1u)) == 0) atomicMax(a.outexp + zbase + n, (int)m);
+                  }
+                }
+              }
+            }
+          }
           const int64_t rbase = (int64_t)tile * kTcRows + (warp & 3) * 32;
 #pragma unroll
           for (int hh = 0; hh < 2; ++hh) {
@@ -455,8 +476,15 @@ __global__ void __launch_bounds__(kPipeThreads, 1) tc_pipe_kernel(const TcArgs<T
       }
       int emax = 1;
       if (a.rowexp) {
-        // bound written by the sweep that produced A: no pass over the row
-        if (valid) emax = max(emax, a.rowexp[row]);
+        // bound written by the kernel that produced A: no pass over the row
+        if (valid) {
+          if constexpr (GATHER) {
+            const int64_t q = row / a.nm;
+            emax = max(emax, a.rowexp[(int64_t)a.zl[q] * a.ks + a.m0 + (row - q * a.nm)]);
+          } else {
+            emax = max(emax, a.rowexp[row]);
+          }
+        }
       } else if (valid) {
         if (vec && a.K == a.kpad) {
 #pragma unroll 4

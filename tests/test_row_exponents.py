@@ -1,14 +1,16 @@
-"""Row exponents of psi recorded by the sweep for the next tensor-core LTimes.
+"""Row exponents recorded by the producer of a tensor-core operand.
 
-With "psi_row_exponents" (FP64, tensor-core LTimes) the solver loop's sweep
+With "row_exponents" (FP64, tensor-core LTimes) the solver loop's sweep
 records, for every (zone, group) row of psi, the largest biased exponent
 (an atomic max over the lanes of each group), and the next LTimes scales its
-digit split of the row by it instead of reading the row once more to find it.
-The recorded value is exactly what the kernel would find, so every iterate is
-bit for bit that of the option off.  Any other write of psi drops the record:
-the tests below write psi in each of those ways -- with values far outside
-the swept ones, so a stale record would overflow the digit split -- and check
-that the next iteration still matches a context that never records.
+digit split of the row by it instead of reading the row once more to find it;
+that LTimes likewise records phi's exponents per (zone, moment) over the
+groups for the tensor-core scattering's gathered rows.  A recorded value is
+exactly what the consuming kernel would find, so every iterate is bit for bit
+that of the option off.  Any other write of psi drops its record: the tests
+below write psi in each of those ways -- with values far outside the swept
+ones, so a stale record would overflow the digit split -- and check that the
+next iteration still matches a context that never records.
 """
 import numpy as np
 import pytest
@@ -23,7 +25,7 @@ def pair(kgb, **kw):
     for on in (0, 1):
         c = kgb.Context()
         c.generate(precision=kgb.FP64, **dict(KW, **kw))
-        c.set_option("psi_row_exponents", on)
+        c.set_option("row_exponents", on)
         out.append(c)
     return out
 
@@ -34,7 +36,8 @@ def same(a, b, fields=("psi", "phi", "phi_out", "rhs")):
 
 
 @pytest.mark.parametrize("kw", [dict(), dict(quad=(8, 16)), dict(quad=(8, 8)), dict(zsets=(2, 1, 2)),
-                                dict(zsets=(5, 3, 1), block_jacobi=True)])
+                                dict(zsets=(5, 3, 1), block_jacobi=True), dict(groups=64, legendre=4),
+                                dict(groups=12)])
 def test_iterates_bitwise(kgb, kw):
     bj = kw.pop("block_jacobi", False)
     a, b = pair(kgb, **kw)
@@ -44,6 +47,9 @@ def test_iterates_bitwise(kgb, kw):
     pb = [b.iterate() for _ in range(4)]
     assert b.get_option("psi_row_exponents_active") == 1 and a.get_option("psi_row_exponents_active") == 0
     assert b.get_option("psi_row_exponents_valid") == 1
+    # phi's record needs a power-of-two run of group rows per zone
+    assert b.get_option("phi_row_exponents_active") == int(kw.get("groups", 8) != 12)
+    assert a.get_option("phi_row_exponents_active") == 0
     assert pa == pb
     same(a, b)
     # graph-replayed solves (psi = 0 first: its record is zeroed with it)
@@ -113,7 +119,7 @@ def test_batched_solve_drops_the_record(kgb):
     bt.add(**KW)
     solo = kgb.Context()
     solo.generate(precision=kgb.FP64, **KW)
-    solo.set_option("psi_row_exponents", 0)
+    solo.set_option("row_exponents", 0)
     c = bt.context(0)
     c.iterate()
     c.iterate()
