@@ -7,14 +7,16 @@
 // (src/Kripke/Kernel/LTimes.cpp:54-65) and Kernel::LPlusTimes
 // (src/Kripke/Kernel/LPlusTimes.cpp:49-60) when the shapes fit.
 //
-// Exact products from bf16 digits (the Ozaki splitting, Ozaki et al. 2012,
+// Exact products from f16 digits (the Ozaki splitting, Ozaki et al. 2012,
 // "Error-free transformations of matrix multiplication by using fast
 // routines of matrix multiplication"): every A row is scaled by a power of two
 // taken from its largest element and written as S balanced 8-bit digits,
 //   |A[r][k]| = 2^s_r * sum_i a_i * 2^-8i   (truncated after 8S-2 bits),
 // a_i in [-128, 127] times the element's sign, and every B column likewise
 // with 2^t_n and digits b_j (done on the host).  A digit has at most 8
-// significant bits, so it is exact in bf16; a digit product is below 2^14 in
+// significant bits, so it is exact in f16 (as in bf16; f16 is used because its
+// 11-bit significand lets one packed FMA form two digits from their bytes); a
+// digit product is below 2^14 in
 // magnitude, and for every anti-diagonal i+j the sum over k <= 128 of at most
 // S products stays below 2^24, so tcgen05.mma with FP32 accumulation in tensor
 // memory computes each diagonal sum D_{i+j} exactly.  The diagonals are
@@ -36,7 +38,6 @@
 // the B image reaches shared memory with one cp.async.bulk; every mbarrier
 // wait is bounded, and on timeout the CTA records the failure, releases its
 // tensor memory and returns.
-#include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cstring>
@@ -62,9 +63,10 @@ __device__ __forceinline__ uint64_t matDesc(uint32_t saddr, uint32_t lbo, uint32
   return d;
 }
 
-// kind::f16 instruction descriptor: FP32 accumulate, bf16 A and B, both K-major, M = 128
+// kind::f16 instruction descriptor: FP32 accumulate (bits 4-5 = 1), f16 A and B
+// (type fields at bits 7-9 and 10-12 both 0), both K-major, N >> 3, M = 128
 __device__ __forceinline__ uint32_t instrDesc(int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+  return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
@@ -85,32 +87,35 @@ __device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&v)[8]) {
 }
 
 // The S balanced 8-bit digits (most significant first) of two (8S-2)-bit
-// magnitudes as bf16 pairs: element 0 in the low half, element 1 in the high
+// magnitudes as f16 pairs: element 0 in the low half, element 1 in the high
 // half, each multiplied by its element's sign.  Adding 0x80 to every byte of
 // the magnitude (the carries ripple upward and stay inside its 8S bits,
-// since the magnitude is below 2^(8S-2))
-// turns byte b into the digit b - 128 in [-128, 127]; one byte permute places
-// b under the exponent of 2^23, a float add subtracts 2^23 + 128 exactly, and
-// two digits pack into bf16x2 exactly (|d| <= 128 has at most 8 significant
-// bits); a sign flip applies the element's sign.
+// since the magnitude is below 2^(8S-2)) turns byte b into the digit b - 128
+// in [-128, 127].  Per digit, one byte permute places the two elements' bytes
+// in the low bytes of the two halves, a mask puts them under the exponent of
+// 1024 (the f16 value 1024 + b, exact: f16 has 11 significant bits), and one
+// packed FMA forms s * (1024 + b) - s * 1152 = s * (b - 128) exactly for both
+// elements, their signs s = +-1 applied through the multiplier and the offset.
 template <int S>
 __device__ __forceinline__ void digitPairs(uint64_t f0, uint32_t s0, uint64_t f1, uint32_t s1, uint32_t (&w)[S][4],
                                            int col) {
   static_assert(S == 4 || S == 7, "30-bit (FP32) or 54-bit (FP64) magnitudes");
   constexpr uint64_t kBias = S == 7 ? 0x0080808080808080ull : 0x80808080ull;
   const uint32_t sg = (s0 << 15) | (s1 << 31);
+  const uint32_t mul = 0x3C003C00u ^ sg;  // f16x2 (s0, s1), s = +-1
+  const uint32_t off = 0xE480E480u ^ sg;  // f16x2 (-1152 s0, -1152 s1)
   const uint64_t y0 = f0 + kBias, y1 = f1 + kBias;
   const uint32_t lo0 = (uint32_t)y0, hi0 = (uint32_t)(y0 >> 32), lo1 = (uint32_t)y1, hi1 = (uint32_t)(y1 >> 32);
 #pragma unroll
   for (int i = 0; i < S; ++i) {
     const int byte = S - 1 - i;  // digit i is byte S-1-i of the biased magnitude
     const uint32_t x0 = byte >= 4 ? hi0 : lo0, x1 = byte >= 4 ? hi1 : lo1;
-    // bytes: [b, 0, 0, 0x4B] = the float 2^23 + b
-    const uint32_t sel = (uint32_t)(byte & 3) | 0x7440u;
-    const float v0 = __uint_as_float(__byte_perm(x0, 0x4B000000u, sel)) - 8388736.0f;
-    const float v1 = __uint_as_float(__byte_perm(x1, 0x4B000000u, sel)) - 8388736.0f;
-    const __nv_bfloat162 p = __floats2bfloat162_rn(v0, v1);
-    w[i][col] = *reinterpret_cast<const uint32_t *>(&p) ^ sg;
+    // bytes [b0, -, b1, -], then the f16 pair (1024 + b0, 1024 + b1)
+    const uint32_t sel = (uint32_t)(byte & 3) | ((uint32_t)(4 + (byte & 3)) << 8);
+    const uint32_t t = (__byte_perm(x0, x1, sel) & 0x00FF00FFu) | 0x64006400u;
+    uint32_t d;
+    asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(t), "r"(mul), "r"(off));
+    w[i][col] = d;
   }
 }
 
@@ -648,8 +653,18 @@ void launchPipe(const TcArgs<T> &a, cudaStream_t s) {
 
 }  // namespace
 
+// f16 bit pattern of an integer digit, |v| <= 128 (exact: at most 8 significant bits).
+static uint16_t halfOfDigit(int v) {
+  if (v == 0) return 0;
+  const uint16_t s = v < 0 ? 0x8000u : 0u;
+  const unsigned a = (unsigned)(v < 0 ? -v : v);
+  int e = 0;
+  while ((a >> (e + 1)) != 0) ++e;  // leading bit
+  return (uint16_t)(s | ((unsigned)(e + 15) << 10) | ((a << (10 - e)) & 0x3FFu));
+}
+
 // Host: digits of B (K x N, row-major in `b`) as the kernel's shared-memory image:
-// per N block of NB columns, [K/8][S*NB][8] bf16 (slice j rows (j-1)*NB..), and
+// per N block of NB columns, [K/8][S*NB][8] f16 (slice j rows (j-1)*NB..), and
 // the per-column exponent t_n.
 template <typename T>
 void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhalf, std::vector<uint16_t> &img,
@@ -683,10 +698,7 @@ void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhal
       const uint64_t y = f + bias;  // balanced digits: byte - 128
       for (int j = 1; j <= S; ++j) {
         const int dg = (int)((y >> (8 * (S - j))) & 0xFFu) - 128;
-        const float fv = (float)(neg ? -dg : dg);  // |dg| <= 128: exact in bf16
-        uint32_t fb;
-        std::memcpy(&fb, &fv, 4);
-        const uint16_t bf = (uint16_t)(fb >> 16);
+        const uint16_t bf = halfOfDigit(neg ? -dg : dg);
         const int rowi = (j - 1) * NB + nl;
         const size_t off = (size_t)h * kpad * S * NB + (size_t)(k / 8) * (S * NB * 8) + (size_t)(rowi / 8) * 64 +
                            (size_t)(rowi % 8) * 8 + (k % 8);
