@@ -129,30 +129,36 @@ __device__ __forceinline__ int expOf(float x) {
   return e > 0 ? e : 1;
 }
 
+// 64-bit right shift whose amount may reach or exceed 64 (PTX clamps it: 0)
+__device__ __forceinline__ uint64_t shrClamped(uint64_t x, uint32_t n) {
+  uint64_t r;
+  asm("shr.b64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(n));
+  return r;
+}
+
 // Digit source: the (8S-2)-bit fixed-point magnitude of x relative to the
 // row's largest exponent emax (the largest element's leading bit at 8S-3), and
-// its sign.
+// its sign: the significand placed with its leading bit at 8S-3, then shifted
+// right by emax - e (emax >= e for every element of the row).
 template <typename T, int S> struct Fixed;
 template <int S> struct Fixed<double, S> {
   static __device__ __forceinline__ uint64_t mag(double x, int emax, uint32_t &sign) {
+    static_assert(8 * S - 2 >= 53, "the significand fits the window");
     const uint64_t b = (uint64_t)__double_as_longlong(x);
     sign = (uint32_t)(b >> 63);
     const int e = (int)((b >> 52) & 0x7FF);
     const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
-    const int sh = (e > 0 ? e : 1) - emax + (8 * S - 2 - 53);  // left shift; at most 8S-55
-    if (sh >= 0) return m << sh;
-    return -sh >= 64 ? 0ull : m >> (-sh);
+    return shrClamped(m << (8 * S - 2 - 53), (uint32_t)(emax - (e > 0 ? e : 1)));
   }
 };
 template <int S> struct Fixed<float, S> {
   static __device__ __forceinline__ uint64_t mag(float x, int emax, uint32_t &sign) {
+    static_assert(8 * S - 2 >= 24, "the significand fits the window");
     const uint32_t b = __float_as_uint(x);
     sign = b >> 31;
     const int e = (int)((b >> 23) & 0xFF);
     const uint64_t m = (uint64_t)((b & 0x7FFFFFu) | (e ? (1u << 23) : 0u));
-    const int sh = (e > 0 ? e : 1) - emax + (8 * S - 2 - 24);
-    if (sh >= 0) return m << sh;
-    return -sh >= 64 ? 0ull : m >> (-sh);
+    return shrClamped(m << (8 * S - 2 - 24), (uint32_t)(emax - (e > 0 ? e : 1)));
   }
 };
 
