@@ -203,9 +203,10 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * the next iteration's LTimes scales its digit split by it instead of reading
  * each row twice, and that LTimes records phi's largest exponent per (zone,
  * moment) for the tensor-core scattering's gathered rows likewise; the
- * results are bit for bit those of 0; default 1; any other write of psi --
- * upload, fill, kgb_sweep_subdomain, kgb_sweep_solver, the adjoint, a batched
- * solve -- drops psi's record). */
+ * results are bit for bit those of 0; default 1; a fill of psi with 0
+ * records zeros; any other write of psi -- upload, other fills,
+ * kgb_sweep_subdomain, kgb_sweep_solver, the adjoint, a batched solve --
+ * drops psi's record). */
 int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
 /* Current value of a knob: the keys above, plus "moments_tensor_ltimes",
  * "moments_tensor_lplustimes" and "scattering_tensor_active" (1 when that

@@ -1123,6 +1123,11 @@ int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
   if (!p) return fail(ctx, KGB_ERR_ARG, std::string("field '") + f->name + "' cannot be filled");
   if (v == 0.0) {
     CK(cudaMemsetAsync(p, 0, n * ctx->tsz, ctx->stream));
+    // psi = 0 (Kripke's kConst(psi, 0) before a solve): its row exponents are 0
+    if (p == ctx->psi && psiExpUsable(ctx)) {
+      CK(cudaMemsetAsync(ctx->psi_exp, 0, ctx->Z * ctx->G * sizeof(int), ctx->stream));
+      ctx->psi_exp_valid = true;
+    }
   } else if (ctx->prec == KGB_FP64) {
     launch_fill<double>(as<double>(p), n, v, ctx->stream);
     CKN(1);

@@ -130,3 +130,14 @@ def test_batched_solve_drops_the_record(kgb):
     np.testing.assert_array_equal(c.download("psi"), solo.download("psi"))
     assert c.iterate() == solo.iterate()
     np.testing.assert_array_equal(c.download("phi"), solo.download("phi"))
+
+
+def test_zero_fill_records_zero_exponents(kgb):
+    # kConst(psi, 0) before a solve: psi = 0 has row exponents 0, so the record stays usable
+    a, b = pair(kgb)
+    for c in (a, b):
+        c.iterate()
+        c.fill("psi", 0.0)
+    assert b.get_option("psi_row_exponents_valid") == 1
+    assert [a.iterate() for _ in range(3)] == [b.iterate() for _ in range(3)]
+    same(a, b)
