@@ -231,6 +231,106 @@ __global__ void __launch_bounds__(kMomThreads) batch_moments_kernel(const BatchM
   }
 }
 
+// LTimes, FP32, register-tiled (directions a multiple of 32, M <= 32): a block
+// takes 128-row tiles of psi, copies each 32-direction chunk into shared
+// memory with cp.async (two buffers: the next chunk, or the next tile's first,
+// streams in while one is multiplied) and each thread accumulates 4 rows x MB
+// moments (rows lane + 32 i, moments MB*warp ...) in registers.  Per direction
+// a thread reads its 4 rows' values 16 bytes at a time (4 directions per read)
+// and the warp's MB moments of L as one or two 16-byte broadcasts: 4*MB
+// multiply-adds per 1 + MB/4 shared-memory reads, against MB per one for the
+// row-per-thread kernel.  Each output is one FMA chain over ascending
+// directions, as in ltimesRow, so the results are the same bit for bit.
+constexpr int kTileRows = 128;     // rows per tile (4 per thread)
+constexpr int kTileK = 32;         // directions per shared-memory chunk
+constexpr int kTilePitch = kTileK + 4;  // row pitch: the 8 lanes of a quarter-warp hit distinct banks
+
+template <int MB>
+__global__ void __launch_bounds__(kMomThreads) ltimes_tile_kernel(const float *__restrict__ psi,
+                                                                 float *__restrict__ phi,
+                                                                 const float *__restrict__ ell_dm, int64_t rows,
+                                                                 int D, int M, bool accumulate) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *ls = reinterpret_cast<float *>(smem_raw);  // [D][32]: warp w's moments at 8w .. 8w+MB-1
+  float *as = ls + (size_t)D * 32;                   // [2][kTileRows][kTilePitch]
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  for (int i = tid; i < D * 32; i += blockDim.x) {
+    const int d = i >> 5, c = i & 31, g = c >> 3, j = c & 7, m = MB * g + j;
+    ls[i] = (j < MB && m < M) ? ell_dm[(int64_t)d * M + m] : 0.f;
+  }
+  const int64_t ntiles = (rows + kTileRows - 1) / kTileRows;
+  const int nk = D / kTileK;
+  // chunk q of this block: tile blockIdx.x + (q / nk) * gridDim.x, directions (q % nk) * 32
+  const int64_t nq = ntiles > blockIdx.x ? ((ntiles - 1 - blockIdx.x) / gridDim.x + 1) * nk : 0;
+  auto issue = [&](int64_t q) {
+    const int64_t tile = blockIdx.x + (q / nk) * gridDim.x;
+    const int k0 = (int)(q % nk) * kTileK;
+    float *buf = as + (q & 1) * (kTileRows * kTilePitch);
+#pragma unroll
+    for (int i = 0; i < kTileRows * kTileK / 4 / kMomThreads; ++i) {
+      const int idx = tid + i * kMomThreads, r = idx >> 3, c4 = idx & 7;
+      const int64_t row = tile * kTileRows + r;
+      if (row < rows) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(buf + r * kTilePitch + 4 * c4);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(psi + row * D + k0 + 4 * c4)
+                     : "memory");
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  if (nq > 0) issue(0);
+  __syncthreads();  // L in shared memory
+  float acc[4][MB];
+  for (int64_t q = 0; q < nq; ++q) {
+    if (q % nk == 0) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int m = 0; m < MB; ++m) acc[i][m] = 0.f;
+    }
+    if (q + 1 < nq) {
+      issue(q + 1);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    __syncthreads();
+    const float *buf = as + (q & 1) * (kTileRows * kTilePitch);
+    const float *lk = ls + (size_t)(q % nk) * kTileK * 32 + 8 * w;
+#pragma unroll 2
+    for (int k4 = 0; k4 < kTileK / 4; ++k4) {
+      float4 a[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = *reinterpret_cast<const float4 *>(buf + (lane + 32 * i) * kTilePitch + 4 * k4);
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        float l[8];
+        *reinterpret_cast<float4 *>(l) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32);
+        if (MB > 4) *reinterpret_cast<float4 *>(l + 4) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32 + 4);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float x = kk == 0 ? a[i].x : kk == 1 ? a[i].y : kk == 2 ? a[i].z : a[i].w;
+#pragma unroll
+          for (int m = 0; m < MB; ++m) acc[i][m] = __fmaf_rn(l[m], x, acc[i][m]);
+        }
+      }
+    }
+    __syncthreads();  // the buffer is refilled two chunks later
+    if (q % nk == nk - 1) {
+      const int64_t tile = blockIdx.x + (q / nk) * gridDim.x;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int64_t row = tile * kTileRows + lane + 32 * i;
+        if (row >= rows) continue;
+        float *o = phi + row * M + MB * w;
+#pragma unroll
+        for (int m = 0; m < MB; ++m)
+          if (MB * w + m < M) o[m] = accumulate ? o[m] + acc[i][m] : acc[i][m];
+      }
+    }
+  }
+}
+
 int gridFor(int64_t rows) {
   int64_t b = (rows + kMomThreads - 1) / kMomThreads;
   const int64_t cap = 152 * 16;  // grid-stride beyond 16 resident blocks per SM
@@ -291,8 +391,40 @@ struct LTimesLaunch {
   }
 };
 
+template <int MB>
+void launchLTimesTile(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M, bool acc,
+                      cudaStream_t s) {
+  const size_t smem = sizeof(float) * ((size_t)D * 32 + 2 * kTileRows * kTilePitch);
+  setSmem(ltimes_tile_kernel<MB>, smem);
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ltimes_tile_kernel<MB>, kMomThreads, smem);
+  const int64_t ntiles = (rows + kTileRows - 1) / kTileRows;
+  const int64_t cap = (int64_t)nsm * (per > 0 ? per : 1);
+  const int grid = (int)(ntiles < cap ? (ntiles > 0 ? ntiles : 1) : cap);
+  ltimes_tile_kernel<MB><<<grid, kMomThreads, smem, s>>>(psi, phi, ell_dm, rows, D, M, acc);
+}
+
+// The register-tiled FP32 kernel when it applies (returns false otherwise).
+bool launchLTimesTiled(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M, bool acc,
+                       cudaStream_t s) {
+  if (D % kTileK != 0 || D > 1024 || M > 32 || M < 13) return false;
+  const int mb = (M + 3) / 4;
+  if (mb == 4) launchLTimesTile<4>(psi, phi, ell_dm, rows, D, M, acc, s);
+  else if (mb == 5) launchLTimesTile<5>(psi, phi, ell_dm, rows, D, M, acc, s);
+  else if (mb == 6) launchLTimesTile<6>(psi, phi, ell_dm, rows, D, M, acc, s);
+  else if (mb == 7) launchLTimesTile<7>(psi, phi, ell_dm, rows, D, M, acc, s);
+  else launchLTimesTile<8>(psi, phi, ell_dm, rows, D, M, acc, s);
+  return true;
+}
+bool launchLTimesTiled(const double *, double *, const double *, int64_t, int, int, bool, cudaStream_t) {
+  return false;
+}
+
 template <typename T>
 void launch_ltimes(const T *psi, T *phi, const T *ell_dm, int64_t rows, int D, int M, bool accumulate, cudaStream_t s) {
+  if (launchLTimesTiled(psi, phi, ell_dm, rows, D, M, accumulate, s)) return;
 #define KGB_L(MBV) LTimesLaunch<T, MBV>{psi, phi, ell_dm, rows, D, M, accumulate, s}
   byMoments<T, LTimesLaunch>(M, KGB_L(4), KGB_L(12), KGB_L(16), KGB_L(28), KGB_L(36), KGB_L(52), KGB_L(64));
 #undef KGB_L
