@@ -331,6 +331,106 @@ __global__ void __launch_bounds__(kMomThreads) ltimes_tile_kernel(const float *_
   }
 }
 
+// LPlusTimes, FP32, register-tiled (M <= 32, directions a multiple of 4): a
+// block takes 32-row tiles of phi_out (staged in shared memory, the next tile's
+// values loaded into registers while this one is multiplied) and sweeps the
+// directions 128 at a time; warp w accumulates rows 8w .. 8w+7, lane l the
+// directions 4l .. 4l+3 of the block.  Per 4 moments a thread reads its rows'
+// moments as 8 broadcasts and L+ as 4 contiguous 16-byte reads (128
+// multiply-adds per 12 reads), and each warp stores 512 contiguous bytes of a
+// row.  Every output is the FMA chain of lplusRow (ascending moments, then the
+// zero padding up to the moment class MB), so the results are the same bit
+// for bit -- also those of the fused sweep's prologue.
+constexpr int kPlusRows = 32;
+
+template <int MB>
+__global__ void __launch_bounds__(kMomThreads) lplus_tile_kernel(const float *__restrict__ phi_out,
+                                                                float *__restrict__ rhs,
+                                                                const float *__restrict__ ellp_dm, int64_t rows,
+                                                                int D, int M, bool accumulate) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *lp = reinterpret_cast<float *>(smem_raw);  // [MB][D]: L+ transposed, zero rows beyond M
+  float *po = lp + (size_t)MB * D;                   // [2][kPlusRows][MB]
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  for (int i = tid; i < MB * D; i += blockDim.x) {
+    const int m = i / D, d = i - m * D;
+    lp[i] = m < M ? ellp_dm[(int64_t)d * M + m] : 0.f;
+  }
+  constexpr int kPer = (kPlusRows * 32 + kMomThreads - 1) / kMomThreads;  // staged values per thread (M <= 32)
+  const int64_t ntiles = (rows + kPlusRows - 1) / kPlusRows;
+  float nxt[kPer];
+  auto fetch = [&](int64_t tile) {  // the tile's phi_out block is contiguous: rows * M values
+    const int64_t base = tile * kPlusRows * M;
+    const int64_t n = (tile * kPlusRows + kPlusRows <= rows ? kPlusRows : rows - tile * kPlusRows) * M;
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int idx = tid + i * kMomThreads;
+      nxt[i] = (idx < kPlusRows * M && idx < n) ? phi_out[base + idx] : 0.f;
+    }
+  };
+  auto stage = [&](float *buf) {
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int idx = tid + i * kMomThreads;
+      if (idx < kPlusRows * M) {
+        const int r = idx / M;
+        buf[r * MB + (idx - r * M)] = nxt[i];
+      }
+    }
+    for (int i = tid; i < kPlusRows * (MB - M); i += kMomThreads) {  // zero padding
+      const int r = i / (MB - M);
+      buf[r * MB + M + (i - r * (MB - M))] = 0.f;
+    }
+  };
+  int64_t tile = blockIdx.x;
+  if (tile < ntiles) fetch(tile);
+  for (int b = 0; tile < ntiles; tile += gridDim.x, b ^= 1) {
+    float *buf = po + b * (kPlusRows * MB);
+    stage(buf);
+    __syncthreads();  // L+ (first pass) and this tile's moments in shared memory
+    if (tile + gridDim.x < ntiles) fetch(tile + gridDim.x);
+    for (int d0 = 0; d0 < D; d0 += 128) {
+      const int d = d0 + 4 * lane;
+      if (d >= D) continue;
+      float acc[8][4];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[i][u] = 0.f;
+#pragma unroll
+      for (int m4 = 0; m4 < MB; m4 += 4) {
+        float4 e[4];
+#pragma unroll
+        for (int mm = 0; mm < 4; ++mm) e[mm] = *reinterpret_cast<const float4 *>(lp + (size_t)(m4 + mm) * D + d);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const float4 x = *reinterpret_cast<const float4 *>(buf + (8 * w + i) * MB + m4);
+          const float xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+          for (int mm = 0; mm < 4; ++mm) {
+            acc[i][0] = __fmaf_rn(e[mm].x, xv[mm], acc[i][0]);
+            acc[i][1] = __fmaf_rn(e[mm].y, xv[mm], acc[i][1]);
+            acc[i][2] = __fmaf_rn(e[mm].z, xv[mm], acc[i][2]);
+            acc[i][3] = __fmaf_rn(e[mm].w, xv[mm], acc[i][3]);
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int64_t row = tile * kPlusRows + 8 * w + i;
+        if (row >= rows) continue;
+        float4 *o = reinterpret_cast<float4 *>(rhs + row * D + d);
+        float4 v = make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+        if (accumulate) {
+          const float4 old = *o;
+          v = make_float4(old.x + v.x, old.y + v.y, old.z + v.z, old.w + v.w);
+        }
+        *o = v;
+      }
+    }
+  }
+}
+
 int gridFor(int64_t rows) {
   int64_t b = (rows + kMomThreads - 1) / kMomThreads;
   const int64_t cap = 152 * 16;  // grid-stride beyond 16 resident blocks per SM
@@ -430,9 +530,41 @@ void launch_ltimes(const T *psi, T *phi, const T *ell_dm, int64_t rows, int D, i
 #undef KGB_L
 }
 
+template <int MB>
+void launchLPlusTile(const float *phi_out, float *rhs, const float *ellp_dm, int64_t rows, int D, int M, bool acc,
+                     cudaStream_t s) {
+  const size_t smem = sizeof(float) * ((size_t)MB * D + 2 * kPlusRows * MB);
+  setSmem(lplus_tile_kernel<MB>, smem);
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, lplus_tile_kernel<MB>, kMomThreads, smem);
+  const int64_t ntiles = (rows + kPlusRows - 1) / kPlusRows;
+  const int64_t cap = (int64_t)nsm * (per > 0 ? per : 1);
+  const int grid = (int)(ntiles < cap ? (ntiles > 0 ? ntiles : 1) : cap);
+  lplus_tile_kernel<MB><<<grid, kMomThreads, smem, s>>>(phi_out, rhs, ellp_dm, rows, D, M, acc);
+}
+
+// The register-tiled FP32 kernel when it applies (returns false otherwise).  MB
+// is the moment class of lplusRow, so both add the same zero padding.
+bool launchLPlusTiled(const float *phi_out, float *rhs, const float *ellp_dm, int64_t rows, int D, int M, bool acc,
+                      cudaStream_t s) {
+  if (D % 4 != 0 || D > 2048 || M > 28) return false;
+  const int mb = moment_class(M);
+  if (mb == 4) launchLPlusTile<4>(phi_out, rhs, ellp_dm, rows, D, M, acc, s);
+  else if (mb == 12) launchLPlusTile<12>(phi_out, rhs, ellp_dm, rows, D, M, acc, s);
+  else if (mb == 16) launchLPlusTile<16>(phi_out, rhs, ellp_dm, rows, D, M, acc, s);
+  else launchLPlusTile<28>(phi_out, rhs, ellp_dm, rows, D, M, acc, s);
+  return true;
+}
+bool launchLPlusTiled(const double *, double *, const double *, int64_t, int, int, bool, cudaStream_t) {
+  return false;
+}
+
 template <typename T>
 void launch_lplustimes(const T *phi_out, T *rhs, const T *ellp_dm, int64_t rows, int D, int M, bool accumulate,
                        cudaStream_t s) {
+  if (launchLPlusTiled(phi_out, rhs, ellp_dm, rows, D, M, accumulate, s)) return;
 #define KGB_L(MBV) LPlusLaunch<T, MBV>{phi_out, rhs, ellp_dm, rows, D, M, accumulate, s}
   byMoments<T, LPlusLaunch>(M, KGB_L(4), KGB_L(12), KGB_L(16), KGB_L(28), KGB_L(36), KGB_L(52), KGB_L(64));
 #undef KGB_L
