@@ -198,11 +198,12 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * running LPlusTimes, with the SIMT kernel's arithmetic, so psi is unchanged;
  * rhs is then refreshed, as L+ phi_out, only when an entry point reads it --
  * download, kgb_lplustimes, the sweep entry points, kgb_balance, autotune);
- * "row_exponents" (FP64 with the tensor-core LTimes: 1 = the solver loop's
+ * "row_exponents" (1 = in FP64 with the tensor-core LTimes the solver loop's
  * sweep records the largest exponent of every (zone, group) row of psi, and
  * the next iteration's LTimes scales its digit split by it instead of reading
- * each row twice, and that LTimes records phi's largest exponent per (zone,
- * moment) for the tensor-core scattering's gathered rows likewise; the
+ * each row twice; that LTimes, or in the mixed form the register-tiled SIMT
+ * LTimes, records phi's largest exponent per (zone, moment) for the
+ * tensor-core scattering's gathered rows likewise; the
  * results are bit for bit those of 0; default 1; a fill of psi with 0
  * records zeros; any other write of psi -- upload, other fills,
  * kgb_sweep_subdomain, kgb_sweep_solver, the adjoint, a batched solve --

@@ -953,7 +953,7 @@ int prepareT(kgb_ctx *ctx) {
     if ((rc = dmalloc(ctx, &ctx->psi_exp, (size_t)(ctx->Z * ctx->G)))) return rc;
     ctx->psi_exp_valid = false;
   }
-  if (sizeof(T) == 8 && !ctx->phi_exp && (rc = dmalloc(ctx, &ctx->phi_exp, (size_t)(ctx->Z * ctx->M)))) return rc;
+  if (!ctx->phi_exp && (rc = dmalloc(ctx, &ctx->phi_exp, (size_t)(ctx->Z * ctx->M)))) return rc;
   return KGB_OK;
 }
 
@@ -1024,12 +1024,15 @@ int phiExpWidth(const kgb_ctx *ctx) {
   return (g > 0 && g < 32 && (g & (g - 1)) == 0) ? g : 0;
 }
 
-// The tensor-core LTimes (FP64, one K chunk) records phi's exponents per
-// (zone, moment) for the tensor-core scattering of the same iteration, which
-// then skips its own pass over each gathered row.
+// LTimes records phi's exponents per (zone, moment) for the tensor-core
+// scattering of the same iteration, which then skips its own pass over each
+// gathered row: the tensor-core LTimes in FP64 (one K chunk), the
+// register-tiled SIMT LTimes in the mixed form.
 bool phiExpUsable(const kgb_ctx *ctx) {
-  return ctx->prec == KGB_FP64 && ctx->allow_row_exp && ctx->phi_exp && ctx->tc_lt && ctx->use_tc_lt &&
-         ctx->D <= ctx->tc_lt_kpad && ctx->tc_sc && ctx->use_tc_sc && phiExpWidth(ctx) > 0;
+  if (!ctx->allow_row_exp || !ctx->phi_exp || !ctx->tc_sc || !ctx->use_tc_sc || phiExpWidth(ctx) == 0) return false;
+  const bool tensor = ctx->tc_lt && ctx->use_tc_lt;
+  if (ctx->prec == KGB_FP64) return tensor && ctx->D <= ctx->tc_lt_kpad;
+  return !tensor && ltimes_tiled_applies(ctx->D, ctx->M);
 }
 
 // rowexp: record psi's row exponents there (the caller zeroed it); null: psi
@@ -1252,7 +1255,15 @@ int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr, int *outexp = 
     }
     return KGB_OK;
   }
-  if (outexp) return fail(ctx, KGB_ERR_STATE, "phi exponent record needs the tensor-core LTimes");
+  if (outexp) {  // mixed form: the register-tiled SIMT LTimes records phi's exponents
+    if (ctx->prec != KGB_MIXED || acc) return fail(ctx, KGB_ERR_STATE, "phi exponent record needs a fresh LTimes");
+    CK(cudaMemsetAsync(outexp, 0, ctx->Z * ctx->M * sizeof(int), ctx->stream));
+    if (!launch_ltimes_record(as<float>(ctx->psi), as<float>(ctx->phi), as<float>(ctx->ell), rows, ctx->D, ctx->M,
+                              outexp, phiExpWidth(ctx), ctx->G, ctx->stream))
+      return fail(ctx, KGB_ERR_STATE, "phi exponent record needs the tiled LTimes");
+    CKN(1);
+    return KGB_OK;
+  }
   if (ctx->prec == KGB_FP64)
     launch_ltimes<double>(as<double>(ctx->psi), as<double>(ctx->phi), as<double>(ctx->ell), rows, ctx->D, ctx->M, acc, ctx->stream);
   else
@@ -1346,12 +1357,12 @@ int scatterTensor(kgb_ctx *ctx, bool acc, const int *rowexp) {
   return KGB_OK;
 }
 
-// rowexp (FP64 tensor path): phi's exponents per (zone, moment) recorded by the
+// rowexp (tensor path): phi's exponents per (zone, moment) recorded by the
 // LTimes that wrote phi, or null.
 int doScattering(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr) {
   FamScope fs(ctx, "scattering");
   if (ctx->tc_sc && ctx->use_tc_sc)
-    return ctx->prec == KGB_FP64 ? scatterTensor<double>(ctx, acc, rowexp) : scatterTensor<float>(ctx, acc, nullptr);
+    return ctx->prec == KGB_FP64 ? scatterTensor<double>(ctx, acc, rowexp) : scatterTensor<float>(ctx, acc, rowexp);
   ScatterArgsBase a = scatterArgs(ctx);
   if (ctx->prec == KGB_FP64)
     launch_scattering<double>(as<double>(ctx->phi), as<double>(ctx->phi_out), as<double>(ctx->sigsT), a, acc, ctx->stream);

@@ -94,6 +94,15 @@ template <typename T>
 void launch_ltimes(const T *psi, T *phi, const T *ell_dm, int64_t rows, int D, int M, bool accumulate, cudaStream_t s);
 template <typename T>
 void launch_lplustimes(const T *phi_out, T *rhs, const T *ellp_dm, int64_t rows, int D, int M, bool accumulate, cudaStream_t s);
+// FP32 LTimes (phi = L psi, not accumulated) through the register-tiled kernel,
+// recording phi's largest biased exponent per (zone, moment) over the zone's
+// groups into outexp[zone * M + m] (atomic max; zeroed by the caller), reduced
+// over runs of rexp_w lanes (32, or the group count G when that is a power of
+// two below 32).  Returns false, launching nothing, when the tiled kernel does
+// not apply (ltimes_tiled_applies).
+bool ltimes_tiled_applies(int D, int M);
+bool launch_ltimes_record(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M,
+                          int *outexp, int rexp_w, int G, cudaStream_t s);
 
 struct ScatterArgsBase {
   int64_t Z;                  // zones (rows = Z * destination groups); with zlist, the list's length

@@ -249,7 +249,8 @@ template <int MB>
 __global__ void __launch_bounds__(kMomThreads) ltimes_tile_kernel(const float *__restrict__ psi,
                                                                  float *__restrict__ phi,
                                                                  const float *__restrict__ ell_dm, int64_t rows,
-                                                                 int D, int M, bool accumulate) {
+                                                                 int D, int M, bool accumulate, int *outexp,
+                                                                 int rexp_w, int G) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float *ls = reinterpret_cast<float *>(smem_raw);  // [D][32]: warp w's moments at 8w .. 8w+MB-1
   float *as = ls + (size_t)D * 32;                   // [2][kTileRows][kTilePitch]
@@ -321,7 +322,27 @@ __global__ void __launch_bounds__(kMomThreads) ltimes_tile_kernel(const float *_
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const int64_t row = tile * kTileRows + lane + 32 * i;
-        if (row >= rows) continue;
+        const bool valid = row < rows;
+        if (outexp) {
+          // phi's exponent record for the gathered scattering (not accumulated): the
+          // 32 lanes hold consecutive (zone, group) rows, one warp reduction per moment
+          // over each run of rows of one zone, one atomic per run
+          const unsigned live = __ballot_sync(0xffffffffu, valid);
+          const unsigned rw = (unsigned)rexp_w;
+          const unsigned run = (rw >= 32u ? 0xffffffffu : (((1u << rw) - 1u) << (lane & ~(rw - 1u)))) & live;
+          if (valid) {
+            const int64_t zb = (row / G) * M;
+#pragma unroll
+            for (int m = 0; m < MB; ++m) {
+              if (MB * w + m < M) {
+                const unsigned ex = (__float_as_uint(acc[i][m]) >> 23) & 0xFFu;
+                const unsigned mx = __reduce_max_sync(run, ex);
+                if ((lane & (rw - 1u)) == 0) atomicMax(outexp + zb + MB * w + m, (int)mx);
+              }
+            }
+          }
+        }
+        if (!valid) continue;
         float *o = phi + row * M + MB * w;
 #pragma unroll
         for (int m = 0; m < MB; ++m)
@@ -493,7 +514,7 @@ struct LTimesLaunch {
 
 template <int MB>
 void launchLTimesTile(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M, bool acc,
-                      cudaStream_t s) {
+                      cudaStream_t s, int *outexp = nullptr, int rexp_w = 32, int G = 1) {
   const size_t smem = sizeof(float) * ((size_t)D * 32 + 2 * kTileRows * kTilePitch);
   setSmem(ltimes_tile_kernel<MB>, smem);
   int dev = 0, nsm = 0, per = 0;
@@ -503,23 +524,30 @@ void launchLTimesTile(const float *psi, float *phi, const float *ell_dm, int64_t
   const int64_t ntiles = (rows + kTileRows - 1) / kTileRows;
   const int64_t cap = (int64_t)nsm * (per > 0 ? per : 1);
   const int grid = (int)(ntiles < cap ? (ntiles > 0 ? ntiles : 1) : cap);
-  ltimes_tile_kernel<MB><<<grid, kMomThreads, smem, s>>>(psi, phi, ell_dm, rows, D, M, acc);
+  ltimes_tile_kernel<MB><<<grid, kMomThreads, smem, s>>>(psi, phi, ell_dm, rows, D, M, acc, outexp, rexp_w, G);
 }
+
+bool ltimes_tiled_applies(int D, int M) { return D % kTileK == 0 && D <= 1024 && M <= 32 && M >= 13; }
 
 // The register-tiled FP32 kernel when it applies (returns false otherwise).
 bool launchLTimesTiled(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M, bool acc,
-                       cudaStream_t s) {
-  if (D % kTileK != 0 || D > 1024 || M > 32 || M < 13) return false;
+                       cudaStream_t s, int *outexp = nullptr, int rexp_w = 32, int G = 1) {
+  if (!ltimes_tiled_applies(D, M)) return false;
   const int mb = (M + 3) / 4;
-  if (mb == 4) launchLTimesTile<4>(psi, phi, ell_dm, rows, D, M, acc, s);
-  else if (mb == 5) launchLTimesTile<5>(psi, phi, ell_dm, rows, D, M, acc, s);
-  else if (mb == 6) launchLTimesTile<6>(psi, phi, ell_dm, rows, D, M, acc, s);
-  else if (mb == 7) launchLTimesTile<7>(psi, phi, ell_dm, rows, D, M, acc, s);
-  else launchLTimesTile<8>(psi, phi, ell_dm, rows, D, M, acc, s);
+  if (mb == 4) launchLTimesTile<4>(psi, phi, ell_dm, rows, D, M, acc, s, outexp, rexp_w, G);
+  else if (mb == 5) launchLTimesTile<5>(psi, phi, ell_dm, rows, D, M, acc, s, outexp, rexp_w, G);
+  else if (mb == 6) launchLTimesTile<6>(psi, phi, ell_dm, rows, D, M, acc, s, outexp, rexp_w, G);
+  else if (mb == 7) launchLTimesTile<7>(psi, phi, ell_dm, rows, D, M, acc, s, outexp, rexp_w, G);
+  else launchLTimesTile<8>(psi, phi, ell_dm, rows, D, M, acc, s, outexp, rexp_w, G);
   return true;
 }
 bool launchLTimesTiled(const double *, double *, const double *, int64_t, int, int, bool, cudaStream_t) {
   return false;
+}
+
+bool launch_ltimes_record(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M,
+                          int *outexp, int rexp_w, int G, cudaStream_t s) {
+  return launchLTimesTiled(psi, phi, ell_dm, rows, D, M, false, s, outexp, rexp_w, G);
 }
 
 template <typename T>

@@ -20,11 +20,11 @@ pytestmark = pytest.mark.gpu
 KW = dict(zones=(10, 9, 8), groups=8, quad=(4, 8), legendre=3, geometry=1, scatter=1, gset=2, dset=8)
 
 
-def pair(kgb, **kw):
+def pair(kgb, precision=None, **kw):
     out = []
     for on in (0, 1):
         c = kgb.Context()
-        c.generate(precision=kgb.FP64, **dict(KW, **kw))
+        c.generate(precision=kgb.FP64 if precision is None else precision, **dict(KW, **kw))
         c.set_option("row_exponents", on)
         out.append(c)
     return out
@@ -141,3 +141,21 @@ def test_zero_fill_records_zero_exponents(kgb):
     assert b.get_option("psi_row_exponents_valid") == 1
     assert [a.iterate() for _ in range(3)] == [b.iterate() for _ in range(3)]
     same(a, b)
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(quad=(8, 16), legendre=4), dict(groups=64, legendre=4, zsets=(2, 1, 2)),
+                                dict(groups=12)])
+def test_mixed_form_phi_record_bitwise(kgb, kw):
+    # the mixed form's register-tiled LTimes records phi's exponents for the tensor-core scattering
+    a, b = pair(kgb, precision=kgb.MIXED, **kw)
+    pa = [a.iterate() for _ in range(4)]
+    pb = [b.iterate() for _ in range(4)]
+    assert b.get_option("phi_row_exponents_active") == int(kw.get("groups", 8) != 12)
+    assert b.get_option("psi_row_exponents_active") == 0 and b.get_option("scattering_tensor_active") == 1
+    assert pa == pb
+    same(a, b)
+    np.testing.assert_array_equal(a.solve(5), b.solve(5))
+    same(a, b)
+    ra, rb = a.solve_converged(1.0, 1e-5, 60), b.solve_converged(1.0, 1e-5, 60)
+    assert ra == rb
+    same(a, b, ("psi", "phi"))
