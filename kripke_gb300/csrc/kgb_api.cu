@@ -1841,12 +1841,15 @@ int instance_view(kgb_ctx *ctx, InstanceView *v) {
 int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s) {
   cudaStream_t keep = ctx->stream;
   ctx->stream = s;
+  // a batched iteration runs each problem's LTimes and then its scattering (same
+  // stream), so LTimes can record phi's exponents for the scattering
+  int *const pe = phiExpUsable(ctx) ? ctx->phi_exp : nullptr;
   int rc;
   switch (op) {
-    case InstanceOp::LTimes: rc = doLTimes(ctx, false); break;
+    case InstanceOp::LTimes: rc = doLTimes(ctx, false, nullptr, pe); break;
     case InstanceOp::LPlusTimes: rc = doLPlusTimes(ctx, false); break;
     default:
-      rc = doScattering(ctx, false);
+      rc = doScattering(ctx, false, pe);
       if (!rc) rc = doSource(ctx, q);
       break;
   }
