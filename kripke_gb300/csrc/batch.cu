@@ -44,6 +44,9 @@ struct kgb_batch {
   int rows_per_item = 1024;
   bool use_graph = true;
   int own_mode = -1;  // 1: each problem's own LTimes/scattering/LPlusTimes kernels; 0: batched SIMT; -1: by precision
+  // the problems' psi row-exponent records (FP64, views[i].psi_exp) hold for their current psi:
+  // set by a solve's reset and by every batched sweep, which records them; cleared by a new plan
+  bool rec_ok = false;
 
   // streams the per-problem moment kernels fork onto (graph branches when captured)
   static constexpr int kForks = 4;
@@ -236,6 +239,10 @@ int planT(kgb_batch *b) {
     a.w = v.w;
     a.vol = v.vol;
     a.vol_uniform = v.vol_uniform;
+    if (sizeof(T) == 8 && v.psi_exp) {  // record psi's row exponents for the problem's next LTimes
+      a.rowexp = v.psi_exp;
+      a.rexp_w = v.psi_exp_w;
+    }
     sa[i] = a;
   }
   // sweep work items by global step, then the plane zeroing ranges
@@ -260,6 +267,12 @@ int planT(kgb_batch *b) {
       const int64_t total = b->views[i].plane_chunk[k] * b->views[i].nsdom;
       for (int64_t e = 0; e < total; e += (int64_t)1 << 16) zero.push_back({i, k, e, std::min(total, e + ((int64_t)1 << 16))});
     }
+  for (int i = 0; i < n; ++i)
+    if (sa[i].rowexp) {  // zeroed with the planes: the sweep takes atomic maxima
+      const int64_t total = b->views[i].Z * b->views[i].G;
+      for (int64_t e = 0; e < total; e += (int64_t)1 << 16) zero.push_back({i, 3, e, std::min(total, e + ((int64_t)1 << 16))});
+    }
+  b->rec_ok = false;
   b->nsteps = maxsteps;
   b->nzero = (int)zero.size();
   SweepArgs<T> *sa_d = nullptr;
@@ -340,7 +353,8 @@ int forkPhase(kgb_batch *b, InstanceOp op) {
   BCK(cudaEventRecord(b->fork_ev, b->stream));
   for (int k = 0; k < kgb_batch::kForks; ++k) BCK(cudaStreamWaitEvent(b->aux[k], b->fork_ev, 0));
   for (size_t i = 0; i < b->inst.size(); ++i) {
-    const int rc = instance_op(b->inst[i], op, b->q, b->aux[i % kgb_batch::kForks]);
+    const int *rx = op == InstanceOp::LTimes && b->rec_ok ? b->views[i].psi_exp : nullptr;
+    const int rc = instance_op(b->inst[i], op, b->q, b->aux[i % kgb_batch::kForks], rx);
     if (rc) return fail(b, rc, "problem " + std::to_string(i) + ": " + kgb_last_error(b->inst[i]));
   }
   for (int k = 0; k < kgb_batch::kForks; ++k) {
@@ -387,6 +401,7 @@ int enqueueIteration(kgb_batch *b, double *pop_out, cudaEvent_t *ev = nullptr) {
   if (ev) BCK(cudaEventRecord(ev[3], b->stream));
   BatchSweepPlan p{b->sweep_items, b->step_off, b->nsteps, b->zero, b->nzero, b->bar, b->err_d};
   BCK(launch_batch_sweep<T>((const SweepArgs<T> *)b->sweep_args, p, b->tx, b->ty, b->sweep_grid, b->stream));
+  b->rec_ok = true;  // the sweep recorded psi's row exponents (FP64 problems with a record)
   if (ev) BCK(cudaEventRecord(ev[4], b->stream));
   launch_batch_pop_finish(b->slot_ptrs, b->slot_n, (int)b->inst.size(), pop_out, b->stream);
   if (ev) BCK(cudaEventRecord(ev[5], b->stream));
@@ -395,7 +410,11 @@ int enqueueIteration(kgb_batch *b, double *pop_out, cudaEvent_t *ev = nullptr) {
 }
 
 int enqueueSolve(kgb_batch *b, int niter) {
-  for (auto &v : b->views) BCK(cudaMemsetAsync(v.psi, 0, (size_t)v.Z * v.G * v.D * (b->prec == KGB_FP64 ? 8 : 4), b->stream));
+  for (auto &v : b->views) {
+    BCK(cudaMemsetAsync(v.psi, 0, (size_t)v.Z * v.G * v.D * (b->prec == KGB_FP64 ? 8 : 4), b->stream));
+    if (v.psi_exp) BCK(cudaMemsetAsync(v.psi_exp, 0, (size_t)v.Z * v.G * sizeof(int), b->stream));  // psi = 0
+  }
+  b->rec_ok = true;
   const int n = (int)b->inst.size();
   for (int it = 0; it < niter; ++it) {
     int rc = b->prec == KGB_FP64 ? enqueueIteration<double>(b, b->pop + (size_t)it * n)
@@ -705,6 +724,7 @@ int kgb_batch_profile(kgb_batch *b, double ms[5]) {
   BCK(cudaSetDevice(b->device));
   int rc = ensurePlan(b);
   if (rc || (rc = ensurePop(b, 1))) return rc;
+  b->rec_ok = false;  // psi may have been written through a problem's own context since
   cudaEvent_t ev[6];
   for (auto &e : ev) BCK(cudaEventCreate(&e));
   for (int rep = 0; rep < 2 && !rc; ++rep)  // the second iteration is measured

@@ -1834,11 +1834,13 @@ int instance_view(kgb_ctx *ctx, InstanceView *v) {
   x.cls = ctx->use_recip ? ctx->cls_d : nullptr;
   x.inv = ctx->use_recip ? ctx->inv_d : nullptr;
   x.gen = ctx->gen;
+  x.psi_exp = psiExpUsable(ctx) ? ctx->psi_exp : nullptr;
+  x.psi_exp_w = psiExpWidth(ctx);
   *v = x;
   return KGB_OK;
 }
 
-int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s) {
+int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s, const int *psi_exp) {
   cudaStream_t keep = ctx->stream;
   ctx->stream = s;
   // a batched iteration runs each problem's LTimes and then its scattering (same
@@ -1846,7 +1848,7 @@ int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s) {
   int *const pe = phiExpUsable(ctx) ? ctx->phi_exp : nullptr;
   int rc;
   switch (op) {
-    case InstanceOp::LTimes: rc = doLTimes(ctx, false, nullptr, pe); break;
+    case InstanceOp::LTimes: rc = doLTimes(ctx, false, psi_exp, pe); break;
     case InstanceOp::LPlusTimes: rc = doLPlusTimes(ctx, false); break;
     default:
       rc = doScattering(ctx, false, pe);

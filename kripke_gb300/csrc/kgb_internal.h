@@ -273,13 +273,16 @@ struct InstanceView {
   const uint16_t *cls;  // tabulated sweep reciprocals, or null (divide per cell)
   const void *inv;      // [nclass][D] in the context's precision
   uint64_t gen;         // the context's table generation: changes whenever a table, tile list or kernel choice changes
+  int *psi_exp;         // psi's row-exponent record for the problem's tensor-core LTimes, or null
+  int psi_exp_w;        // lanes of one group in the sweep's chain order (rexp_w)
 };
 int instance_view(kgb_ctx *ctx, InstanceView *v);
 // One of the context's own iteration kernels, launched on stream s with the
 // kernels the context chooses (tensor-core or SIMT): LTimes (phi = L psi),
 // LPlusTimes (rhs = L+ phi_out), or scattering then source (phi_out = S phi + q).
+// psi_exp (LTimes): psi's row exponents as the batched sweep recorded them, or null.
 enum class InstanceOp { LTimes, Scatter, LPlusTimes };
-int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s);
+int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s, const int *psi_exp = nullptr);
 
 // Response, adjoint source and gradients (adjoint.cu).
 struct MixArgs {

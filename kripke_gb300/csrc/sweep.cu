@@ -428,6 +428,10 @@ __global__ void __launch_bounds__(kSweepThreads) batch_sweep_kernel(const SweepA
   for (int i = blockIdx.x; i < p.nzero; i += gridDim.x) {
     const BatchZero z = p.zero[i];
     const SweepArgs<T> &a = inst[z.inst];
+    if (z.plane == 3) {  // the problem's psi row-exponent record
+      for (int64_t e = z.begin + threadIdx.x; e < z.end; e += blockDim.x) a.rowexp[e] = 0;
+      continue;
+    }
     T *base = z.plane == 0 ? a.iplane : (z.plane == 1 ? a.jplane : a.kplane);
     for (int64_t e = z.begin + threadIdx.x; e < z.end; e += blockDim.x) base[e] = T(0);
   }
