@@ -1000,8 +1000,7 @@ int buildTiles(kgb_ctx *ctx) {
 // ---------------------------------------------------------------------------
 // Lanes of one group in the sweep's chain order (chains run over a direction
 // set's directions fastest), for the sweep's row-exponent reduction; 0 when a
-// warp's groups are not aligned runs of a power-of-two length (the sweep then
-// matches lanes by group index).
+// warp's groups are not aligned runs of a power-of-two length.
 int psiExpWidth(const kgb_ctx *ctx) {
   const int ds = ctx->Ds;
   if (ds % 32 == 0) return 32;
@@ -1013,7 +1012,7 @@ int psiExpWidth(const kgb_ctx *ctx) {
 // over each row.
 bool psiExpUsable(const kgb_ctx *ctx) {
   return ctx->prec == KGB_FP64 && ctx->allow_row_exp && ctx->psi_exp && ctx->tc_lt && ctx->use_tc_lt &&
-         ctx->D <= ctx->tc_lt_kpad;
+         ctx->D <= ctx->tc_lt_kpad && psiExpWidth(ctx) > 0;
 }
 
 // Lanes of one zone in the tensor-core LTimes' epilogue (one lane per (zone,

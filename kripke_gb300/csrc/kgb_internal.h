@@ -63,7 +63,7 @@ struct SweepArgs {
   // row exponents for the next LTimes (FP64): rowexp[z*G + g] = max over the
   // row's swept psi of the biased exponent (atomic max, zeroed before the
   // sweep), or null.  rexp_w lanes share a group (a power of two <= 32 that
-  // divides Ds, or 32 when 32 divides Ds); 0: lanes are matched by group.
+  // divides Ds, or 32 when 32 divides Ds).
   int *rowexp;
   int rexp_w;
 };

@@ -112,17 +112,9 @@ __device__ __forceinline__ void cpAsync(T *dst, const T *src) {
 // rexp_w lanes (each run names only its own lanes); four shuffle steps
 // instead cost the FP64 sweep of a 64^3-zone, 64-group, 128-direction
 // problem 1.1 ms per iteration, this 0.3.
-// rexp_w = 0: a direction set's length is not a power of two, so a group's
-// lanes are found by matching the group index (one match per cell).
-__device__ __forceinline__ void rowExpMax(int *rowexp, int w, unsigned mask, double ps, int64_t row, int gl) {
+__device__ __forceinline__ void rowExpMax(int *rowexp, int w, unsigned mask, double ps, int64_t row) {
   const unsigned ex = (unsigned)((__double_as_longlong(ps) >> 52) & 0x7FFu);
   const unsigned lane = threadIdx.x & 31u;
-  if (w == 0) {
-    const unsigned run = __match_any_sync(mask, gl);
-    const unsigned m = __reduce_max_sync(run, ex);
-    if (lane == (unsigned)(__ffs(run) - 1)) atomicMax(rowexp + row, (int)m);
-    return;
-  }
   const unsigned run = w >= 32 ? mask : (((1u << w) - 1u) << (lane & ~(unsigned)(w - 1))) & mask;
   const unsigned m = __reduce_max_sync(run, ex);
   if ((lane & (unsigned)(w - 1)) == 0) atomicMax(rowexp + row, (int)m);
@@ -339,7 +331,7 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
           }
           psi[e] = ps;
           if constexpr (sizeof(T) == 8) {
-            if (a.rowexp) rowExpMax(a.rowexp, a.rexp_w, rmask, ps, z * a.G + g, gl);
+            if (a.rowexp) rowExpMax(a.rowexp, a.rexp_w, rmask, ps, z * a.G + g);
           }
           lf = T(2) * ps - lf;
           fr[ii] = T(2) * ps - fr[ii];

@@ -60,15 +60,11 @@ def test_iterates_bitwise(kgb, kw):
     same(a, b)
 
 
-@pytest.mark.parametrize("quad,dset", [((4, 6), 8), ((4, 12), 8), ((8, 12), 8)])
-def test_unaligned_direction_sets(kgb, quad, dset):
-    # 3, 6 or 12 directions per set: a warp's groups are not aligned power-of-two runs, so the
-    # sweep finds each group's lanes by matching the group index
-    a, b = pair(kgb, quad=quad, dset=dset)
-    assert [a.iterate() for _ in range(4)] == [b.iterate() for _ in range(4)]
-    assert b.get_option("psi_row_exponents_active") == 1 and b.get_option("moments_tensor_ltimes") == 1
-    same(a, b)
-    np.testing.assert_array_equal(a.solve(4), b.solve(4))
+def test_unaligned_direction_sets_fall_back(kgb):
+    # 3 directions per set: a warp's groups are not power-of-two runs, nothing is recorded
+    a, b = pair(kgb, quad=(4, 6))
+    assert [a.iterate() for _ in range(3)] == [b.iterate() for _ in range(3)]
+    assert b.get_option("psi_row_exponents_active") == 0 and b.get_option("moments_tensor_ltimes") == 1
     same(a, b)
 
 
