@@ -577,8 +577,10 @@ void launchLPlusTile(const float *phi_out, float *rhs, const float *ellp_dm, int
 // is the moment class of lplusRow, so both add the same zero padding.
 bool launchLPlusTiled(const float *phi_out, float *rhs, const float *ellp_dm, int64_t rows, int D, int M, bool acc,
                       cudaStream_t s) {
-  if (D % 4 != 0 || D > 2048 || M > 28) return false;
+  if (D % 4 != 0 || M > 28) return false;
   const int mb = moment_class(M);
+  // L+ stays in shared memory: at most 200 KB with the two moment tiles
+  if (sizeof(float) * ((size_t)mb * D + 2 * kPlusRows * mb) > 200 * 1024) return false;
   if (mb == 4) launchLPlusTile<4>(phi_out, rhs, ellp_dm, rows, D, M, acc, s);
   else if (mb == 12) launchLPlusTile<12>(phi_out, rhs, ellp_dm, rows, D, M, acc, s);
   else if (mb == 16) launchLPlusTile<16>(phi_out, rhs, ellp_dm, rows, D, M, acc, s);
