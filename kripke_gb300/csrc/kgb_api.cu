@@ -1248,6 +1248,7 @@ int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr, int *outexp = 
         tcRows<double>(ctx, as<double>(ctx->psi) + k0, as<double>(ctx->phi), ctx->D, ctx->M, K, kc, ctx->M, 1, img,
                        ex, acc || c > 0, false, one ? rowexp : nullptr, outexp);
       } else {
+        if (outexp) return fail(ctx, KGB_ERR_STATE, "phi exponent record: not on the FP32 tensor-core LTimes");
         tcRows<float>(ctx, as<float>(ctx->psi) + k0, as<float>(ctx->phi), ctx->D, ctx->M, K, kc, ctx->M, 1, img, ex,
                       acc || c > 0, false);
       }
