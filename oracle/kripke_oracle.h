@@ -6,12 +6,16 @@
  * scheduler and the steady-state loop).  Only tests/, __graft_entry__.smoke()
  * and bench.py's CPU-baseline leg may load it; the product path never does.
  *
- * Parity status: the reference (LLNL Kripke v1.2.x) cannot be compiled here --
- * every kernel is a RAJA lambda and RAJA/camp/BLT are absent -- so this
- * oracle is NOT pinned against reference binaries ("parity unpinned" against
- * the reference itself).  It is pinned against analytic known answers
- * (closed-form diamond difference, pure absorber, quadrature identities,
- * exact material volumes) in tests/test_oracle.py.
+ * Parity status: pinned to the reference itself.  oracle/ref_build.sh compiles
+ * the reference's own sources (LLNL Kripke v1.2.x: generator, Kernel::*,
+ * SweepSolver, SteadyStateSolver) against a project-written stand-in for the
+ * RAJA loop names (oracle/refshim/), and this oracle equals that build bit for
+ * bit -- every generated input, every kernel's output and the solved
+ * psi/phi/phi_out/rhs -- on every configuration tests/test_ref_pin.py checks,
+ * live and against the golden records in tests/golden/ (the particle count
+ * differs by summation order only).  It is also pinned by analytic known
+ * answers (closed-form diamond difference, pure absorber, quadrature
+ * identities, exact material volumes) in tests/test_oracle.py.
  *
  * Data model: every field is stored exactly as the reference's
  * Core::Field stores it -- one chunk per subdomain of the field's partition
