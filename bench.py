@@ -43,7 +43,7 @@ WORKLOAD = dict(zones=(64, 64, 64), groups=64, quad=(8, 16), legendre=4, gset=1,
 WORKLOAD_NAME = "kripke 64^3 zones x 64 groups x 128 GL directions, P4, cube100, downscatter, DGZ, dset 8"
 # bounded CPU sample: same physics and per-zone work, 32^3 zones (1/8 of the unknowns)
 CPU_SAMPLE = dict(WORKLOAD, zones=(32, 32, 32))
-FP64_PEAK_GFLOPS = 1196.0  # DFMA rate measured on this machine's GB300 (profiles/fp64_peak_gb300.md)
+FP64_PEAK_GFLOPS = 1196.0  # DFMA rate kripke_gb300/bin/peak_probe measured on a GB300 at 2,070 MHz (fallback only)
 MIXED_PHI_ITERS = 20  # the mixed form's phi error is taken against FP64 after this many iterations
 # adjoint gradient workload: cross sections of the reference problem, +-20% per group, isotropic P0
 ADJ_WORKLOAD = dict(zones=(32, 32, 32), groups=32, quad=96, legendre=4, gset=1, dset=8, geometry=1, scatter=0,
@@ -56,15 +56,20 @@ ADJ_NAME = ("32^3 zones x 32 groups x 96 directions, P4, cube100, isotropic P0 w
             "absorption in the detector block [80,100]^3 cm")
 
 
-def fp64_peak():
-    """FP64 FMA rate of this GPU from kripke_gb300/bin/peak_probe; the recorded figure if it cannot run."""
+def fp64_peak(device=0):
+    """FP64 FMA rate of this GPU from kripke_gb300/bin/peak_probe, with the SM clock sampled while it
+    ran (so the roof can be audited as rate / clock); the recorded figure if the probe cannot run."""
     probe = os.path.join(ROOT, "kripke_gb300", "bin", "peak_probe")
+    clocks = ClockSampler(device)
     try:
+        clocks.start()
         out = subprocess.run([probe], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=60)
+        clk = clocks.stop()
         v = json.loads(out.stdout.strip().splitlines()[-1])["fp64_fma_gflops"]
-        return float(v), "measured live by kripke_gb300/bin/peak_probe (MEASURED_PEAKS.json has no FP64 figure)"
+        return float(v), "measured live by kripke_gb300/bin/peak_probe (MEASURED_PEAKS.json has no FP64 figure)", clk
     except Exception:
-        return FP64_PEAK_GFLOPS, "recorded probe figure (profiles/fp64_peak_gb300.md)"
+        clocks.stop()
+        return FP64_PEAK_GFLOPS, "recorded peak_probe figure at 2,070 MHz (the probe could not run)", None
 
 
 def unknowns(w):
@@ -285,6 +290,87 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     return out
 
 
+def phi_errors(got, want):
+    """max|got - want| / max|want| and the 2-norm ratio."""
+    import numpy as np
+    got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+    d = got - want
+    return {"max_rel": float(np.abs(d).max() / np.abs(want).max()),
+            "l2_rel": float(np.linalg.norm(d) / np.linalg.norm(want))}
+
+
+# the CPU configuration (16^3 zones on the cube, 32 identical groups, 96 directions, P4, 10 iterations)
+C0 = dict(zones=(16, 16, 16), groups=32, legendre=4, gset=1, dset=8, geometry=1, scatter=0, layout="DGZ")
+C0_ITERS = 10
+PARITY_TOL = {"fp64": 1e-12, "mixed": 1e-6}
+
+
+def fp64_parity(local, w, niter, threads, with_mixed):
+    """One problem solved by the FP64 GPU path and by the oracle (which reproduces the reference's own
+    code bit for bit; tests/test_ref_pin.py): phi, every iteration's particle count and the balance
+    terms; optionally the mixed form's phi against both."""
+    import numpy as np
+    from kripke_gb300 import abi
+    from oracle import pyoracle
+    ctx = abi.Context(local)
+    ctx.generate(**w)
+    part = ctx.solve(niter)
+    phi = ctx.download("phi")
+    bal = ctx.balance()
+    ref = pyoracle.Problem(threads=threads, **w)
+    rpart = ref.solve(niter)
+    rphi = ref.get("phi")
+    rbal = ref.balance()
+    out = {"iterations": niter, "phi": phi_errors(phi, rphi),
+           "population_max_rel": max(abs(a - b) / abs(b) for a, b in zip(part, rpart)),
+           # emission, collision and leakage relative to themselves; the residual relative to the emission
+           "balance_max_rel": max([abs(bal[i] - rbal[i]) / abs(rbal[i]) for i in (0, 1, 2)] +
+                                  [abs(bal[4] - rbal[4]) / abs(rbal[0])])}
+    ctx.close()
+    if with_mixed:
+        m = abi.Context(local)
+        m.generate(precision=abi.MIXED, **w)
+        m.solve(niter)
+        mphi = m.download("phi")
+        out["mixed_phi_vs_fp64_gpu"] = phi_errors(mphi, phi)
+        out["mixed_phi_vs_oracle"] = phi_errors(mphi, rphi)
+        m.close()
+    ref.close()
+    return out
+
+
+def parity_report(local, line):
+    """Parity of every configuration, in the same run: the FP64 form against the oracle at 1e-12 and
+    the mixed form's phi against FP64 at 1e-6."""
+    threads = os.cpu_count() or 1
+    out = {"tolerance": PARITY_TOL,
+           "oracle": "C++ restatement of the reference (oracle/), equal bit for bit to the reference's own "
+                     "code on the recorded configurations (tests/test_ref_pin.py, tests/golden/)",
+           "errors": "phi: max|d|/max|ref| and 2-norm ratio; populations of every iteration; balance terms"}
+    progress("parity: c0, dummy S2")
+    out["c0_s2_96"] = fp64_parity(local, dict(C0, quad=96), C0_ITERS, threads, True)
+    progress("parity: c0, Gauss-Legendre")
+    out["c0_gl_8x12"] = fp64_parity(local, dict(C0, quad=(8, 12)), C0_ITERS, threads, True)
+    progress("parity: c1 physics at 32^3")
+    out["c1_physics_32cube"] = fp64_parity(local, CPU_SAMPLE, 3, threads, False)
+    mixed = {"c0_s2_96": out["c0_s2_96"]["mixed_phi_vs_fp64_gpu"]["max_rel"],
+             "c0_gl_8x12": out["c0_gl_8x12"]["mixed_phi_vs_fp64_gpu"]["max_rel"]}
+    if "mixed" in line:
+        mixed["c2"] = line["mixed"]["phi_rel_err_vs_fp64"]
+    if "adjoint" in line:
+        mixed["c3_forward"] = line["adjoint"]["mixed"]["phi_rel_err_vs_fp64"]["max_rel"]
+    if "batch" in line:
+        mixed["c4_worst_problem"] = line["batch"]["mixed_phi_vs_fp64"]["max_rel_err_max"]
+    out["mixed_phi_max_rel_vs_fp64"] = mixed
+    fp64 = [max(v["phi"]["max_rel"], v["population_max_rel"], v["balance_max_rel"])
+            for k, v in out.items() if isinstance(v, dict) and "phi" in v]
+    out["fp64_worst"] = max(fp64)
+    out["mixed_worst"] = max(mixed.values())
+    out["all_within_tolerance"] = bool(out["fp64_worst"] <= PARITY_TOL["fp64"] and
+                                       out["mixed_worst"] <= PARITY_TOL["mixed"])
+    return out
+
+
 def adjoint_report(local, fd_params=3):
     """Gradient / forward time and accuracy of the adjoint at the adjoint workload, FP64 and mixed."""
     import numpy as np
@@ -297,7 +383,7 @@ def adjoint_report(local, fd_params=3):
         return r, time.perf_counter() - t0
 
     res = {"workload": ADJ_NAME, "unknowns": unknowns(ADJ_WORKLOAD)}
-    grads = {}
+    grads, phis = {}, {}
     # FP64 solves to 1e-12; the mixed form, whose FP32 change stalls near 1e-7 while the far
     # (detector) region is still converging, runs the FP64 solves' iteration counts
     counts = {}
@@ -309,6 +395,7 @@ def adjoint_report(local, fd_params=3):
         ctx.solve_converged(1.0, tol, nf)  # builds the tables; untimed
         ctx.adjoint_solve(tol, na)
         (fit, fch), t_fwd = timed(lambda: ctx.solve_converged(1.0, tol, nf))
+        phis[name] = ctx.download("phi")
         (ait, ach), t_adj = timed(lambda: ctx.adjoint_solve(tol, na))
         counts = {"fwd": fit, "adj": ait}
         g, t_grad = timed(ctx.gradient)
@@ -349,6 +436,8 @@ def adjoint_report(local, fd_params=3):
             r["fd_max_rel_err"] = max(e["rel_err"] for e in errs)
         res[name] = r
         ctx.close()
+    res["mixed"]["phi_rel_err_vs_fp64"] = phi_errors(phis["mixed"], phis["fp64"])
+    del phis
     ref, got = grads["fp64"], grads["mixed"]
     res["mixed"]["grad_rel_err_vs_fp64"] = max(
         float(np.abs(got[1] - ref[1]).max() / np.abs(ref[1]).max()),
@@ -362,6 +451,7 @@ def batch_report(local, problems=BATCH_PROBLEMS, niter=10):
     from kripke_gb300.batching import uneven_inputs, unknowns as problem_unknowns
     name = BATCH_NAME if problems == BATCH_PROBLEMS else BATCH_NAME.replace("48 independent", "%d independent" % problems)
     out = {"workload": name, "iterations_per_solve": niter}
+    kept = {}
     for name, prec in (("mixed", abi.MIXED), ("fp64", abi.FP64)):
         inputs = uneven_inputs(problems, seed=2026, precision=prec)
         U = sum(problem_unknowns(x) for x in inputs)
@@ -390,6 +480,14 @@ def batch_report(local, problems=BATCH_PROBLEMS, niter=10):
                      "one_by_one": {"value": U / t_seq, "ms_per_iteration": t_seq * 1e3,
                                     "how": "each problem's own context, default options, solved in turn"},
                      "speedup_vs_one_by_one": t_seq / t_batch}
+        kept[name] = b
+    # each problem's mixed phi after the solve against its FP64 context's (same inputs, same iterations)
+    errs = [phi_errors(kept["mixed"].context(i).download("phi"), kept["fp64"].context(i).download("phi"))
+            for i in range(len(kept["fp64"]))]
+    out["mixed_phi_vs_fp64"] = {"problems": len(errs), "iterations": niter,
+                                "max_rel_err_max": max(e["max_rel"] for e in errs),
+                                "l2_rel_err_max": max(e["l2_rel"] for e in errs)}
+    for b in kept.values():
         b.close()
     return out
 
@@ -483,9 +581,10 @@ def run_gpu(args, world, rank, local):
     flops, nbytes = alg[dom]["flops"], alg[dom]["bytes"]
     if precision == abi.FP64:
         achieved = flops / (dom_ms * 1e-3) / 1e9
-        p64, p64_src = fp64_peak()
+        p64, p64_src, p64_clk = fp64_peak(local)
         roof = {"bound": "fp64", "achieved": achieved, "peak": p64, "unit": "GFLOP/s",
                 "frac": achieved / p64, "traffic": None, "kernel": dom, "peak_source": p64_src,
+                "peak_probe_clocks": p64_clk,
                 "hbm": {"achieved": nbytes / (dom_ms * 1e-3) / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
                         "frac": nbytes / (dom_ms * 1e-3) / 1e9 / pk["hbm_gbs"]}}
     else:
@@ -515,23 +614,31 @@ def run_gpu(args, world, rank, local):
         "gpu_launches": launches,
         "clocks": clk,
         "e2e": {"value": e2e_value, "unit": "unknowns/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * niter,
-                "step": "upload all inputs from pinned host memory + %d-iteration solve + populations to host" % niter},
+                "step": "upload all inputs from pinned host memory + %d-iteration solve + populations to host" % niter,
+                "read_back": "the %d particle counts (the figure of merit); phi and psi stay on the device" % niter},
         "population_after_timed_steps": part,
     }
+    mixed = None
     if rank == 0 and world == 1 and precision == abi.FP64 and not args.no_mixed:
         progress("mixed form")
-        line["mixed"] = mixed_report(args, local, w, ctx, ms)
+        mixed = mixed_report(args, local, w, ctx, ms)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, dt = cpu_run(CPU_SAMPLE, threads, 1, 2)
+        line["cpu_baseline"] = {"value": v, "unit": "unknowns/s", "cores": threads, "kind": "port",
+                                "sample": "oracle (OpenMP restatement, equal bit for bit to the reference's own "
+                                          "code on its recorded configurations) on the 32^3-zone sample, "
+                                          "2 iterations"}
     if rank == 0 and world == 1 and not args.no_adjoint:
         progress("adjoint")
         line["adjoint"] = adjoint_report(local)
     if rank == 0 and world == 1 and not args.no_batch:
         progress("batch")
         line["batch"] = batch_report(local, args.batch_problems)
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        v, dt = cpu_run(CPU_SAMPLE, threads, 1, 2)
-        line["cpu_baseline"] = {"value": v, "unit": "unknowns/s", "cores": threads, "kind": "port",
-                                "sample": "oracle (OpenMP restatement) on the 32^3-zone sample, 2 iterations"}
+    if mixed is not None:
+        line["mixed"] = mixed
+    if rank == 0 and world == 1 and not args.no_parity:
+        line["parity"] = parity_report(local, line)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -553,6 +660,7 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-form comparison")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint gradient report")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-problems report")
+    ap.add_argument("--no-parity", action="store_true", help="skip the per-configuration parity report")
     ap.add_argument("--batch-problems", type=int, default=BATCH_PROBLEMS,
                     help="problems in the batched report (profiling on a smaller batch)")
     args = ap.parse_args()

@@ -320,7 +320,10 @@ int kgb_batch_context(kgb_batch *b, int32_t index, kgb_ctx **ctx);
  * of a moment / scattering work item), "graph" (1: capture solves, the
  * default), "per_problem_kernels" (1: each problem's own LTimes,
  * scattering and LPlusTimes kernels; 0: batched SIMT; -1: by precision, the
- * default).  Read-only:
+ * default), "barrier_wait_ns" (how long a grid-barrier wait of the persistent
+ * sweep waits before it gives up; default 2e9; a solve whose wait gave up
+ * returns KGB_ERR_TIMEOUT with its results undefined, and the batch stays
+ * usable).  Read-only:
  * "graph_active" (the last solve replayed a graph),
  * "sweep_grid" (blocks of the persistent sweep), "sweep_steps",
  * "kernels_per_iteration". */

@@ -42,6 +42,8 @@ struct kgb_batch {
   // tuning (kgb_batch_set_option / kgb_batch_autotune)
   int tx = 2, ty = 2, tz = 8;
   int rows_per_item = 1024;
+  // a grid-barrier wait of the persistent sweep gives up after this long (then KGB_ERR_TIMEOUT)
+  int64_t barrier_wait_ns = 2000000000;
   bool use_graph = true;
   int own_mode = -1;  // 1: each problem's own LTimes/scattering/LPlusTimes kernels; 0: batched SIMT; -1: by precision
   // the problems' psi row-exponent records (FP64, views[i].psi_exp) hold for their current psi:
@@ -399,7 +401,8 @@ int enqueueIteration(kgb_batch *b, double *pop_out, cudaEvent_t *ev = nullptr) {
   BCK(cudaGetLastError());
   BCK(cudaMemsetAsync(b->bar, 0, 2 * sizeof(unsigned int), b->stream));
   if (ev) BCK(cudaEventRecord(ev[3], b->stream));
-  BatchSweepPlan p{b->sweep_items, b->step_off, b->nsteps, b->zero, b->nzero, b->bar, b->err_d};
+  BatchSweepPlan p{b->sweep_items, b->step_off, b->nsteps, b->zero,
+                   b->nzero,          b->bar,      b->err_d, (unsigned long long)b->barrier_wait_ns};
   BCK(launch_batch_sweep<T>((const SweepArgs<T> *)b->sweep_args, p, b->tx, b->ty, b->sweep_grid, b->stream));
   b->rec_ok = true;  // the sweep recorded psi's row exponents (FP64 problems with a record)
   if (ev) BCK(cudaEventRecord(ev[4], b->stream));
@@ -602,6 +605,9 @@ int kgb_batch_set_option(kgb_batch *b, const char *key, int64_t value) {
   } else if (k == "rows_per_item") {
     if (value < 32 || value > (1 << 20)) return fail(b, KGB_ERR_ARG, "rows_per_item must be in [32, 2^20]");
     b->rows_per_item = (int)value;
+  } else if (k == "barrier_wait_ns") {
+    if (value < 0 || value > 60000000000ll) return fail(b, KGB_ERR_ARG, "barrier_wait_ns must be in [0, 6e10]");
+    b->barrier_wait_ns = value;
   } else if (k == "graph") {
     b->use_graph = value != 0;
   } else if (k == "per_problem_kernels") {
@@ -620,6 +626,7 @@ int kgb_batch_get_option(kgb_batch *b, const char *key, int64_t *value) {
   if (k == "sweep_tile_xy") *value = b->tx * 10 + b->ty;
   else if (k == "sweep_tile_z") *value = b->tz;
   else if (k == "rows_per_item") *value = b->rows_per_item;
+  else if (k == "barrier_wait_ns") *value = b->barrier_wait_ns;
   else if (k == "graph") *value = b->use_graph;
   else if (k == "per_problem_kernels") *value = perProblem(b);
   else if (k == "graph_active") *value = b->graph_active;

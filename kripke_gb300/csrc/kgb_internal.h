@@ -249,6 +249,7 @@ struct BatchSweepPlan {
   int nzero;
   unsigned int *bar;      // [2] grid barrier: arrivals, generation (zero before a launch)
   int *err;               // set when a barrier wait gives up
+  unsigned long long wait_ns;  // a barrier wait gives up after this long (globaltimer ns)
 };
 template <typename T>
 int batch_sweep_grid(int tx, int ty, int nsm);

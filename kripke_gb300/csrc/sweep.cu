@@ -371,8 +371,6 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const __grid_
 }
 
 namespace {
-constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // a barrier wait gives up after 2 s
-
 __device__ __forceinline__ unsigned long long globalNs() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -381,10 +379,12 @@ __device__ __forceinline__ unsigned long long globalNs() {
 
 // Grid-wide barrier of a cooperative launch (all blocks resident): arrivals
 // are counted in bar[0]; the last block resets the count and advances the
-// generation bar[1], which the others wait on -- for at most
-// kBarrierLimitNs, after which they record the failure in *err and go on.
-// Once *err is set no block waits any more, so a failed launch ends quickly.
-__device__ __forceinline__ void gridBarrier(unsigned int *bar, unsigned int nblocks, int *err) {
+// generation bar[1], which the others wait on -- for at most limit_ns
+// (globaltimer), after which they record the failure in *err and go on.
+// Once *err is set no block waits any more, so a failed launch ends quickly;
+// its outputs are then undefined, but every access stays where it would be.
+__device__ __forceinline__ void gridBarrier(unsigned int *bar, unsigned int nblocks, int *err,
+                                            unsigned long long limit_ns) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned int *gen = bar + 1;
@@ -399,7 +399,7 @@ __device__ __forceinline__ void gridBarrier(unsigned int *bar, unsigned int nblo
       const unsigned long long t0 = globalNs();
       while (*gen == g && !*failed) {
         __nanosleep(64);
-        if (globalNs() - t0 > kBarrierLimitNs) {
+        if (globalNs() - t0 >= limit_ns) {
           atomicExch(err, 1);
           break;
         }
@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(kSweepThreads) batch_sweep_kernel(const SweepA
     T *base = z.plane == 0 ? a.iplane : (z.plane == 1 ? a.jplane : a.kplane);
     for (int64_t e = z.begin + threadIdx.x; e < z.end; e += blockDim.x) base[e] = T(0);
   }
-  gridBarrier(p.bar, nb, p.err);
+  gridBarrier(p.bar, nb, p.err, p.wait_ns);
   for (int st = 0; st < p.nsteps; ++st) {
     for (int i = p.step_off[st] + blockIdx.x; i < p.step_off[st + 1]; i += gridDim.x) {
       const int4 w = p.items[i];
@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(kSweepThreads) batch_sweep_kernel(const SweepA
       if (a.cls != nullptr) sweepTile<T, TX, TY, true, true, true, false, PFM>(a, w.y, w.z, w.w, ncb, rbuf);
       else sweepTile<T, TX, TY, false, true, true, false, PFM>(a, w.y, w.z, w.w, ncb, rbuf);
     }
-    gridBarrier(p.bar, nb, p.err);
+    gridBarrier(p.bar, nb, p.err, p.wait_ns);
   }
 }
 

@@ -110,3 +110,35 @@ def test_batch_rejects_unsupported(kgb):
         b.add(zones=(8, 8, 8), groups=4, quad=(4, 8), legendre=5)
     with pytest.raises(kgb.KgbError):
         b.solve(1)  # empty
+
+
+@pytest.mark.gpu
+def test_barrier_wait_gives_up_and_batch_recovers(kgb, oracle):
+    """Failure path of the persistent sweep's grid barrier: with a wait limit of 0 ns every wait
+    that finds the barrier still closed gives up at once, so the solve ends with KGB_ERR_TIMEOUT
+    and a readable message (no trap, no hang; the waits record the failure and the launch runs
+    to its end).  The batch stays usable: with the default limit restored, the next solve on the
+    same problems matches the oracle."""
+    inputs = small_set(kgb, n=4, seed=3)
+    b = make_batch(kgb, inputs, kgb.FP64)
+    assert b.get_option("barrier_wait_ns") == 2_000_000_000
+    b.set_option("barrier_wait_ns", 0)
+    with pytest.raises(kgb.KgbError) as err:
+        b.solve(3)
+    assert err.value.code == 4  # KGB_ERR_TIMEOUT
+    assert "gave up" in str(err.value)
+    b.set_option("barrier_wait_ns", 2_000_000_000)
+    parts = b.solve(5)
+    for i, inp in enumerate(inputs):
+        p = oracle.Problem(zones=(inp.nx, inp.ny, inp.nz), groups=inp.num_groups,
+                           quad=(inp.quad_num_polar, inp.quad_num_azimuthal), legendre=inp.legendre_order, gset=1,
+                           dset=8, geometry=1, scatter=1, sigt=tuple(inp.sigt), sigs=tuple(inp.sigs), seed=inp.seed)
+        np.testing.assert_allclose(parts[:, i], p.solve(5), rtol=1e-12)
+
+
+@pytest.mark.gpu
+def test_barrier_wait_option_is_checked(kgb):
+    b = make_batch(kgb, small_set(kgb, n=2, seed=4), kgb.FP64)
+    with pytest.raises(kgb.KgbError):
+        b.set_option("barrier_wait_ns", -1)
+    assert b.get_option("barrier_wait_ns") == 2_000_000_000
