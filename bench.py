@@ -261,10 +261,16 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     parts_fused = ctx.solve(MIXED_PHI_ITERS)
     phi_fused = ctx.download("phi")
     ctx.set_option("fused_sweep", 0)
+    kernels = {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "moments_tf32_ltimes",
+                                              "moments_tf32_lplustimes", "moments_tensor_ltimes",
+                                              "moments_tensor_lplustimes", "scattering_tensor_active")}
     parts = ctx.solve(MIXED_PHI_ITERS)
     fp64_ctx.solve(MIXED_PHI_ITERS)
     a, b = fp64_ctx.download("phi"), ctx.download("phi")
-    fused_same = bool(np.array_equal(parts, parts_fused) and np.array_equal(b, phi_fused))
+    # the fused sweep forms rhs with the SIMT LPlusTimes arithmetic: compare with that unfused iteration
+    ctx.set_option("moments_tf32", 0)
+    parts_simt = ctx.solve(MIXED_PHI_ITERS)
+    fused_same = bool(np.array_equal(parts_simt, parts_fused) and np.array_equal(ctx.download("phi"), phi_fused))
     del phi_fused
     err = float(np.abs(b - a).max() / np.abs(a).max())
     err_l2 = float(np.linalg.norm(b - a) / np.linalg.norm(a))
@@ -280,12 +286,13 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
                                  "all moments, groups and zones; also the 2-norm ratio and the max-abs relative "
                                  "error of moment 0" % MIXED_PHI_ITERS,
            "autotuned": tuned,
-           "kernels": {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "moments_tensor_ltimes",
-                                                      "moments_tensor_lplustimes", "scattering_tensor_active")},
+           "kernels": kernels,
            "fused_sweep": {"ms_per_step": ms_fused, "value": unknowns(w) / (ms_fused * 1e-3),
                            "speedup_vs_unfused": ms / ms_fused, "active": fused_active,
-                           "identical_to_unfused": fused_same,
-                           "what": "LPlusTimes formed inside the sweep (rhs neither written nor read), same tiles"}}
+                           "identical_to_unfused_simt": fused_same,
+                           "what": "LPlusTimes formed inside the sweep (rhs neither written nor read), same tiles; "
+                                   "compared bit for bit with the unfused iteration whose LPlusTimes is the SIMT "
+                                   "kernel (same arithmetic)"}}
     ctx.close()
     return out
 
@@ -321,11 +328,15 @@ def fp64_parity(local, w, niter, threads, with_mixed):
     rpart = ref.solve(niter)
     rphi = ref.get("phi")
     rbal = ref.balance()
+    names = ("emission", "collision", "leakage", "population", "residual")
     out = {"iterations": niter, "phi": phi_errors(phi, rphi),
            "population_max_rel": max(abs(a - b) / abs(b) for a, b in zip(part, rpart)),
-           # emission, collision and leakage relative to themselves; the residual relative to the emission
-           "balance_max_rel": max([abs(bal[i] - rbal[i]) / abs(rbal[i]) for i in (0, 1, 2)] +
-                                  [abs(bal[4] - rbal[4]) / abs(rbal[0])])}
+           # each balance term's difference relative to the emission (the balance's scale), and to itself
+           "balance_rel_vs_emission": {n: abs(bal[i] - rbal[i]) / abs(rbal[0]) for i, n in enumerate(names)},
+           "balance_rel_vs_itself": {n: abs(bal[i] - rbal[i]) / abs(rbal[i]) for i, n in enumerate(names)
+                                     if n != "residual" and rbal[i] != 0.0},
+           "balance_terms": dict(zip(names, rbal))}
+    out["balance_max_rel"] = max(out["balance_rel_vs_emission"].values())
     ctx.close()
     if with_mixed:
         m = abi.Context(local)
@@ -353,19 +364,28 @@ def parity_report(local, line):
     out["c0_gl_8x12"] = fp64_parity(local, dict(C0, quad=(8, 12)), C0_ITERS, threads, True)
     progress("parity: c1 physics at 32^3")
     out["c1_physics_32cube"] = fp64_parity(local, CPU_SAMPLE, 3, threads, False)
-    mixed = {"c0_s2_96": out["c0_s2_96"]["mixed_phi_vs_fp64_gpu"]["max_rel"],
-             "c0_gl_8x12": out["c0_gl_8x12"]["mixed_phi_vs_fp64_gpu"]["max_rel"]}
+    l2 = {"c0_s2_96": out["c0_s2_96"]["mixed_phi_vs_fp64_gpu"]["l2_rel"],
+          "c0_gl_8x12": out["c0_gl_8x12"]["mixed_phi_vs_fp64_gpu"]["l2_rel"]}
+    mx = {"c0_s2_96": out["c0_s2_96"]["mixed_phi_vs_fp64_gpu"]["max_rel"],
+          "c0_gl_8x12": out["c0_gl_8x12"]["mixed_phi_vs_fp64_gpu"]["max_rel"]}
     if "mixed" in line:
-        mixed["c2"] = line["mixed"]["phi_rel_err_vs_fp64"]
+        l2["c2"], mx["c2"] = line["mixed"]["phi_rel_err_l2"], line["mixed"]["phi_rel_err_vs_fp64"]
     if "adjoint" in line:
-        mixed["c3_forward"] = line["adjoint"]["mixed"]["phi_rel_err_vs_fp64"]["max_rel"]
+        e = line["adjoint"]["mixed"]["phi_rel_err_vs_fp64"]
+        l2["c3_forward"], mx["c3_forward"] = e["l2_rel"], e["max_rel"]
     if "batch" in line:
-        mixed["c4_worst_problem"] = line["batch"]["mixed_phi_vs_fp64"]["max_rel_err_max"]
-    out["mixed_phi_max_rel_vs_fp64"] = mixed
+        e = line["batch"]["mixed_phi_vs_fp64"]
+        l2["c4_worst_problem"], mx["c4_worst_problem"] = e["l2_rel_err_max"], e["max_rel_err_max"]
+    out["mixed_phi_l2_rel_vs_fp64"] = l2
+    out["mixed_phi_max_rel_vs_fp64"] = mx
+    out["criterion"] = ("FP64: phi max|d|/max|ref|, every iteration's population and every balance term relative "
+                        "to the emission, each <= 1e-12 against the oracle; mixed: phi 2-norm ratio <= 1e-6 "
+                        "against FP64 (max-abs relative reported beside it)")
     fp64 = [max(v["phi"]["max_rel"], v["population_max_rel"], v["balance_max_rel"])
             for k, v in out.items() if isinstance(v, dict) and "phi" in v]
     out["fp64_worst"] = max(fp64)
-    out["mixed_worst"] = max(mixed.values())
+    out["mixed_worst"] = max(l2.values())
+    out["mixed_worst_max_abs"] = max(mx.values())
     out["all_within_tolerance"] = bool(out["fp64_worst"] <= PARITY_TOL["fp64"] and
                                        out["mixed_worst"] <= PARITY_TOL["mixed"])
     return out

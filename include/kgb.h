@@ -184,7 +184,12 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * FP64 default; 0 = divide in every cell, the mixed default); "moments_tensor"
  * (1 = LTimes and LPlusTimes on the tensor cores with exact digit products when
  * the shapes fit; 0 = SIMT kernels; default: tensor for FP64, SIMT for the
- * mixed form); "scattering_tensor" (1 = the single-material zones' scattering on
+ * mixed form); "moments_tf32" (mixed form: 1 = LTimes and LPlusTimes as
+ * split-TF32 tensor-core GEMMs -- hi + lo operands, three products, FP32
+ * accumulation -- when moments <= 32 and there are at least 32 directions, a
+ * multiple of 4 (LTimes) or of 16 up to 256 (LPlusTimes); ahead of
+ * "moments_tensor"; the
+ * default; 0 = off); "scattering_tensor" (1 = the single-material zones' scattering on
  * the tensor cores, exact digit products, when groups <= 64; the default in both
  * forms);
  * "graph" (1 = kgb_solve replays a captured CUDA graph, the default);
@@ -346,8 +351,9 @@ int kgb_batch_launch_count(kgb_batch *b, int64_t *out);
 
 /* Allocation-free population edit.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory at the point they
- * need the particle count -- code recorded into a CUDA graph, frameworks that
- * own all device memory through their own pool, latency-bound loops.  Same
+ * need the particle count -- frameworks that own all device memory through
+ * their own pool allocator, latency-bound loops that cannot afford an
+ * allocation's implicit synchronisation.  Same
  * sum as kgb_population, over caller-owned device arrays: psi in the device
  * nesting [zone][group][direction] (FP64), w [directions], volume [zones];
  * *out (device memory) receives the FP64 result.  Allocates nothing: its
@@ -355,8 +361,11 @@ int kgb_batch_launch_count(kgb_batch *b, int64_t *out);
  * 33,554,432 rows (larger sizes return KGB_ERR_ARG).  Launches on `stream`
  * (a cudaStream_t, NULL = legacy default stream) on the current device; the
  * first call on each device looks up the scratch address and should come
- * before any stream capture.  Calls share the scratch: calls that overlap on
- * the GPU race.  err/err_len (optional) receive a message on failure. */
+ * before any stream capture; a cudaDeviceReset invalidates that address, so
+ * do not call it on a device after resetting it.  Calls share the scratch and
+ * it keeps the last call's contents: calls that overlap on the GPU race, so
+ * issue them on one stream.  err/err_len (optional) receive a message on
+ * failure. */
 int kgb_population_noalloc(const double *psi, const double *w, const double *volume, int64_t zones,
                            int32_t groups, int32_t directions, double *out, void *stream, char *err,
                            int32_t err_len);

@@ -336,7 +336,9 @@ class Context:
                     "kgb_autotune")
         return {"sweep_ms": ms.value, "sweep_tile_xy": xy.value, "sweep_tile_z": tz.value,
                 "ltimes_tensor": self.get_option("moments_tensor_ltimes"),
-                "lplustimes_tensor": self.get_option("moments_tensor_lplustimes")}
+                "lplustimes_tensor": self.get_option("moments_tensor_lplustimes"),
+                "ltimes_tf32": self.get_option("moments_tf32_ltimes"),
+                "lplustimes_tf32": self.get_option("moments_tf32_lplustimes")}
 
     def launch_count(self):
         n = ctypes.c_int64()

@@ -29,11 +29,12 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include"),
 ]
+CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")  # NVTX (header-only)
 CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall", "-I" + os.path.join(ROOT, "include"),
-             "-I" + HOST]
+             "-I" + HOST, "-I" + CUDA_INCLUDE]
 
 CU_SOURCES = ["kgb_api.cu", "sweep.cu", "moments.cu", "scatter.cu", "reduce.cu", "xpose.cu", "noalloc.cu", "tc_moments.cu",
-              "adjoint.cu", "batch.cu"]
+              "adjoint.cu", "batch.cu", "tf32_moments.cu"]
 CPP_SOURCES = ["generate.cpp"]
 HEADERS = ["kgb_internal.h", "kgb_layout.h", "exact_round.h"]
 
@@ -100,7 +101,7 @@ def build(force=False, verbose=False):
         hhdrs = [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]
         if force or _stale(CLI, host + hhdrs + [LIB]):
             _run(["g++"] + CXX_FLAGS + ["-o", CLI] + host +
-                 ["-L" + LIBDIR, "-lkgb", "-Wl,-rpath,$ORIGIN/../lib"])
+                 ["-L" + LIBDIR, "-lkgb", "-Wl,-rpath,$ORIGIN/../lib", "-ldl"])
     return LIB
 
 

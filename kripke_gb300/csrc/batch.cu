@@ -482,6 +482,12 @@ int checkBarrier(kgb_batch *b) {
     BCK(cudaMemsetAsync(b->err_d, 0, sizeof(int), b->stream));
     return fail(b, KGB_ERR_TIMEOUT, "a grid barrier of the persistent sweep gave up waiting");
   }
+  // the problems' own tensor-core kernels report their bounded waits through their contexts
+  if (perProblem(b))
+    for (size_t i = 0; i < b->inst.size(); ++i)
+      if (instance_check(b->inst[i]) != KGB_OK)
+        return fail(b, KGB_ERR_TIMEOUT,
+                    "problem " + std::to_string(i) + ": a tensor-core kernel's bounded wait gave up");
   return KGB_OK;
 }
 

@@ -1,5 +1,6 @@
 // KripkeCore.cpp -- input variables, arch/layout names, the GB300 context
 // variable, timers and problem generation for the kripke driver.
+#include <nvtx3/nvToolsExt.h>
 #include <strings.h>
 
 #include <algorithm>
@@ -111,7 +112,10 @@ static double nowSeconds() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// Every KRIPKE_TIMER region is also an NVTX range of the same name (the
+// reference opens a Caliper region there, src/Kripke/Timing.h:86-115).
 void Timing::start(const std::string &name) {
+  nvtxRangePushA(name.c_str());
   T &t = timers_[name];
   t.t0 = nowSeconds();
   t.running = true;
@@ -123,6 +127,7 @@ void Timing::stop(const std::string &name) {
   if (t.running) {
     t.elapsed += nowSeconds() - t.t0;
     t.running = false;
+    nvtxRangePop();
   }
 }
 

@@ -26,6 +26,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "kgb_internal.h"
 #include "kgb_layout.h"
 
@@ -85,6 +87,7 @@ struct kgb_ctx {
   cudaStream_t aux[kMaxSweepStreams - 1] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[kMaxSweepStreams - 1] = {};
   int sweep_streams = 2, max_streams = kMaxSweepStreams;
+  bool sweep_l2_hints = false;  // option sweep_l2_hints
   cudaStream_t stream = nullptr;
   std::string err;
   bool ready = false;
@@ -160,6 +163,12 @@ struct kgb_ctx {
   int *tc_lt_exp = nullptr, *tc_lp_exp = nullptr;
   int tc_lt_kpad = 0, tc_lp_nhalf = 0;
   int tc_lp_stages = 2, tc_lp_stage_out = 1;
+  // split-TF32 tensor-core LTimes / LPlusTimes of the mixed form (tf32_moments.cu): B images
+  // of the forward operators and of the adjoint's (exchanged by AdjointView)
+  bool allow_tf32 = true;                          // option "moments_tf32"
+  bool use_tf32_lt = true, use_tf32_lp = true;     // autotuner's choice
+  float *tf32_lt_img = nullptr, *tf32_lp_img = nullptr;
+  float *tf32_lt_img_adj = nullptr, *tf32_lp_img_adj = nullptr;
   // row exponents of psi for the tensor-core LTimes (FP64), written by the solver's sweep:
   // while psi_exp_valid, psi_exp[z*G + g] is the largest biased exponent in psi's row (z, g)
   int *psi_exp = nullptr;
@@ -423,12 +432,13 @@ void freeAll(kgb_ctx *c) {
                   c->gp_lo_adj, c->gp_hi_adj, c->colsum_d, c->e0_d, c->det_d, c->norm_d, c->resp_part, c->resp_d,
                   c->tc_lt_img_adj, c->tc_lp_img_adj, c->tc_lt_exp_adj, c->tc_lp_exp_adj, c->tc_sc_img,
                   c->tc_sc_img_adj, c->tc_sc_exp, c->tc_sc_exp_adj, c->pure_z,  // mixed_z lies inside pure_z
-                  c->psi_exp, c->phi_exp};
+                  c->psi_exp, c->phi_exp, c->tf32_lt_img, c->tf32_lp_img, c->tf32_lt_img_adj, c->tf32_lp_img_adj};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->psi = c->rhs = c->phi = c->phi_out = c->sigt = nullptr;
   c->psi_exp = c->phi_exp = nullptr;
   c->psi_exp_valid = false;
+  c->tf32_lt_img = c->tf32_lp_img = c->tf32_lt_img_adj = c->tf32_lp_img_adj = nullptr;
   c->plane[0] = c->plane[1] = c->plane[2] = nullptr;
   c->ell = c->ellp = c->sigsT = c->cx = c->cy = c->cz = nullptr;
   c->w_d = c->vol_d = nullptr;
@@ -475,17 +485,24 @@ void freeAll(kgb_ctx *c) {
 // ---------------------------------------------------------------------------
 // Timers (CUDA events on the context's stream)
 // ---------------------------------------------------------------------------
+// One kernel family's launches: an NVTX range on the calling thread (named
+// "kgb:<family>", visible to Nsight Systems and any NVTX tool; a no-op without
+// one) and, while timing is on, CUDA events on the context's stream.
 struct FamScope {
   kgb_ctx *c;
   TimerFam *fam = nullptr;
   cudaEvent_t b = nullptr;
   FamScope(kgb_ctx *ctx, const char *name) : c(ctx) {
+    char label[48];
+    std::snprintf(label, sizeof label, "kgb:%s", name);
+    nvtxRangePushA(label);
     if (!c->timing) return;
     fam = &c->fams[name];
     cudaEventCreate(&b);
     cudaEventRecord(b, c->stream);
   }
   ~FamScope() {
+    nvtxRangePop();
     if (!fam) return;
     cudaEvent_t e;
     cudaEventCreate(&e);
@@ -679,6 +696,51 @@ int planTensorMomentsFrom(kgb_ctx *ctx, const std::vector<double> &lt_src, const
   return KGB_OK;
 }
 
+// Split-TF32 plan of the mixed form: TF32 hi/lo images of L (K = directions,
+// N = moments padded to 16 or 32) and of L+ (K = moments padded to 32, N =
+// directions) from the [D][M] host tables the two operators read.
+int planTf32From(kgb_ctx *ctx, const std::vector<double> &lt_src, const std::vector<double> &lp_src, float **lt_img,
+                 float **lp_img) {
+  for (float **p : {lt_img, lp_img}) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
+  if (ctx->prec != KGB_MIXED || !ctx->allow_tf32) return KGB_OK;
+  const int D = ctx->D, M = ctx->M;
+  auto upload = [&](float **dst, const std::vector<float> &img) -> int {
+    int r;
+    if ((r = dmalloc(ctx, dst, img.size()))) return r;
+    if (cudaMemcpyAsync(*dst, img.data(), img.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      return fail(ctx, KGB_ERR_CUDA, "TF32 plan upload failed");
+    return (int)KGB_OK;
+  };
+  std::vector<float> b, img;
+  int rc;
+  if (tf32_ltimes_applies(D, M)) {
+    b.assign((size_t)D * M, 0.0f);  // B[d][m] = L(m, d), stored [D][M]
+    for (size_t i = 0; i < b.size(); ++i) b[i] = (float)lt_src[i];
+    tf32_build_b(b.data(), D, M, (D + 31) / 32 * 32, M <= 16 ? 16 : 32, img);
+    if ((rc = upload(lt_img, img))) return rc;
+  }
+  if (tf32_lplustimes_applies(D, M)) {
+    b.assign((size_t)M * D, 0.0f);  // B[m][d] = L+(d, m)
+    for (int d = 0; d < D; ++d)
+      for (int m = 0; m < M; ++m) b[(size_t)m * D + d] = (float)lp_src[(size_t)d * M + m];
+    tf32_build_b(b.data(), M, D, 32, D, img);
+    if ((rc = upload(lp_img, img))) return rc;
+  }
+  return KGB_OK;
+}
+
+bool tf32LtActive(const kgb_ctx *ctx) {
+  return ctx->prec == KGB_MIXED && ctx->allow_tf32 && ctx->use_tf32_lt && ctx->tf32_lt_img != nullptr;
+}
+bool tf32LpActive(const kgb_ctx *ctx) {
+  return ctx->prec == KGB_MIXED && ctx->allow_tf32 && ctx->use_tf32_lp && ctx->tf32_lp_img != nullptr;
+}
+
 template <typename T>
 int planTensorMoments(kgb_ctx *ctx) {
   return planTensorMomentsFrom<T>(ctx, ctx->ell_h, ctx->ellp_h, &ctx->tc_lt, &ctx->tc_lt_img, &ctx->tc_lt_exp,
@@ -842,6 +904,7 @@ int prepareT(kgb_ctx *ctx) {
     if ((rc = uploadVec<T>(ctx, ctx->ell, ctx->ell_h))) return rc;
     if ((rc = uploadVec<T>(ctx, ctx->ellp, ctx->ellp_h))) return rc;
     if ((rc = planTensorMoments<T>(ctx))) return rc;
+    if ((rc = planTf32From(ctx, ctx->ell_h, ctx->ellp_h, &ctx->tf32_lt_img, &ctx->tf32_lp_img))) return rc;
     ctx->dirty_ell = false;
     ++ctx->gen;
     ctx->adj_stale = true;
@@ -1032,7 +1095,7 @@ bool phiExpUsable(const kgb_ctx *ctx) {
   if (!ctx->allow_row_exp || !ctx->phi_exp || !ctx->tc_sc || !ctx->use_tc_sc || phiExpWidth(ctx) == 0) return false;
   const bool tensor = ctx->tc_lt && ctx->use_tc_lt;
   if (ctx->prec == KGB_FP64) return tensor && ctx->D <= ctx->tc_lt_kpad;
-  return !tensor && ltimes_tiled_applies(ctx->D, ctx->M);
+  return !tensor && !tf32LtActive(ctx) && ltimes_tiled_applies(ctx->D, ctx->M);
 }
 
 // rowexp: record psi's row exponents there (the caller zeroed it); null: psi
@@ -1054,6 +1117,7 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool
   a.rhs = as<T>(ctx->rhs);
   a.psi = as<T>(ctx->psi);
   a.sigt = as<T>(ctx->sigt);
+  a.l2hints = ctx->sweep_l2_hints ? 1 : 0;
   a.iplane = as<T>(ctx->plane[0]);
   a.jplane = as<T>(ctx->plane[1]);
   a.kplane = as<T>(ctx->plane[2]);
@@ -1234,6 +1298,13 @@ void tcRows(kgb_ctx *ctx, const T *A, T *C, int lda, int ldc, int K, int kpad, i
 int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr, int *outexp = nullptr) {
   FamScope fs(ctx, "ltimes");
   const int64_t rows = ctx->Z * ctx->G;
+  if (!outexp && tf32LtActive(ctx)) {  // mixed form: split-TF32 tensor cores
+    if (launch_tf32_ltimes(as<float>(ctx->psi), as<float>(ctx->phi), rows, ctx->D, ctx->M, ctx->tf32_lt_img, acc,
+                           ctx->err_d, ctx->nsm, ctx->stream))
+      return fail(ctx, KGB_ERR_CUDA, "split-TF32 LTimes launch failed");
+    CKN(1);
+    return KGB_OK;
+  }
   if (ctx->tc_lt && ctx->use_tc_lt) {
     // one launch per K chunk of kc directions (one chunk up to 128 FP64 / 256 FP32 directions)
     const int kc = ctx->tc_lt_kpad, S = ctx->prec == KGB_FP64 ? tcDigits<double>() : tcDigits<float>();
@@ -1277,6 +1348,13 @@ int doLPlusTimes(kgb_ctx *ctx, bool acc) {
   FamScope fs(ctx, "lplustimes");
   ctx->rhs_stale = false;
   const int64_t rows = ctx->Z * ctx->G;
+  if (tf32LpActive(ctx)) {  // mixed form: split-TF32 tensor cores
+    if (launch_tf32_lplustimes(as<float>(ctx->phi_out), as<float>(ctx->rhs), rows, ctx->D, ctx->M,
+                               ctx->tf32_lp_img, acc, ctx->err_d, ctx->nsm, ctx->stream))
+      return fail(ctx, KGB_ERR_CUDA, "split-TF32 LPlusTimes launch failed");
+    CKN(1);
+    return KGB_OK;
+  }
   if (ctx->tc_lp && ctx->use_tc_lp) {
     if (ctx->prec == KGB_FP64)
       tcRows<double>(ctx, as<double>(ctx->phi_out), as<double>(ctx->rhs), ctx->M, ctx->D, ctx->M, 32, ctx->D,
@@ -1300,7 +1378,13 @@ int doLPlusTimes(kgb_ctx *ctx, bool acc) {
 int ensureRhs(kgb_ctx *ctx) {
   if (!ctx->rhs_stale) return KGB_OK;
   int rc = prepare(ctx);
-  return rc ? rc : doLPlusTimes(ctx, false);
+  if (rc) return rc;
+  // with the SIMT kernel's arithmetic, as the fused sweep formed it
+  const bool tf32 = ctx->use_tf32_lp;
+  ctx->use_tf32_lp = false;
+  rc = doLPlusTimes(ctx, false);
+  ctx->use_tf32_lp = tf32;
+  return rc;
 }
 
 template <typename T>
@@ -1548,6 +1632,7 @@ int prepareAdjointT(kgb_ctx *ctx) {
                                      &ctx->tc_lt_exp_adj, &ctx->tc_lt_kpad_adj, &ctx->tc_lp_adj, &ctx->tc_lp_img_adj,
                                      &ctx->tc_lp_exp_adj, &ctx->tc_lp_nhalf_adj)))
     return rc;
+  if ((rc = planTf32From(ctx, ctx->ellp_h, ctx->ell_h, &ctx->tf32_lt_img_adj, &ctx->tf32_lp_img_adj))) return rc;
   ctx->adj_stale = false;
   return KGB_OK;
 }
@@ -1581,6 +1666,8 @@ struct AdjointView {
     std::swap(c->tc_lp_exp, c->tc_lp_exp_adj);
     std::swap(c->tc_lt_kpad, c->tc_lt_kpad_adj);
     std::swap(c->tc_lp_nhalf, c->tc_lp_nhalf_adj);
+    std::swap(c->tf32_lt_img, c->tf32_lt_img_adj);
+    std::swap(c->tf32_lp_img, c->tf32_lp_img_adj);
     std::swap(c->tc_sc_img, c->tc_sc_img_adj);
     std::swap(c->tc_sc_exp, c->tc_sc_exp_adj);
     c->flip ^= 1;
@@ -1859,6 +1946,7 @@ int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s, const int
   ctx->stream = keep;
   return rc;
 }
+int instance_check(kgb_ctx *ctx) { return checkDeviceError(ctx); }
 }  // namespace kgb
 
 // ===========================================================================
@@ -1936,6 +2024,17 @@ int kgb_setup(kgb_ctx *ctx, const kgb_dims *d) {
     if (d->num_zonesets[k] < 1) return fail(ctx, KGB_ERR_ARG, "zone sets must be >= 1");
   if (d->nx % d->num_zonesets[0] || d->ny % d->num_zonesets[1] || d->nz % d->num_zonesets[2])
     return fail(ctx, KGB_ERR_ARG, "zone sets must divide the zones");
+  {
+    // the SIMT moment kernels stage the whole [D][moment class] table in shared memory
+    const int M = (d->legendre_order + 1) * (d->legendre_order + 1);
+    const size_t need = (size_t)(d->precision == KGB_FP64 ? 8 : 4) * d->num_directions * moment_class(M);
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    if (optin > 0 && need > (size_t)optin)
+      return fail(ctx, KGB_ERR_ARG,
+                  "directions x moments too large: the moment tables (" + std::to_string(need) +
+                      " bytes) exceed the " + std::to_string(optin) + " bytes of shared memory of a block");
+  }
   cudaStreamSynchronize(ctx->stream);
   freeAll(ctx);
   ctx->dims = *d;
@@ -1978,7 +2077,9 @@ int kgb_setup(kgb_ctx *ctx, const kgb_dims *d) {
   ctx->plane_chunk[2] = nch * ctx->nxs * ctx->nys;
   const size_t T = ctx->tsz;
   int rc;
-  const int64_t flux = ctx->Z * ctx->G * ctx->D, mom = ctx->Z * ctx->G * ctx->M;
+  // moments are allocated for whole 128-row tiles (the split-TF32 kernels copy whole tiles); the
+  // padding is zeroed here and never read as part of a field
+  const int64_t flux = ctx->Z * ctx->G * ctx->D, mom = tf32_padded_rows(ctx->Z * ctx->G) * ctx->M;
   if ((rc = dalloc(ctx, &ctx->psi, flux * T)) || (rc = dalloc(ctx, &ctx->rhs, flux * T)) ||
       (rc = dalloc(ctx, &ctx->phi, mom * T)) || (rc = dalloc(ctx, &ctx->phi_out, mom * T)) ||
       (rc = dalloc(ctx, &ctx->sigt, ctx->Z * ctx->G * T)))
@@ -2006,6 +2107,8 @@ int kgb_setup(kgb_ctx *ctx, const kgb_dims *d) {
     ctx->nsm = nsm > 0 ? nsm : 152;
   }
   if ((rc = dalloc(ctx, (void **)&ctx->err_d, sizeof(int)))) goto oom;
+  CK(cudaMemsetAsync(ctx->phi, 0, mom * T, ctx->stream));
+  CK(cudaMemsetAsync(ctx->phi_out, 0, mom * T, ctx->stream));
   ctx->npart = 152 * 4;
   if ((rc = dmalloc(ctx, &ctx->partials, 2 * ctx->npart)) || (rc = dmalloc(ctx, &ctx->results, 16))) goto oom;
   {
@@ -2495,6 +2598,14 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->dirty_ell = true;
     return KGB_OK;
   }
+  if (!std::strcmp(key, "moments_tf32")) {
+    ctx->allow_tf32 = value != 0;
+    ctx->use_tf32_lt = ctx->use_tf32_lp = value != 0;
+    ctx->dirty_ell = true;
+    ctx->adj_stale = true;
+    ++ctx->gen;
+    return KGB_OK;
+  }
   if (!std::strcmp(key, "block_jacobi")) {
     if (value != 0 && value != 1) return fail(ctx, KGB_ERR_ARG, "block_jacobi must be 0 (sweep) or 1 (bj)");
     ctx->block_jacobi = value != 0;
@@ -2507,6 +2618,11 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
   }
   if (!std::strcmp(key, "fused_sweep")) {
     ctx->fuse_sweep = value != 0;
+    return KGB_OK;
+  }
+  if (!std::strcmp(key, "sweep_l2_hints")) {
+    ctx->sweep_l2_hints = value != 0;
+    ++ctx->gen;  // captured solves bake the sweep arguments in
     return KGB_OK;
   }
   if (!std::strcmp(key, "row_exponents")) {
@@ -2578,9 +2694,13 @@ int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_
   cudaEvent_t f0, f1;
   CK(cudaEventCreate(&f0));
   CK(cudaEventCreate(&f1));
-  auto timeIt = [&](bool lt, bool tc, float &ms) -> int {
-    bool &flag = lt ? ctx->use_tc_lt : ctx->use_tc_lp;
-    flag = tc;
+  // mode 2: split-TF32 tensor cores (mixed form), 1: exact digit products, 0: SIMT
+  auto setMode = [&](bool lt, int mode) {
+    (lt ? ctx->use_tf32_lt : ctx->use_tf32_lp) = mode == 2;
+    (lt ? ctx->use_tc_lt : ctx->use_tc_lp) = mode == 1;
+  };
+  auto timeIt = [&](bool lt, int mode, float &ms) -> int {
+    setMode(lt, mode);
     int r = lt ? doLTimes(ctx, false) : doLPlusTimes(ctx, false);  // warm-up
     if (r) return r;
     CK(cudaEventRecord(f0, ctx->stream));
@@ -2591,10 +2711,20 @@ int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_
     return r ? r : checkDeviceError(ctx);
   };
   for (int lt = 1; lt >= 0 && !rc; --lt) {
-    if (!(lt ? ctx->tc_lt : ctx->tc_lp)) continue;
-    float t_tc = 0.f, t_simt = 0.f;
-    if ((rc = timeIt(lt, true, t_tc)) || (rc = timeIt(lt, false, t_simt))) break;
-    (lt ? ctx->use_tc_lt : ctx->use_tc_lp) = t_tc <= t_simt;
+    const bool tf32 = ctx->prec == KGB_MIXED && ctx->allow_tf32 && (lt ? ctx->tf32_lt_img : ctx->tf32_lp_img);
+    const bool tc = lt ? ctx->tc_lt : ctx->tc_lp;
+    float best_t = 0.f;
+    int best_mode = -1;
+    for (int mode = 2; mode >= 0 && !rc; --mode) {
+      if ((mode == 2 && !tf32) || (mode == 1 && !tc)) continue;
+      float t = 0.f;
+      if ((rc = timeIt(lt, mode, t))) break;
+      if (best_mode < 0 || t < best_t) {
+        best_t = t;
+        best_mode = mode;
+      }
+    }
+    if (!rc && best_mode >= 0) setMode(lt, best_mode);
   }
   // scattering: tensor-core digit products for single-material zones, or SIMT
   auto timeScat = [&](bool tc, float &ms) -> int {
@@ -2631,6 +2761,9 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "moments_tensor")) *value = ctx->allow_tc ? 1 : 0;
   else if (!std::strcmp(key, "moments_tensor_ltimes")) *value = (ctx->tc_lt && ctx->use_tc_lt) ? 1 : 0;
   else if (!std::strcmp(key, "moments_tensor_lplustimes")) *value = (ctx->tc_lp && ctx->use_tc_lp) ? 1 : 0;
+  else if (!std::strcmp(key, "moments_tf32")) *value = ctx->allow_tf32 ? 1 : 0;
+  else if (!std::strcmp(key, "moments_tf32_ltimes")) *value = tf32LtActive(ctx) ? 1 : 0;
+  else if (!std::strcmp(key, "moments_tf32_lplustimes")) *value = tf32LpActive(ctx) ? 1 : 0;
   else if (!std::strcmp(key, "graph")) *value = ctx->use_graph ? 1 : 0;
   else if (!std::strcmp(key, "scattering_tensor")) *value = ctx->allow_tc_sc ? 1 : 0;
   else if (!std::strcmp(key, "scattering_tensor_active")) *value = (ctx->tc_sc && ctx->use_tc_sc) ? 1 : 0;
@@ -2638,6 +2771,7 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "block_jacobi")) *value = ctx->block_jacobi ? 1 : 0;
   else if (!std::strcmp(key, "fused_sweep")) *value = ctx->fuse_sweep ? 1 : 0;
   else if (!std::strcmp(key, "sweep_streams")) *value = ctx->sweep_streams;
+  else if (!std::strcmp(key, "sweep_l2_hints")) *value = ctx->sweep_l2_hints ? 1 : 0;
   else if (!std::strcmp(key, "fused_sweep_active")) *value = ctx->fuse_active ? 1 : 0;
   else if (!std::strcmp(key, "row_exponents")) *value = ctx->allow_row_exp ? 1 : 0;
   else if (!std::strcmp(key, "phi_row_exponents_active")) *value = phiExpUsable(ctx) ? 1 : 0;

@@ -66,6 +66,11 @@ struct SweepArgs {
   // divides Ds, or 32 when 32 divides Ds).
   int *rowexp;
   int rexp_w;
+  // 1: L2 eviction priorities -- the streamed rhs and psi evict first, the running
+  // face planes last (a face written by one tile is read by the next tile along
+  // its line one step later; the step's rhs and psi traffic would otherwise push
+  // it out of L2); 0: default caching
+  int l2hints;
 };
 
 // Largest moment count (Legendre order 4) of the fused LPlusTimes prologue.
@@ -101,6 +106,19 @@ void launch_lplustimes(const T *phi_out, T *rhs, const T *ellp_dm, int64_t rows,
 // two below 32).  Returns false, launching nothing, when the tiled kernel does
 // not apply (ltimes_tiled_applies).
 bool ltimes_tiled_applies(int D, int M);
+
+// Split-TF32 tensor-core LTimes / LPlusTimes of the mixed form (tf32_moments.cu):
+// phi (rhs) = or += L psi (L+ phi_out) over rows (zone, group) of the device
+// nesting.  phi and phi_out must be allocated for tf32_padded_rows(rows)
+// rows.  bimg: the B image built by tf32_build_b.  Nonzero return: not launched.
+bool tf32_ltimes_applies(int D, int M);
+bool tf32_lplustimes_applies(int D, int M);
+int64_t tf32_padded_rows(int64_t rows);
+void tf32_build_b(const float *b, int K, int N, int kpad, int npad, std::vector<float> &img);
+int launch_tf32_ltimes(const float *psi, float *phi, int64_t rows, int D, int M, const float *bimg, bool accumulate,
+                       int *err, int nsm, cudaStream_t s);
+int launch_tf32_lplustimes(const float *phi_out, float *rhs, int64_t rows, int D, int M, const float *bimg,
+                           bool accumulate, int *err, int nsm, cudaStream_t s);
 bool launch_ltimes_record(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M,
                           int *outexp, int rexp_w, int G, cudaStream_t s);
 
@@ -284,6 +302,10 @@ int instance_view(kgb_ctx *ctx, InstanceView *v);
 // psi_exp (LTimes): psi's row exponents as the batched sweep recorded them, or null.
 enum class InstanceOp { LTimes, Scatter, LPlusTimes };
 int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s, const int *psi_exp = nullptr);
+// Reports (KGB_ERR_TIMEOUT) and clears a bounded wait of one of the context's
+// tensor-core kernels that gave up; the caller has synchronised the streams
+// those kernels ran on.
+int instance_check(kgb_ctx *ctx);
 
 // Response, adjoint source and gradients (adjoint.cu).
 struct MixArgs {

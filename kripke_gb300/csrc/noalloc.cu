@@ -1,11 +1,10 @@
 // noalloc.cu -- a population edit that allocates nothing.
 //
-// Some callers cannot call cudaMalloc when they need the particle count:
-// an application that records its whole transport step into a CUDA graph
-// (allocation is not a capturable operation), a host framework that has
-// reserved all device memory up front for its own pool allocator (a cudaMalloc
-// would fail or fragment that pool), or a latency-bound control loop where an
-// allocation's implicit device synchronisation is not acceptable.  For them
+// Some callers cannot call cudaMalloc when they need the particle count: a
+// host framework that has reserved all device memory up front for its own pool
+// allocator (a cudaMalloc would fail or fragment that pool), or a
+// latency-bound control loop where an allocation's implicit device
+// synchronisation is not acceptable.  For them
 // kgb_population_noalloc computes the same sum as kgb_population (sum over
 // d, g, z of w(d) * psi(d,g,z) * volume(z), FP64) from device arrays the caller
 // owns, using a fixed scratch array that lives in this file's device image.
@@ -22,7 +21,9 @@
 // Host code cannot use the array's name as a device address, so the first
 // call on each device (with that device current) looks it up with
 // cudaGetSymbolAddress and caches it; that first call should come before any
-// stream capture.
+// stream capture.  The address belongs to the device's primary context: a
+// cudaDeviceReset ends that context, and the cached address with it, so a
+// process that resets a device must not call this function on it afterwards.
 #include <cstdio>
 #include <mutex>
 
@@ -91,16 +92,16 @@ extern "C" int kgb_population_noalloc(const double *psi, const double *w, const 
     setError(err, err_len, "kgb_population_noalloc: null pointer or non-positive size");
     return KGB_ERR_ARG;
   }
-  const int64_t rows = zones * (int64_t)groups;
   const int64_t limit = (int64_t)kNoallocMaxPartials * kNoallocRowsPerPartial;
-  if (rows > limit) {
-    char msg[200];
+  if (zones > limit / groups) {  // checked before the product, which could overflow
+    char msg[240];
     std::snprintf(msg, sizeof msg,
-                  "kgb_population_noalloc: zones*groups = %lld exceeds the %lld-row limit of its static scratch",
-                  (long long)rows, (long long)limit);
+                  "kgb_population_noalloc: zones*groups = %lld*%d exceeds the %lld-row limit of its static scratch",
+                  (long long)zones, (int)groups, (long long)limit);
     setError(err, err_len, msg);
     return KGB_ERR_ARG;
   }
+  const int64_t rows = zones * (int64_t)groups;
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     setError(err, err_len, "kgb_population_noalloc: no usable current device");

@@ -30,6 +30,7 @@ def single_run(kgb, b, i, niter):
     c.set_option("sweep_tile_xy", b.get_option("sweep_tile_xy"))
     c.set_option("sweep_tile_z", b.get_option("sweep_tile_z"))
     if not b.get_option("per_problem_kernels"):
+        c.set_option("moments_tf32", 0)
         c.set_option("moments_tensor", 0)
         c.set_option("scattering_tensor", 0)
     return np.array(c.solve(niter)), c.download("psi")

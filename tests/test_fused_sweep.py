@@ -4,8 +4,9 @@ With "fused_sweep" the LPlusTimes launch of every iteration
 (SteadyStateSolver.cpp:69-71) is dropped and the sweep forms each cell's rhs
 from phi_out and ell_plus with the SIMT LPlusTimes kernel's arithmetic
 (ascending moments, one FMA chain), so every iterate equals the unfused one
-bit for bit.  rhs itself is refreshed lazily, as L+ phi_out, when an entry
-point reads it.
+with the SIMT LPlusTimes bit for bit (the contexts here turn the split-TF32
+tensor-core moments off).  rhs itself is refreshed lazily, as L+ phi_out, when
+an entry point reads it.
 """
 import numpy as np
 import pytest
@@ -20,6 +21,7 @@ def pair(kgb, precision, **kw):
     for fused in (0, 1):
         c = kgb.Context()
         c.generate(precision=precision, **dict(KW, **kw))
+        c.set_option("moments_tf32", 0)
         c.set_option("fused_sweep", fused)
         out.append(c)
     return out

@@ -1,8 +1,8 @@
 """kgb_population_noalloc against kgb_population, through the C ABI.
 
 The allocation-free entry point serves callers that cannot allocate device
-memory when they need the particle count (graph-captured steps, frameworks
-that own all device memory, latency-bound loops).  It must give the same FP64
+memory when they need the particle count (frameworks that own all device
+memory through their own pool, latency-bound loops).  It must give the same FP64
 population as the context-based kgb_population, within the 1e-12 relative
 tolerance of the other FP64 parity tests, on two calls in a row (the second
 call reuses the static scratch the first one left behind).  This file sorts
