@@ -185,13 +185,16 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * (1 = LTimes and LPlusTimes on the tensor cores with exact digit products when
  * the shapes fit; 0 = SIMT kernels; default: tensor for FP64, SIMT for the
  * mixed form); "moments_tf32" (mixed form: 1 = LTimes and LPlusTimes as
- * split-TF32 tensor-core GEMMs -- hi + lo operands, three products, FP32
- * accumulation -- when moments <= 32 and there are at least 32 directions, a
- * multiple of 4 (LTimes) or of 16 up to 256 (LPlusTimes); ahead of
- * "moments_tensor"; the
- * default; 0 = off); "scattering_tensor" (1 = the single-material zones' scattering on
- * the tensor cores, exact digit products, when groups <= 64; the default in both
- * forms);
+ * split-TF32 tensor-core GEMMs -- each FP32 operand split exactly into three
+ * TF32 pieces, six products, FP32 accumulation -- when moments <= 32 and there
+ * are at least 32 directions, a multiple of 4 (LTimes) or of 16 up to 256
+ * (LPlusTimes); ahead of "moments_tensor"; the default; 0 = off);
+ * "scattering_tensor" (1 = the single-material zones' scattering on the tensor
+ * cores, exact digit products, when groups <= 64; the default in both forms);
+ * "scattering_block" (mixed form: 1 = the single-material zones' scattering by
+ * the zone-blocked FP32 kernel, bit for bit the SIMT kernel's sums, when
+ * groups <= 64 and Legendre order <= 4; ahead of "scattering_tensor"; the
+ * default; 0 = off);
  * "graph" (1 = kgb_solve replays a captured CUDA graph, the default);
  * "sweep_streams" (1 to 4: each sweep step launches its subdomains in that
  * many parts on as many streams, so one part's wave tail overlaps the others'

@@ -33,10 +33,10 @@ CUDA_INCLUDE = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "inc
 CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall", "-I" + os.path.join(ROOT, "include"),
              "-I" + HOST, "-I" + CUDA_INCLUDE]
 
-CU_SOURCES = ["kgb_api.cu", "sweep.cu", "moments.cu", "scatter.cu", "reduce.cu", "xpose.cu", "noalloc.cu", "tc_moments.cu",
+CU_SOURCES = ["kgb_context.cu", "kgb_solver.cu", "kgb_adjoint_api.cu", "kgb_options.cu", "sweep.cu", "moments.cu", "scatter.cu", "reduce.cu", "xpose.cu", "noalloc.cu", "tc_moments.cu",
               "adjoint.cu", "batch.cu", "tf32_moments.cu"]
 CPP_SOURCES = ["generate.cpp"]
-HEADERS = ["kgb_internal.h", "kgb_layout.h", "exact_round.h"]
+HEADERS = ["kgb_ctx.h", "kgb_internal.h", "kgb_layout.h", "exact_round.h"]
 
 
 def _nvcc():

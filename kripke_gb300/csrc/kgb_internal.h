@@ -66,11 +66,6 @@ struct SweepArgs {
   // divides Ds, or 32 when 32 divides Ds).
   int *rowexp;
   int rexp_w;
-  // 1: L2 eviction priorities -- the streamed rhs and psi evict first, the running
-  // face planes last (a face written by one tile is read by the next tile along
-  // its line one step later; the step's rhs and psi traffic would otherwise push
-  // it out of L2); 0: default caching
-  int l2hints;
 };
 
 // Largest moment count (Legendre order 4) of the fused LPlusTimes prologue.
@@ -137,6 +132,20 @@ void launch_scattering(const T *phi, T *phi_out, const T *sigsT, const ScatterAr
 template <typename T>
 void launch_source(T *phi_out, int64_t nmix, const int *mix_zone, const int *mix_mat, const double *mix_frac,
                    int G, int M, double strength, cudaStream_t s);
+// Zone-blocked FP32 scattering of the single-material zones (scatter.cu): zl
+// holds every material's pure zones, material m's at [off[m], off[m+1]).
+struct ScatterBlockPlan {
+  int64_t off[4];
+  int64_t nitems[3];  // work items (runs of zpc zones) per material
+  int64_t items;
+  int G, zpc;
+  const int *gp_lo, *gp_hi;
+};
+bool scatter_block_applies(int G, int L);
+size_t scatter_block_smem(int G, int L);
+void launch_scatter_block(const float *phi, float *phi_out, const float *sigsT, const int *zl, const int64_t off[4],
+                          int G, int L, const int *gp_lo, const int *gp_hi, bool accumulate, int nsm,
+                          cudaStream_t s);
 
 // Tensor-core row products C[r][n] (+)= sum_k A[r][k] B[k][n] (tc_moments.cu).
 template <typename T>

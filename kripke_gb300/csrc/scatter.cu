@@ -12,6 +12,8 @@
 // nonzero (adding an exact zero term leaves the sum unchanged).
 // sigs is stored transposed, [mat][l][g'][g], so a warp's coefficient loads
 // are contiguous.
+#include <algorithm>
+
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -96,6 +98,107 @@ __global__ void __launch_bounds__(kScatThreads) batch_scattering_kernel(const Ba
   }
 }
 
+// Zone-blocked scattering of single-material zones (mixed form; groups <= 64,
+// Legendre order <= 4).  Work items are runs of a material's zone list; a CTA
+// keeps the material's transfer matrices ([l][g'][g], from sigsT) in shared
+// memory and stages its zones' phi blocks ([g'][m] rows padded to a multiple
+// of 4 floats, so the moment loads are 16-byte vectors).  A warp covers up to
+// 32 destination groups of one zone (groups < 32: several zones, one per run of
+// G lanes): each lane keeps all (L+1)^2 moment sums of its (zone, group) and
+// walks the source groups over the warp's nonzero range; the matrix entries
+// of a warp are contiguous and the phi entries of one zone are broadcast.
+// Every lane sums the same terms in the same order as scattering_kernel (source
+// groups ascending from 0; beyond its own nonzero range the coefficients are
+// exact zeros), so the outputs are bit for bit that kernel's.  The outputs go
+// back through the staging buffer as contiguous zone blocks.
+constexpr int kBlkThreads = 256;
+
+template <int LMAX>
+__global__ void __launch_bounds__(kBlkThreads, 2)
+    scatter_block_kernel(const float *__restrict__ phi, float *__restrict__ phi_out, const float *__restrict__ sigsT,
+                         const int *__restrict__ zl, const __grid_constant__ ScatterBlockPlan pl, bool accumulate) {
+  constexpr int MM = (LMAX + 1) * (LMAX + 1);
+  constexpr int MP = (MM + 3) / 4 * 4;  // padded row of the staged blocks
+  extern __shared__ __align__(16) float blk_smem[];
+  const int G = pl.G, L1 = LMAX + 1;
+  float *sS = blk_smem;                       // [L1][G][G]: S(l)[g' -> g] at (l * G + g') * G + g
+  float *sB = blk_smem + (size_t)L1 * G * G;  // [zpc][G][MP]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int Gw = G < 32 ? G : 32, zpw = 32 / Gw, gblocks = (G + 31) / 32;
+  const int gb = warp % gblocks, zsub = lane / Gw;
+  const int zc = (warp / gblocks) * zpw + zsub;  // zone of the chunk this lane serves
+  const int g = gb * 32 + lane % Gw;
+  const bool lane_ok = zsub < zpw && g < G;
+  int lo = lane_ok ? pl.gp_lo[g] : G, hi = lane_ok ? pl.gp_hi[g] : -1;
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  int cur = -1;
+  for (int64_t it = blockIdx.x; it < pl.items; it += gridDim.x) {
+    // item -> (material, run of zones)
+    int m = 0;
+    int64_t first = it;
+    while (m < 2 && first >= pl.nitems[m]) first -= pl.nitems[m++];
+    const int64_t z0 = pl.off[m] + first * pl.zpc;
+    const int nz = (int)min((int64_t)pl.zpc, pl.off[m + 1] - z0);
+    if (m != cur) {  // this material's matrices
+      __syncthreads();
+      const float *src = sigsT + (size_t)m * L1 * G * G;
+      for (int i = threadIdx.x; i < L1 * G * G; i += kBlkThreads) sS[i] = src[i];
+      cur = m;
+    }
+    // the zones' phi blocks, contiguous [G][MM] in global memory, into padded rows
+    const int n = G * MM;
+    for (int c = 0; c < nz; ++c) {
+      const float *src = phi + (int64_t)zl[z0 + c] * n;
+      float *dst = sB + (size_t)c * G * MP;
+      for (int e = threadIdx.x; e < n; e += kBlkThreads) {
+        const int gp = e / MM;
+        dst[gp * MP + (e - gp * MM)] = src[e];
+      }
+    }
+    __syncthreads();
+    float acc[MM];
+#pragma unroll
+    for (int k = 0; k < MM; ++k) acc[k] = 0.0f;
+    if (lane_ok && zc < nz) {
+      const float *pb = sB + (size_t)zc * G * MP;
+      for (int gp = lo; gp <= hi; ++gp) {
+        float sl[LMAX + 1];
+#pragma unroll
+        for (int l = 0; l <= LMAX; ++l) sl[l] = sS[(l * G + gp) * G + g];
+        const float4 *pr = reinterpret_cast<const float4 *>(pb + gp * MP);
+#pragma unroll
+        for (int q = 0; q < MP / 4; ++q) {
+          const float4 v = pr[q];
+          const float pv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int k = 4 * q + u;
+            if (k < MM) acc[k] += sl[legendreOf(k)] * pv[u];
+          }
+        }
+      }
+    }
+    __syncthreads();  // every lane has read the staged blocks
+    if (lane_ok && zc < nz) {
+      float *ob = sB + ((size_t)zc * G + g) * MP;
+#pragma unroll
+      for (int k = 0; k < MM; ++k) ob[k] = acc[k];
+    }
+    __syncthreads();
+    for (int c = 0; c < nz; ++c) {
+      float *dst = phi_out + (int64_t)zl[z0 + c] * n;
+      const float *src = sB + (size_t)c * G * MP;
+      for (int e = threadIdx.x; e < n; e += kBlkThreads) {
+        const int gp = e / MM;
+        const float v = src[gp * MP + (e - gp * MM)];
+        dst[e] = accumulate ? dst[e] + v : v;
+      }
+    }
+    __syncthreads();  // the buffer is refilled by the next item
+  }
+}
+
 template <typename T>
 __global__ void source_kernel(T *__restrict__ phi_out, int64_t nmix, const int *__restrict__ mix_zone,
                               const int *__restrict__ mix_mat, const double *__restrict__ mix_frac, int G, int M,
@@ -132,6 +235,46 @@ void launch_scattering(const T *phi, T *phi_out, const T *sigsT, const ScatterAr
     case 5: scattering_kernel<T, 5><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
     case 6: scattering_kernel<T, 6><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
     default: scattering_kernel<T, 7><<<grid, kScatThreads, 0, s>>>(phi, phi_out, sigsT, a, accumulate); break;
+  }
+}
+
+bool scatter_block_applies(int G, int L) { return G >= 1 && G <= 64 && L <= 4; }
+
+size_t scatter_block_smem(int G, int L) {
+  const int MM = (L + 1) * (L + 1), MP = (MM + 3) / 4 * 4;
+  const int Gw = G < 32 ? G : 32, zpc = (kBlkThreads / 32) * (32 / Gw) / ((G + 31) / 32);
+  return sizeof(float) * ((size_t)(L + 1) * G * G + (size_t)zpc * G * MP);
+}
+
+void launch_scatter_block(const float *phi, float *phi_out, const float *sigsT, const int *zl, const int64_t off[4],
+                          int G, int L, const int *gp_lo, const int *gp_hi, bool accumulate, int nsm,
+                          cudaStream_t s) {
+  ScatterBlockPlan pl{};
+  pl.G = G;
+  const int Gw = G < 32 ? G : 32;
+  pl.zpc = (kBlkThreads / 32) * (32 / Gw) / ((G + 31) / 32);
+  pl.items = 0;
+  for (int m = 0; m < 3; ++m) {
+    pl.off[m] = off[m];
+    pl.nitems[m] = (off[m + 1] - off[m] + pl.zpc - 1) / pl.zpc;
+    pl.items += pl.nitems[m];
+  }
+  pl.off[3] = off[3];
+  pl.gp_lo = gp_lo;
+  pl.gp_hi = gp_hi;
+  if (pl.items == 0) return;
+  const size_t smem = scatter_block_smem(G, L);
+  const int grid = (int)std::min<int64_t>(pl.items, (int64_t)2 * nsm);
+  auto go = [&](auto kernel) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kernel<<<grid, kBlkThreads, smem, s>>>(phi, phi_out, sigsT, zl, pl, accumulate);
+  };
+  switch (L) {
+    case 0: go(scatter_block_kernel<0>); break;
+    case 1: go(scatter_block_kernel<1>); break;
+    case 2: go(scatter_block_kernel<2>); break;
+    case 3: go(scatter_block_kernel<3>); break;
+    default: go(scatter_block_kernel<4>); break;
   }
 }
 

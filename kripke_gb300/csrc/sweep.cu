@@ -97,40 +97,6 @@ __device__ __forceinline__ T ldFace(const T *p) {
   else return *p;
 }
 
-// Loads and stores with an L2 eviction policy (createpolicy), or plain ones (pol == 0).
-__device__ __forceinline__ uint64_t l2Policy(bool first) {
-  uint64_t p;
-  if (first) asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  else asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ float ldHint(const float *p, uint64_t pol) {
-  if (!pol) return *p;
-  float v;
-  asm volatile("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ double ldHint(const double *p, uint64_t pol) {
-  if (!pol) return *p;
-  double v;
-  asm volatile("ld.global.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ void stHint(float *p, float v, uint64_t pol) {
-  if (!pol) {
-    *p = v;
-    return;
-  }
-  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol) : "memory");
-}
-__device__ __forceinline__ void stHint(double *p, double v, uint64_t pol) {
-  if (!pol) {
-    *p = v;
-    return;
-  }
-  asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(pol) : "memory");
-}
-
 // Asynchronous copy of one element into this thread's own shared-memory slot.
 template <typename T>
 __device__ __forceinline__ void cpAsync(T *dst, const T *src) {
@@ -212,9 +178,6 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
       cyr[jj] = jv[jj] ? a.cy[(int64_t)d * a.ny + sd.jo + jloc[jj]] : T(0);
     }
 
-    // L2 policies: streamed operands evict first, running faces last (per-step launches)
-    const bool hints = !COH && a.l2hints != 0;
-    const uint64_t pstream = hints ? l2Policy(true) : 0, pface = hints ? l2Policy(false) : 0;
     T *const ipl = a.iplane + sd.ip;  // [nzs][nys][nchain]
     T *const jpl = a.jplane + sd.jp;  // [nzs][nxs][nchain]
     T *const kpl = a.kplane + sd.kp;  // [nys][nxs][nchain]
@@ -224,10 +187,7 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
     for (int ii = 0; ii < TX; ++ii)
 #pragma unroll
       for (int jj = 0; jj < TY; ++jj)
-        bo[ii][jj] = (iv[ii] && jv[jj])
-                         ? (COH ? ldFace<COH>(kpl + ((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c)
-                                : ldHint(kpl + ((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c, pface))
-                         : T(0);
+        bo[ii][jj] = (iv[ii] && jv[jj]) ? ldFace<COH>(kpl + ((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c) : T(0);
 
     T ep[FUSE ? kFuseMaxM : 1];
     if constexpr (FUSE) {
@@ -324,7 +284,7 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
             } else if constexpr (PF) {
               rv[jj][ii] = slot(kk & 1, jj * TX + ii);
             } else {
-              rv[jj][ii] = ldHint(rhs + (z * a.G + g) * a.D + d, pstream);
+              rv[jj][ii] = rhs[(z * a.G + g) * a.D + d];
             }
             if constexpr (PF) {
               if constexpr (RECIP) sv[jj][ii] = a.inv[(int64_t)cc[jj][ii] * a.D + d];
@@ -345,8 +305,7 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
 #pragma unroll
       for (int ii = 0; ii < TX; ++ii) {
         if constexpr (kFaces > 0) fr[ii] = iv[ii] ? slot(kk & 1, TX * TY + ii) : T(0);
-        else if constexpr (COH) fr[ii] = iv[ii] ? ldFace<COH>(jpl + ((int64_t)k * a.nxs + iloc[ii]) * nchain + c) : T(0);
-        else fr[ii] = iv[ii] ? ldHint(jpl + ((int64_t)k * a.nxs + iloc[ii]) * nchain + c, pface) : T(0);
+        else fr[ii] = iv[ii] ? ldFace<COH>(jpl + ((int64_t)k * a.nxs + iloc[ii]) * nchain + c) : T(0);
       }
 #pragma unroll
       for (int jj = 0; jj < TY; ++jj) {
@@ -355,8 +314,7 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
         T *const lfp = ipl + ((int64_t)k * a.nys + j) * nchain + c;
         T lf;
         if constexpr (kFaces > 0) lf = slot(kk & 1, TX * TY + TX + jj);
-        else if constexpr (COH) lf = ldFace<COH>(lfp);
-        else lf = ldHint(lfp, pface);
+        else lf = ldFace<COH>(lfp);
         const int64_t zrow = (zslice + (sd.jo + j)) * a.nx + sd.io;
 #pragma unroll
         for (int ii = 0; ii < TX; ++ii) {
@@ -371,7 +329,7 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
             const T den = cxr[ii] + cyr[jj] + czk + sv[jj][ii];
             ps = num / den;
           }
-          stHint(psi + e, ps, pstream);
+          psi[e] = ps;
           if constexpr (sizeof(T) == 8) {
             if (a.rowexp) rowExpMax(a.rowexp, a.rexp_w, rmask, ps, z * a.G + g);
           }
@@ -383,17 +341,17 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
             else pop.add((T)a.vol[z] * ps);
           }
         }
-        stHint(lfp, lf, pface);
+        *lfp = lf;
       }
 #pragma unroll
       for (int ii = 0; ii < TX; ++ii)
-        if (iv[ii]) stHint(jpl + ((int64_t)k * a.nxs + iloc[ii]) * nchain + c, fr[ii], pface);
+        if (iv[ii]) jpl[((int64_t)k * a.nxs + iloc[ii]) * nchain + c] = fr[ii];
     }
 #pragma unroll
     for (int ii = 0; ii < TX; ++ii)
 #pragma unroll
       for (int jj = 0; jj < TY; ++jj)
-        if (iv[ii] && jv[jj]) stHint(kpl + ((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c, bo[ii][jj], pface);
+        if (iv[ii] && jv[jj]) kpl[((int64_t)jloc[jj] * a.nxs + iloc[ii]) * nchain + c] = bo[ii][jj];
   }
   if (POP) {
     double v = pop.value() * wd;

@@ -20,9 +20,11 @@
 // (six kind::tf32 MMAs per K step; TF32 x TF32 products are exact, the sums
 // accumulate in FP32 in tensor memory); the dropped mid lo + lo mid + lo lo are
 // below 2^-32 |a b|, so what remains is the FP32 accumulation.  The tensor
-// core's accumulation is not rounded to nearest at every step, so LTimes
-// accumulates each 32-direction chunk (24 MMAs) separately and the epilogue
-// adds the chunks in FP32, rounded to nearest, in K order.  (Two pieces, hi + lo with
+// core's accumulation is not rounded to nearest at every step, so a chunk's
+// MMAs add the small terms of all its K steps first and the four leading
+// hi x hi products last, and LTimes accumulates each 32-direction chunk
+// separately, the epilogue adding the chunks in FP32, rounded to nearest, in
+// K order.  (Two pieces, hi + lo with
 // lo rounded to TF32, leave 2^-22 |a b| per product: measured four times the
 // SIMT kernel's error on 192-direction rows with cancellation.)  B is split on
 // the host once.
@@ -458,18 +460,24 @@ __global__ void __launch_bounds__(kThreads, 1) tf32x3_kernel(const __grid_consta
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t ahi = tmem + aBase + (uint32_t)u * kSlotCols, amid = ahi + 32, alo = ahi + 64;
+        // the five small terms of every K step first (their sum stays near 2^-10 of the
+        // result, so the accumulator's roundings there are small), then the leading
+        // hi x hi products: four large-magnitude accumulations per chunk instead of 24
 #pragma unroll
         for (int ks = 0; ks < kChunk / 8; ++ks) {
           const uint32_t boff = (uint32_t)((c * kChunk + ks * 8) / 4) * lbo;
           const uint64_t dh = matDesc(bHi + boff, lbo, 128), dm = matDesc(bMid + boff, lbo, 128),
                          dl = matDesc(bLo + boff, lbo, 128);
-          // the small terms first, the leading product last
           mmaTf32(dcol, alo + ks * 8, dh, idesc, (!fresh || ks > 0) ? 1u : 0u);
           mmaTf32(dcol, ahi + ks * 8, dl, idesc, 1u);
           mmaTf32(dcol, amid + ks * 8, dm, idesc, 1u);
           mmaTf32(dcol, amid + ks * 8, dh, idesc, 1u);
           mmaTf32(dcol, ahi + ks * 8, dm, idesc, 1u);
-          mmaTf32(dcol, ahi + ks * 8, dh, idesc, 1u);
+        }
+#pragma unroll
+        for (int ks = 0; ks < kChunk / 8; ++ks) {
+          const uint32_t boff = (uint32_t)((c * kChunk + ks * 8) / 4) * lbo;
+          mmaTf32(dcol, ahi + ks * 8, matDesc(bHi + boff, lbo, 128), idesc, 1u);
         }
         commit(&tfree[u]);  // slot u's last reader
       }

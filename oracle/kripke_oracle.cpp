@@ -824,8 +824,23 @@ double kPopulation(orc_problem &p) {
   return part;
 }
 
+// Compensated sum (Neumaier): the balance adds up to 10^8 positive terms, where
+// one running double would carry an error of order sqrt(n) ulps of the total.
+struct CSum {
+  double s = 0.0, c = 0.0;
+  CSum &operator+=(double x) {
+    const double t = s + x;
+    c += std::fabs(s) >= std::fabs(x) ? (s - t) + x : (x - t) + s;
+    s = t;
+    return *this;
+  }
+  double value() const { return s + c; }
+};
+
+// Particle balance after a sweep (an extension of Kernel::population,
+// Kernel/Population.cpp:51-63, to the emission, collision and leakage terms).
 void kBalance(orc_problem &p, double out[5]) {
-  double emis = 0.0, coll = 0.0, leak = 0.0;
+  CSum emis, coll, leak;
   const int64_t Zs = (int64_t)p.nxs * p.nys * p.nzs;
   for (int sdom = 0; sdom < p.dc.num(); ++sdom) {
     const double *psi = p.dptr("psi", sdom), *rhs = p.dptr("rhs", sdom), *w = p.dptr("quadrature/w", sdom);
@@ -854,11 +869,11 @@ void kBalance(orc_problem &p, double out[5]) {
             }
     }
   }
-  out[0] = emis;
-  out[1] = coll;
-  out[2] = leak;
+  out[0] = emis.value();
+  out[1] = coll.value();
+  out[2] = leak.value();
   out[3] = kPopulation(p);
-  out[4] = emis - coll - leak;
+  out[4] = out[0] - out[1] - out[2];
 }
 
 }  // namespace
