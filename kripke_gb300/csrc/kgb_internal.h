@@ -286,7 +286,7 @@ cudaError_t launch_batch_sweep(const SweepArgs<T> *inst, const BatchSweepPlan &p
 // per-problem fixed-order sums of the fused population partials: out[i] = sum of slots[i][0 .. n[i])
 void launch_batch_pop_finish(const double *const *slots, const int64_t *n, int ninst, double *out, cudaStream_t s);
 
-// Device view of one prepared context (kgb_api.cu), for the batched driver.
+// Device view of one prepared context (kgb_solver.cu), for the batched driver.
 struct InstanceView {
   int prec;
   int64_t Z;
