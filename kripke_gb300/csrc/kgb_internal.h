@@ -141,10 +141,20 @@ struct ScatterBlockPlan {
   int G, zpc;
   const int *gp_lo, *gp_hi;
 };
+// Groups a multiple of 4 take the staged form (scatter_zone_kernel): zone blocks
+// arrive by bulk copies, each thread keeps a 4-group x (L+1)^2 register tile.
+struct ScatterZonePlan {
+  int64_t off[4];
+  int G, zpi;            // groups; zones per item of one 128-thread group
+  uint32_t slot;         // floats between staged zone blocks
+  const int *gp_lo, *gp_hi;
+  int *err;              // raised when a copy's bounded wait gives up
+};
 bool scatter_block_applies(int G, int L);
 size_t scatter_block_smem(int G, int L);
+// err: the context's device error word (the staged form's bounded waits)
 void launch_scatter_block(const float *phi, float *phi_out, const float *sigsT, const int *zl, const int64_t off[4],
-                          int G, int L, const int *gp_lo, const int *gp_hi, bool accumulate, int nsm,
+                          int G, int L, const int *gp_lo, const int *gp_hi, bool accumulate, int *err, int nsm,
                           cudaStream_t s);
 
 // Tensor-core row products C[r][n] (+)= sum_k A[r][k] B[k][n] (tc_moments.cu).

@@ -404,7 +404,7 @@ int doScattering(kgb_ctx *ctx, bool acc, const int *rowexp) {
   FamScope fs(ctx, "scattering");
   if (blockScatterActive(ctx)) {  // mixed form: zone-blocked kernel, mixed zones SIMT
     launch_scatter_block(as<float>(ctx->phi), as<float>(ctx->phi_out), as<float>(ctx->sigsT), ctx->pure_z,
-                         ctx->pure_off, ctx->G, ctx->L, ctx->gp_lo, ctx->gp_hi, acc, ctx->nsm, ctx->stream);
+                         ctx->pure_off, ctx->G, ctx->L, ctx->gp_lo, ctx->gp_hi, acc, ctx->err_d, ctx->nsm, ctx->stream);
     CKN(1);
     if (ctx->nmixed_z > 0) {
       ScatterArgsBase a = scatterArgs(ctx);
@@ -456,7 +456,7 @@ int checkDeviceError(kgb_ctx *ctx) {
   CK(cudaStreamSynchronize(ctx->stream));
   if (h) {
     CK(cudaMemsetAsync(ctx->err_d, 0, sizeof(int), ctx->stream));
-    return fail(ctx, KGB_ERR_TIMEOUT, "a tensor-core kernel's bounded wait gave up");
+    return fail(ctx, KGB_ERR_TIMEOUT, "a device kernel's bounded wait gave up");
   }
   return KGB_OK;
 }

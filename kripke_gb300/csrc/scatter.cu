@@ -121,8 +121,9 @@ __global__ void __launch_bounds__(kBlkThreads, 2)
   constexpr int MP = (MM + 3) / 4 * 4;  // padded row of the staged blocks
   extern __shared__ __align__(16) float blk_smem[];
   const int G = pl.G, L1 = LMAX + 1;
-  float *sS = blk_smem;                       // [L1][G][G]: S(l)[g' -> g] at (l * G + g') * G + g
-  float *sB = blk_smem + (size_t)L1 * G * G;  // [zpc][G][MP]
+  float *sS = blk_smem;  // [L1][G][G]: S(l)[g' -> g] at (l * G + g') * G + g
+  // [zpc][G][MP], after the matrices rounded up to whole float4s (the rows are read as float4)
+  float *sB = blk_smem + ((size_t)L1 * G * G + 3) / 4 * 4;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Gw = G < 32 ? G : 32, zpw = 32 / Gw, gblocks = (G + 31) / 32;
   const int gb = warp % gblocks, zsub = lane / Gw;
@@ -199,6 +200,205 @@ __global__ void __launch_bounds__(kBlkThreads, 2)
   }
 }
 
+// Staged zone-blocked scattering (groups a multiple of 4, at most 64; Legendre
+// order <= 4).  A CTA holds one material's transfer matrices ([l][g'][g]) and
+// runs two independent 128-thread groups.  A group's item is a run of zpi zones
+// of that material: one elected thread brings each zone's contiguous [G][MM]
+// phi block into the group's buffer with one bulk copy (an mbarrier counts the
+// bytes); a thread then owns 4 destination groups x MM moments of one zone in
+// registers and walks the source groups g' over its warp's nonzero range, in
+// steps of 4 so that the offset of row g' within its 16-byte word is a
+// compile-time constant (rows are MM floats; (MM g') mod 4 depends on g' mod 4
+// only): a row is read as 16-byte broadcasts, a matrix row as one 16-byte load
+// per Legendre order.  Each output keeps scattering_kernel's sum -- source
+// groups ascending from 0, exact zeros outside a row's nonzero range -- so the
+// results are bit for bit that kernel's.  The group's 4 x MM outputs of a
+// thread are contiguous in phi_out and 16-byte aligned, stored (or added to,
+// one FP32 add per element) as 16-byte words, while the next item's copies are
+// in flight.
+constexpr int kZoneThreads = 256;  // two groups
+constexpr int kZoneGroup = 128;
+constexpr uint64_t kZoneWaitNs = 200000000ull;  // 0.2 s
+
+__device__ __forceinline__ uint64_t zoneNowNs() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool zoneTestWait(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// bounded wait for the phase with the given parity (false: gave up after kZoneWaitNs)
+__device__ __forceinline__ bool zoneWait(uint32_t bar, uint32_t parity) {
+  uint64_t t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 15u) == 15u) {
+      const uint64_t t = zoneNowNs();
+      if (t0 == 0) t0 = t;
+      else if (t - t0 > kZoneWaitNs) return false;
+    }
+  }
+}
+
+template <int LMAX>
+__global__ void __launch_bounds__(kZoneThreads, 1)
+    scatter_zone_kernel(const float *__restrict__ phi, float *__restrict__ phi_out, const float *__restrict__ sigsT,
+                        const int *__restrict__ zl, const __grid_constant__ ScatterZonePlan pl, bool accumulate) {
+  constexpr int MM = (LMAX + 1) * (LMAX + 1), L1 = LMAX + 1;
+  extern __shared__ __align__(16) float zone_smem[];
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ int bad[2];
+  const int G = pl.G, GQ = G / 4, zpi = pl.zpi;
+  float *sS = zone_smem;  // [L1][G][G]
+  const int tid = threadIdx.x, gi = tid / kZoneGroup, gt = tid % kZoneGroup;
+  float *buf = zone_smem + (size_t)L1 * G * G + (size_t)gi * zpi * pl.slot;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&full[gi]);
+  const int c = gt / GQ, q = gt - (gt / GQ) * GQ;  // zone slot, group quad
+  const bool lane_ok = c < zpi;
+  const int cr = lane_ok ? c : zpi - 1;  // slot read by idle lanes (results unused)
+  // this warp's source-group range, rounded out to whole steps of 4
+  int lo = G, hi = -1;
+  if (lane_ok)
+    for (int i = 0; i < 4; ++i) {
+      lo = min(lo, pl.gp_lo[4 * q + i]);
+      hi = max(hi, pl.gp_hi[4 * q + i]);
+    }
+  lo = __reduce_min_sync(0xffffffffu, lo) & ~3;
+  hi = (__reduce_max_sync(0xffffffffu, hi) + 4) & ~3;
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&full[i])));
+      bad[i] = 0;
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int stride = 2 * gridDim.x, first = 2 * blockIdx.x + gi;
+  const uint32_t zbytes = (uint32_t)G * MM * 4;
+  uint32_t ph = 0;
+  bool pending = false;  // a copy issued by this group and not yet waited for (elected thread)
+  for (int m = 0; m < 3; ++m) {
+    const int64_t n = pl.off[m + 1] - pl.off[m];
+    if (n == 0) continue;
+    __syncthreads();  // both groups are done with the previous material's matrices
+    {
+      const float4 *src = reinterpret_cast<const float4 *>(sigsT + (size_t)m * L1 * G * G);
+      float4 *dst = reinterpret_cast<float4 *>(sS);
+      for (int i = tid; i < L1 * G * G / 4; i += kZoneThreads) dst[i] = src[i];
+    }
+    __syncthreads();
+    const int64_t nitems = (n + zpi - 1) / zpi;
+    auto issue = [&](int64_t it) {
+      const int64_t z0 = pl.off[m] + it * zpi;
+      const int nz = (int)min((int64_t)zpi, pl.off[m + 1] - z0);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the buffer's last generic reads
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"((uint32_t)nz * zbytes)
+                   : "memory");
+      for (int k = 0; k < nz; ++k)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(buf + (size_t)k * pl.slot)),
+                     "l"(phi + (int64_t)zl[z0 + k] * G * MM), "r"(zbytes), "r"(bar)
+                     : "memory");
+      pending = true;
+    };
+    int64_t it = first;
+    if (it < nitems && gt == 0 && !bad[gi]) issue(it);
+    while (it < nitems) {
+      // one elected thread waits (bounded), the group learns the outcome at its barrier
+      if (gt == 0) {
+        if (!bad[gi] && !zoneWait(bar, ph)) {
+          bad[gi] = 1;
+          atomicExch(pl.err, 1);
+        } else if (!bad[gi]) {
+          pending = false;
+        }
+      }
+      asm volatile("bar.sync %0, %1;" ::"r"(1 + gi), "r"(kZoneGroup) : "memory");
+      if (bad[gi]) break;
+      zoneTestWait(bar, ph);  // completed phase: this thread's own acquire of the copied bytes
+      ph ^= 1u;
+      const int64_t z0 = pl.off[m] + it * zpi;
+      const int nz = (int)min((int64_t)zpi, pl.off[m + 1] - z0);
+      float acc[4][MM];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < MM; ++k) acc[i][k] = 0.0f;
+      const float *zb = buf + (size_t)cr * pl.slot;
+      for (int gb = lo; gb < hi; gb += 4) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const int gp = gb + r;
+          constexpr int kAlignMul = MM & 3;  // (MM gp) mod 4 = (MM mod 4)(gp mod 4) mod 4
+          const int R = (kAlignMul * r) & 3;
+          const float4 *pr = reinterpret_cast<const float4 *>(zb + MM * gp - R);
+          float v[MM + 3 + 4];
+#pragma unroll
+          for (int j = 0; j < (MM + 3 + 3) / 4; ++j) {
+            if (4 * j < R + MM) {
+              const float4 w = pr[j];
+              v[4 * j] = w.x;
+              v[4 * j + 1] = w.y;
+              v[4 * j + 2] = w.z;
+              v[4 * j + 3] = w.w;
+            }
+          }
+          float4 sl[L1];
+#pragma unroll
+          for (int l = 0; l < L1; ++l) sl[l] = *reinterpret_cast<const float4 *>(sS + ((size_t)l * G + gp) * G + 4 * q);
+#pragma unroll
+          for (int k = 0; k < MM; ++k) {
+            const float p = v[R + k];
+            const float4 s4 = sl[legendreOf(k)];
+            acc[0][k] += s4.x * p;
+            acc[1][k] += s4.y * p;
+            acc[2][k] += s4.z * p;
+            acc[3][k] += s4.w * p;
+          }
+        }
+      }
+      asm volatile("bar.sync %0, %1;" ::"r"(1 + gi), "r"(kZoneGroup) : "memory");  // the buffer is read
+      const int64_t next = it + stride;
+      if (next < nitems && gt == 0) issue(next);
+      if (lane_ok && c < nz) {
+        float4 *o = reinterpret_cast<float4 *>(phi_out + ((int64_t)zl[z0 + c] * G + 4 * q) * MM);
+#pragma unroll
+        for (int j = 0; j < MM; ++j) {  // the thread's 4 x MM outputs, row-major, as MM 16-byte words
+          float4 w = make_float4(acc[(4 * j) / MM][(4 * j) % MM], acc[(4 * j + 1) / MM][(4 * j + 1) % MM],
+                                 acc[(4 * j + 2) / MM][(4 * j + 2) % MM], acc[(4 * j + 3) / MM][(4 * j + 3) % MM]);
+          if (accumulate) {
+            const float4 old = o[j];
+            w.x = old.x + w.x;
+            w.y = old.y + w.y;
+            w.z = old.z + w.z;
+            w.w = old.w + w.w;
+          }
+          o[j] = w;
+        }
+      }
+      it = next;
+    }
+  }
+  // a copy still in flight (only after a wait that gave up) must land before the CTA's memory goes away
+  if (gt == 0 && pending) zoneWait(bar, ph);
+  __syncthreads();
+}
+
 template <typename T>
 __global__ void source_kernel(T *__restrict__ phi_out, int64_t nmix, const int *__restrict__ mix_zone,
                               const int *__restrict__ mix_mat, const double *__restrict__ mix_frac, int G, int M,
@@ -240,15 +440,57 @@ void launch_scattering(const T *phi, T *phi_out, const T *sigsT, const ScatterAr
 
 bool scatter_block_applies(int G, int L) { return G >= 1 && G <= 64 && L <= 4; }
 
+namespace {
+// staged form: floats between zone blocks (16-byte multiple; an odd number of
+// 16-byte words, so the zones that share a warp read distinct banks)
+uint32_t zoneSlot(int G, int L) {
+  const uint32_t mm = (uint32_t)(L + 1) * (L + 1);
+  uint32_t slot = ((uint32_t)G * mm + 3u) & ~3u;
+  if ((slot / 4) % 2 == 0) slot += 4;
+  return slot;
+}
+int zoneItemZones(int G) { return std::max(1, kZoneGroup / (G / 4)); }
+}  // namespace
+
 size_t scatter_block_smem(int G, int L) {
   const int MM = (L + 1) * (L + 1), MP = (MM + 3) / 4 * 4;
+  if (G % 4 == 0)  // staged form: the matrices and two groups' zone buffers
+    return sizeof(float) * ((size_t)(L + 1) * G * G + (size_t)2 * zoneItemZones(G) * zoneSlot(G, L));
   const int Gw = G < 32 ? G : 32, zpc = (kBlkThreads / 32) * (32 / Gw) / ((G + 31) / 32);
-  return sizeof(float) * ((size_t)(L + 1) * G * G + (size_t)zpc * G * MP);
+  return sizeof(float) * (((size_t)(L + 1) * G * G + 3) / 4 * 4 + (size_t)zpc * G * MP);
 }
 
+
 void launch_scatter_block(const float *phi, float *phi_out, const float *sigsT, const int *zl, const int64_t off[4],
-                          int G, int L, const int *gp_lo, const int *gp_hi, bool accumulate, int nsm,
+                          int G, int L, const int *gp_lo, const int *gp_hi, bool accumulate, int *err, int nsm,
                           cudaStream_t s) {
+  if (G % 4 == 0) {
+    ScatterZonePlan pl{};
+    pl.G = G;
+    pl.zpi = zoneItemZones(G);
+    pl.slot = zoneSlot(G, L);
+    pl.gp_lo = gp_lo;
+    pl.gp_hi = gp_hi;
+    pl.err = err;
+    int64_t most = 0;
+    for (int m = 0; m < 4; ++m) pl.off[m] = off[m];
+    for (int m = 0; m < 3; ++m) most = std::max(most, (off[m + 1] - off[m] + pl.zpi - 1) / pl.zpi);
+    if (most == 0) return;
+    const size_t smem = scatter_block_smem(G, L);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((most + 1) / 2, nsm));
+    auto go = [&](auto kernel) {
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kernel<<<grid, kZoneThreads, smem, s>>>(phi, phi_out, sigsT, zl, pl, accumulate);
+    };
+    switch (L) {
+      case 0: go(scatter_zone_kernel<0>); break;
+      case 1: go(scatter_zone_kernel<1>); break;
+      case 2: go(scatter_zone_kernel<2>); break;
+      case 3: go(scatter_zone_kernel<3>); break;
+      default: go(scatter_zone_kernel<4>); break;
+    }
+    return;
+  }
   ScatterBlockPlan pl{};
   pl.G = G;
   const int Gw = G < 32 ? G : 32;

@@ -152,6 +152,7 @@ def test_scattering_tensor_wide_range(oracle, kgb, precision, groups, legendre):
     p, ctx = pair(oracle, kgb, precision=precision, scatter=1, groups=groups, legendre=legendre, geometry=1,
                   zones=(9, 7, 5), quad=16)
     ctx.set_option("scattering_tensor", 1)
+    ctx.set_option("scattering_block", 0)  # the mixed form's zone-blocked kernel is tested on its own
     rng = np.random.default_rng(5)
     n = ctx.field_bytes("phi") // 8
     phi = rng.standard_normal(n) * 10.0 ** rng.uniform(-20 if precision == 0 else -6, 2, n)

@@ -147,10 +147,12 @@ def test_zero_fill_records_zero_exponents(kgb):
                                 dict(groups=12)])
 def test_mixed_form_phi_record_bitwise(kgb, kw):
     # the mixed form's register-tiled SIMT LTimes records phi's exponents for the tensor-core
-    # scattering (the split-TF32 LTimes does not: it is turned off here)
+    # scattering (the split-TF32 LTimes does not, and the zone-blocked FP32 scattering needs none:
+    # both are turned off here)
     a, b = pair(kgb, precision=kgb.MIXED, **kw)
     for c in (a, b):
         c.set_option("moments_tf32", 0)
+        c.set_option("scattering_block", 0)
     pa = [a.iterate() for _ in range(4)]
     pb = [b.iterate() for _ in range(4)]
     assert b.get_option("phi_row_exponents_active") == int(kw.get("groups", 8) != 12)

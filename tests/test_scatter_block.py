@@ -5,7 +5,8 @@ memory and sums, for every (zone, destination group), the same terms in the same
 scattering kernel (source groups ascending; exact zeros outside a row's nonzero range), so its
 outputs must equal that kernel's bit for bit: single calls (accumulating onto phi_out, as
 Kernel::scattering does, Kernel/Scattering.cpp:79-98), whole solves and adjoint gradients, over
-group counts that fill a warp, pack several zones into one, or leave lanes idle.  Against the FP64
+group counts that fill a warp, pack several zones into one, or leave lanes idle, and odd group
+counts whose matrices end off a 16-byte boundary of shared memory.  Against the FP64
 oracle the outputs stay within FP32 rounding.
 """
 import numpy as np
@@ -28,7 +29,7 @@ def scatter_both(ctx, phi, out0):
     return res
 
 
-@pytest.mark.parametrize("groups,legendre", [(64, 4), (32, 2), (16, 3), (8, 4), (12, 1), (48, 0), (64, 1)])
+@pytest.mark.parametrize("groups,legendre", [(64, 4), (32, 2), (16, 3), (8, 4), (12, 1), (48, 0), (64, 1), (37, 2), (5, 3), (63, 4), (1, 1)])
 def test_block_scattering_bitwise(oracle, kgb, groups, legendre):
     p, ctx = pair(oracle, kgb, precision=kgb.MIXED, groups=groups, legendre=legendre, zones=(10, 9, 8), quad=(4, 8),
                   scatter=1, geometry=1)
@@ -72,6 +73,25 @@ def test_block_scattering_solve_and_adjoint_bitwise(kgb, kw):
     np.testing.assert_array_equal(sa, sb)
     for x, y in zip(ga, gb):
         np.testing.assert_array_equal(np.asarray(x), np.asarray(y))
+
+
+@pytest.mark.parametrize("groups,legendre,zones", [(64, 4, (32, 32, 16)), (16, 2, (24, 20, 16)), (4, 1, (40, 16, 12)),
+                                                    (48, 3, (16, 16, 20))])
+def test_staged_block_scattering_many_items(kgb, groups, legendre, zones):
+    """Enough zones that each 128-thread group of the staged kernel (groups a multiple of 4) runs
+    many items of every material, the next item's copies in flight while the last one is stored."""
+    ctx = kgb.Context(0)
+    ctx.generate(precision=kgb.MIXED, groups=groups, legendre=legendre, zones=zones, quad=(4, 8), scatter=1,
+                 geometry=1)
+    ctx.set_option("scattering_tensor", 0)
+    rng = np.random.default_rng(groups + 100 * legendre)
+    n = ctx.field_bytes("phi") // 8
+    phi = rng.uniform(-1.0, 1.0, n).astype(np.float32).astype(np.float64)
+    out0 = rng.uniform(0.0, 1.0, n).astype(np.float32).astype(np.float64)
+    (on, blk), (off, simt) = scatter_both(ctx, phi, out0)
+    assert on == 1 and off == 0
+    np.testing.assert_array_equal(blk, simt)
+    ctx.close()
 
 
 def test_block_scattering_not_in_fp64(oracle, kgb):
