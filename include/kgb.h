@@ -206,6 +206,14 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * running LPlusTimes, with the SIMT kernel's arithmetic, so psi is unchanged;
  * rhs is then refreshed, as L+ phi_out, only when an entry point reads it --
  * download, kgb_lplustimes, the sweep entry points, kgb_balance, autotune);
+ * "fused_ltimes" (mixed form, forward solves, (directions per set) x (groups
+ * per set) a multiple of 128, without "fused_sweep": 1 = inside kgb_solve the
+ * sweep of every iteration but the last also adds the next iteration's moments
+ * phi = L psi -- per k-slice of a tile, each (zone, group, moment) takes the
+ * sum over the subdomain's directions, added with FP32 reductions whose order
+ * between subdomains is not fixed -- and the next iteration skips LTimes; phi
+ * after the solve is still L of the psi the last iteration started from;
+ * default 0);
  * "row_exponents" (1 = in FP64 with the tensor-core LTimes the solver loop's
  * sweep records the largest exponent of every (zone, group) row of psi, and
  * the next iteration's LTimes scales its digit split by it instead of reading
@@ -222,7 +230,9 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
  * kernel runs on the tensor cores), "sweep_reciprocals_active" (1 when the
  * sweep uses tabulated reciprocals), "graph_active" (1 when the last
  * kgb_solve replayed a graph), "fused_sweep_active" (1 when the last
- * iteration formed rhs inside the sweep), "psi_row_exponents_active" and
+ * iteration formed rhs inside the sweep), "fused_ltimes_active" (1 when
+ * kgb_solve fuses the LTimes epilogue on this problem),
+ * "psi_row_exponents_active" and
  * "phi_row_exponents_active" (1 when the solver loop records them on this
  * problem) and "psi_row_exponents_valid" (1 when psi's record matches the
  * current psi). */

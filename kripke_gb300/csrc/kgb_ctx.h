@@ -249,6 +249,9 @@ struct kgb_ctx {
   // mixed form: the solver loop forms rhs inside the sweep (no LPlusTimes launch);
   // rhs then holds an older value until an entry point that reads it refreshes it
   bool fuse_sweep = false, fuse_active = false, rhs_stale = false;
+  // fused LTimes epilogue (option fused_ltimes): inside one solve, the sweep of every
+  // iteration but the last adds L psi into phi, and the next iteration skips LTimes
+  bool fuse_lt = false, phi_fused = false;
 };
 
 namespace kgb {
@@ -361,9 +364,11 @@ bool psiExpUsable(const kgb_ctx *ctx);
 int phiExpWidth(const kgb_ctx *ctx);
 bool phiExpUsable(const kgb_ctx *ctx);
 int sweepWaveAny(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop = false, bool fused_rhs = false,
-                 int *rowexp = nullptr);
+                 int *rowexp = nullptr, bool fused_lt = false);
 int fillField(kgb_ctx *ctx, const FieldInfo *f, double v);
-int sweepSolver(kgb_ctx *ctx, bool fused_pop = false, bool fused_rhs = false, int *rowexp = nullptr);
+int sweepSolver(kgb_ctx *ctx, bool fused_pop = false, bool fused_rhs = false, int *rowexp = nullptr,
+                bool fused_lt = false);
+bool fusedLtUsable(const kgb_ctx *ctx);
 ScatterArgsBase scatterArgs(kgb_ctx *ctx);
 int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr, int *outexp = nullptr);
 int doLPlusTimes(kgb_ctx *ctx, bool acc);
@@ -373,7 +378,8 @@ int doScattering(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr);
 int doSource(kgb_ctx *ctx, double q);
 int doPopulation(kgb_ctx *ctx, double *out);
 int checkDeviceError(kgb_ctx *ctx);
-int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot = nullptr);
+// lt_next: the sweep also adds L psi into phi for the next iteration of the same solve
+int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot = nullptr, bool lt_next = false);
 bool lagPopulation(const kgb_ctx *ctx);
 int resetPsiExp(kgb_ctx *ctx);
 int solveIterations(kgb_ctx *ctx, int niter, double q);

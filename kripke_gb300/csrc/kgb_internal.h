@@ -60,6 +60,11 @@ struct SweepArgs {
   const T *phiout;            // [Z][G][M]
   const T *ellp;              // [D][M]
   int M;
+  // fused LTimes epilogue (mixed form): phiacc(z,g,m) += sum over this subdomain's
+  // directions of ell[d][m] * psi(z,g,d), added per (zone, group, moment) after each
+  // k-slice of a tile (FP32 reductions; phiacc zeroed before the sweep), or null
+  T *phiacc;                  // [Z][G][M]
+  const T *ell;               // [D][M]
   // row exponents for the next LTimes (FP64): rowexp[z*G + g] = max over the
   // row's swept psi of the biased exponent (atomic max, zeroed before the
   // sweep), or null.  rexp_w lanes share a group (a power of two <= 32 that

@@ -61,6 +61,10 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->fuse_sweep = value != 0;
     return KGB_OK;
   }
+  if (!std::strcmp(key, "fused_ltimes")) {
+    ctx->fuse_lt = value != 0;
+    return KGB_OK;
+  }
   if (!std::strcmp(key, "scattering_block")) {
     ctx->allow_blk_sc = ctx->use_blk_sc = value != 0;
     ctx->dirty_tcsc = true;  // the zone lists are (re)built with the scattering plan
@@ -233,6 +237,8 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "scattering_block")) *value = ctx->allow_blk_sc ? 1 : 0;
   else if (!std::strcmp(key, "scattering_block_active")) *value = blockScatterActive(ctx) ? 1 : 0;
   else if (!std::strcmp(key, "fused_sweep_active")) *value = ctx->fuse_active ? 1 : 0;
+  else if (!std::strcmp(key, "fused_ltimes")) *value = ctx->fuse_lt ? 1 : 0;
+  else if (!std::strcmp(key, "fused_ltimes_active")) *value = fusedLtUsable(ctx) ? 1 : 0;
   else if (!std::strcmp(key, "row_exponents")) *value = ctx->allow_row_exp ? 1 : 0;
   else if (!std::strcmp(key, "phi_row_exponents_active")) *value = phiExpUsable(ctx) ? 1 : 0;
   else if (!std::strcmp(key, "psi_row_exponents_active")) *value = psiExpUsable(ctx) ? 1 : 0;

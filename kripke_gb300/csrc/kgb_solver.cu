@@ -53,8 +53,14 @@ bool phiExpUsable(const kgb_ctx *ctx) {
 // rowexp: record psi's row exponents there (the caller zeroed it); null: psi
 // changes without them, so the recorded ones no longer hold.
 template <typename T>
-int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool fused_rhs, int *rowexp) {
+int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool fused_rhs, int *rowexp,
+              bool fused_lt) {
   SweepArgs<T> a{};
+  if (fused_lt && fused_pop && !fused_rhs) {  // the epilogue's kernels carry the fused population
+    a.phiacc = as<T>(ctx->phi);
+    a.ell = as<T>(ctx->ell);
+    a.M = ctx->M;
+  }
   if (rowexp) {
     a.rowexp = rowexp;
     a.rexp_w = psiExpWidth(ctx);
@@ -129,9 +135,16 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool
 }
 
 int sweepWaveAny(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool fused_rhs,
-                 int *rowexp) {
-  return ctx->prec == KGB_FP64 ? sweepWave<double>(ctx, wave_dev, nwave, fused_pop, fused_rhs, rowexp)
-                               : sweepWave<float>(ctx, wave_dev, nwave, fused_pop, fused_rhs, nullptr);
+                 int *rowexp, bool fused_lt) {
+  return ctx->prec == KGB_FP64 ? sweepWave<double>(ctx, wave_dev, nwave, fused_pop, fused_rhs, rowexp, false)
+                               : sweepWave<float>(ctx, wave_dev, nwave, fused_pop, fused_rhs, nullptr, fused_lt);
+}
+
+// The fused LTimes epilogue: the mixed forward sweep with its population fused, no
+// LPlusTimes prologue, and a chain count that fills whole blocks.
+bool fusedLtUsable(const kgb_ctx *ctx) {
+  return ctx->fuse_lt && ctx->prec == KGB_MIXED && !ctx->flip && !(ctx->fuse_sweep && ctx->M <= kFuseMaxM) &&
+         (ctx->Ds * ctx->Gs) % kSweepThreads == 0;
 }
 
 int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
@@ -157,14 +170,16 @@ int fillField(kgb_ctx *ctx, const FieldInfo *f, double v) {
 }
 
 // rowexp (FP64, optional): zeroed here and filled with psi's row exponents.
-int sweepSolver(kgb_ctx *ctx, bool fused_pop, bool fused_rhs, int *rowexp) {
+int sweepSolver(kgb_ctx *ctx, bool fused_pop, bool fused_rhs, int *rowexp, bool fused_lt) {
   for (int k = 0; k < 3; ++k) CK(cudaMemsetAsync(ctx->plane[k], 0, ctx->plane_chunk[k] * ctx->dc.num() * ctx->tsz, ctx->stream));
+  if (fused_lt) CK(cudaMemsetAsync(ctx->phi, 0, ctx->Z * ctx->G * ctx->M * ctx->tsz, ctx->stream));  // kConst(phi, 0)
   if (rowexp) CK(cudaMemsetAsync(rowexp, 0, ctx->Z * ctx->G * sizeof(int), ctx->stream));
   // Block Jacobi (BlockJacobiComm.cpp:46-98 with SweepSolver.cpp:28-30): the
   // planes every subdomain receives are the ones saved right after the zeroing
   // above, so no subdomain waits on another and none hands its outgoing planes
   // on.  One launch sweeps all of them, each from zero inflow on every face.
-  if (ctx->block_jacobi) return sweepWaveAny(ctx, ctx->levels_d, ctx->dc.num(), fused_pop, fused_rhs, rowexp);
+  if (ctx->block_jacobi)
+    return sweepWaveAny(ctx, ctx->levels_d, ctx->dc.num(), fused_pop, fused_rhs, rowexp, fused_lt);
   const int nlev = (int)ctx->level_off.size() - 1;
   const int S[3] = {ctx->dc.Sx, ctx->dc.Sy, ctx->dc.Sz};
   // the reversed (adjoint) orientation visits the zone-set levels last to first
@@ -173,7 +188,7 @@ int sweepSolver(kgb_ctx *ctx, bool fused_pop, bool fused_rhs, int *rowexp) {
     const int lv = ctx->flip ? nlev - 1 - step : step;
     const int b = ctx->level_off[lv], e = ctx->level_off[lv + 1];
     if (e == b) continue;
-    int rc = sweepWaveAny(ctx, ctx->levels_d + b, e - b, fused_pop, fused_rhs, rowexp);
+    int rc = sweepWaveAny(ctx, ctx->levels_d + b, e - b, fused_pop, fused_rhs, rowexp, fused_lt);
     if (rc) return rc;
     // hand the outgoing planes to downwind zone sets (ParallelComm.cpp:146-162)
     for (int x = b; x < e; ++x) {
@@ -465,14 +480,17 @@ int checkDeviceError(kgb_ctx *ctx) {
 // the sweep.  prev_slot: particle count of the psi the iteration starts from,
 // taken from this iteration's own moments (one small pass over moment 0) --
 // a solve counts every iterate that way and the last one after its loop.
-int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot) {
+int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot, bool lt_next) {
   int rc;
   // psi's row exponents, when the sweep that wrote psi recorded them
   const bool px = psiExpUsable(ctx);
   const int *rx = px && ctx->psi_exp_valid ? ctx->psi_exp : nullptr;
   ctx->psi_exp_valid = false;
-  int *const pe = phiExpUsable(ctx) ? ctx->phi_exp : nullptr;  // phi's, for the scattering
-  if ((rc = doLTimes(ctx, false, rx, pe))) return rc;  // phi = L psi        (kConst + LTimes)
+  // phi = L psi already, added up by the previous iteration's sweep (same solve)
+  const bool have_phi = ctx->phi_fused;
+  ctx->phi_fused = false;
+  int *const pe = !have_phi && phiExpUsable(ctx) ? ctx->phi_exp : nullptr;  // phi's, for the scattering
+  if (!have_phi && (rc = doLTimes(ctx, false, rx, pe))) return rc;  // phi = L psi  (kConst + LTimes)
   if (prev_slot) {
     FamScope fs(ctx, "population");
     const int64_t rows = ctx->Z * ctx->G;
@@ -493,9 +511,11 @@ int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot) 
   // rhs = L+ phi_out (kConst + LPlusTimes), or formed cell by cell inside the sweep
   ctx->fuse_active = ctx->fuse_sweep && ctx->prec == KGB_MIXED && ctx->M <= kFuseMaxM;
   if (!ctx->fuse_active && (rc = doLPlusTimes(ctx, false))) return rc;
-  if ((rc = sweepSolver(ctx, part_slot != nullptr, ctx->fuse_active, px ? ctx->psi_exp : nullptr)))
-    return rc;  // psi = H^-1 rhs (+ population, + row exponents)
+  // psi = H^-1 rhs (+ population, + row exponents, + the next iteration's phi)
+  const bool lt = lt_next && part_slot != nullptr && !ctx->fuse_active;
+  if ((rc = sweepSolver(ctx, part_slot != nullptr, ctx->fuse_active, px ? ctx->psi_exp : nullptr, lt))) return rc;
   ctx->psi_exp_valid = px;
+  ctx->phi_fused = lt;
   if (ctx->fuse_active) ctx->rhs_stale = true;
   if (part_slot) {
     FamScope fs(ctx, "population");
@@ -524,8 +544,14 @@ int resetPsiExp(kgb_ctx *ctx) {
 int solveIterations(kgb_ctx *ctx, int niter, double q) {
   int rc;
   if (!lagPopulation(ctx)) {
+    // the last iteration's sweep adds no moments: phi ends as the reference leaves it, L of
+    // the psi the last iteration started from
+    const bool lt = fusedLtUsable(ctx);
     for (int it = 0; it < niter; ++it)
-      if ((rc = iterateDevice(ctx, q, ctx->parts_dev + it))) return rc;
+      if ((rc = iterateDevice(ctx, q, ctx->parts_dev + it, nullptr, lt && it + 1 < niter))) {
+        ctx->phi_fused = false;
+        return rc;
+      }
     return KGB_OK;
   }
   // the count after iteration it-1 from iteration it's moments, the last one from psi

@@ -135,9 +135,13 @@ constexpr int sweepSlots() {
                         (PFM == 2 && TX * TY <= 8 && !RECIP ? TX * TY : 0);
 }
 
-template <typename T, int TX, int TY, bool RECIP, bool POP, bool COH, bool FUSE = false, int PFM = 0>
+template <typename T, int TX, int TY, bool RECIP, bool POP, bool COH, bool FUSE = false, int PFM = 0, bool LTF = false>
 __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom, const int tile, const int cb,
-                                          const int ncb, T (*rbuf)[kSweepThreads] = nullptr) {
+                                          const int ncb, T (*rbuf)[kSweepThreads] = nullptr,
+                                          T (*ltb)[kSweepThreads] = nullptr) {
+  // LTF: every thread of the block owns a chain (the caller launches it only when the
+  // chain count is a multiple of the block), so the slice barriers below are block-wide
+  static_assert(!LTF || (!COH && !FUSE && PFM == 0), "fused LTimes: per-step mixed sweep only");
   const SdomDesc sd = a.sdoms[sdom];
   // the adjoint sweep (transposed operator) runs every direction in its reversed orientation
   const int sid = a.flip ? -sd.id : sd.id, sjd = a.flip ? -sd.jd : sd.jd, skd = a.flip ? -sd.kd : sd.kd;
@@ -260,6 +264,13 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
         }
       }
       const T czk = a.cz[(int64_t)d * a.nz + sd.ko + k];
+      T pv[LTF ? TY : 1][LTF ? TX : 1];  // LTF: this slice's psi values (0 at cells off the mesh)
+      if constexpr (LTF) {
+#pragma unroll
+        for (int jj = 0; jj < TY; ++jj)
+#pragma unroll
+          for (int ii = 0; ii < TX; ++ii) pv[jj][ii] = T(0);
+      }
       // The slice's loads do not depend on the upwind chain: issue them all
       // before the first cell so their latency overlaps.
       T rv[TY][TX], sv[TY][TX];
@@ -330,6 +341,7 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
             ps = num / den;
           }
           psi[e] = ps;
+          if constexpr (LTF) pv[jj][ii] = ps;
           if constexpr (sizeof(T) == 8) {
             if (a.rowexp) rowExpMax(a.rowexp, a.rexp_w, rmask, ps, z * a.G + g);
           }
@@ -346,6 +358,48 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
 #pragma unroll
       for (int ii = 0; ii < TX; ++ii)
         if (iv[ii]) jpl[((int64_t)k * a.nxs + iloc[ii]) * nchain + c] = fr[ii];
+      if constexpr (LTF) {
+        // The slice's moments of this subdomain: the block's psi values go to shared
+        // memory (two buffers, alternating by slice, so one barrier per slice), then each
+        // thread takes (group, moment) pairs of the block's chains and, for every cell,
+        // sums ell[d][m] psi over the group's directions in the block (ascending), and
+        // adds the sum to phiacc.
+        T(*sm)[kSweepThreads] = ltb + (kk & 1) * (TX * TY);
+#pragma unroll
+        for (int jj = 0; jj < TY; ++jj)
+#pragma unroll
+          for (int ii = 0; ii < TX; ++ii) sm[jj * TX + ii][threadIdx.x] = pv[jj][ii];
+        __syncthreads();
+        const int c0 = cb * (int)blockDim.x;
+        const int gfirst = c0 / a.Ds, glast = (c0 + (int)blockDim.x - 1) / a.Ds;
+        const int npair = (glast - gfirst + 1) * a.M;
+        for (int p = threadIdx.x; p < npair; p += blockDim.x) {
+          const int gi = p / a.M, m = p - gi * a.M;
+          const int gl2 = gfirst + gi;
+          const int cs = max(gl2 * a.Ds, c0), ce = min(gl2 * a.Ds + a.Ds, c0 + (int)blockDim.x);
+          T acc[TY][TX];
+#pragma unroll
+          for (int jj = 0; jj < TY; ++jj)
+#pragma unroll
+            for (int ii = 0; ii < TX; ++ii) acc[jj][ii] = T(0);
+          for (int ch = cs; ch < ce; ++ch) {
+            const T e = a.ell[(int64_t)(sd.dlo + ch - gl2 * a.Ds) * a.M + m];
+#pragma unroll
+            for (int jj = 0; jj < TY; ++jj)
+#pragma unroll
+              for (int ii = 0; ii < TX; ++ii) acc[jj][ii] += e * sm[jj * TX + ii][ch - c0];
+          }
+          const int64_t gz = sd.glo + gl2;
+#pragma unroll
+          for (int jj = 0; jj < TY; ++jj)
+#pragma unroll
+            for (int ii = 0; ii < TX; ++ii)
+              if (iv[ii] && jv[jj]) {
+                const int64_t z = (zslice + (sd.jo + jloc[jj])) * a.nx + sd.io + iloc[ii];
+                atomicAdd(a.phiacc + (z * a.G + gz) * a.M + m, acc[jj][ii]);
+              }
+        }
+      }
     }
 #pragma unroll
     for (int ii = 0; ii < TX; ++ii)
@@ -361,13 +415,14 @@ __device__ __forceinline__ void sweepTile(const SweepArgs<T> &a, const int sdom,
   }
 }
 
-template <typename T, int TX, int TY, bool RECIP, bool POP, bool FUSE = false>
+template <typename T, int TX, int TY, bool RECIP, bool POP, bool FUSE = false, bool LTF = false>
 __global__ void __launch_bounds__(kSweepThreads) sweep_step_kernel(const __grid_constant__ SweepArgs<T> a) {
-  constexpr int PFM = (sizeof(T) == 8 && !FUSE) ? 2 : 0;
+  constexpr int PFM = (sizeof(T) == 8 && !FUSE && !LTF) ? 2 : 0;
   constexpr int kSlots = sweepSlots<TX, TY, RECIP, false, PFM>();
   __shared__ T rbuf[kSlots > 0 ? 2 * kSlots : 1][kSweepThreads];
-  sweepTile<T, TX, TY, RECIP, POP, false, FUSE, PFM>(a, a.wave[blockIdx.z], a.tile_off + blockIdx.y, blockIdx.x,
-                                                     gridDim.x, rbuf);
+  __shared__ T ltb[LTF ? 2 * TX * TY : 1][kSweepThreads];
+  sweepTile<T, TX, TY, RECIP, POP, false, FUSE, PFM, LTF>(a, a.wave[blockIdx.z], a.tile_off + blockIdx.y,
+                                                          blockIdx.x, gridDim.x, rbuf, ltb);
 }
 
 namespace {
@@ -458,11 +513,17 @@ void launchTileAs(const SweepArgs<T> &a, dim3 grid, cudaStream_t s) {
   else if (pop) sweep_step_kernel<T, TX, TY, false, true, FUSE><<<grid, kSweepThreads, 0, s>>>(a);
   else sweep_step_kernel<T, TX, TY, false, false, FUSE><<<grid, kSweepThreads, 0, s>>>(a);
 }
-// the fused LPlusTimes prologue exists for the mixed form only
+// the fused LPlusTimes prologue and LTimes epilogue exist for the mixed form only
 template <typename T, int TX, int TY>
 void launchTile(const SweepArgs<T> &a, dim3 grid, cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
     if (a.phiout != nullptr) return launchTileAs<T, TX, TY, true>(a, grid, s);
+    if (a.phiacc != nullptr && a.pop != nullptr) {  // the epilogue rides on the fused population
+      const bool recip = a.cls != nullptr && a.inv != nullptr;
+      if (recip) sweep_step_kernel<T, TX, TY, true, true, false, true><<<grid, kSweepThreads, 0, s>>>(a);
+      else sweep_step_kernel<T, TX, TY, false, true, false, true><<<grid, kSweepThreads, 0, s>>>(a);
+      return;
+    }
   }
   launchTileAs<T, TX, TY, false>(a, grid, s);
 }
