@@ -236,6 +236,19 @@ def timed_steps(ctx, stream, steps):
     return e0.elapsed_time(e1) / steps
 
 
+def timed_solve(ctx, stream, steps):
+    """One solve of K iterations (the replayed solve graph) between CUDA events; ms per iteration."""
+    import torch
+    ctx.solve(steps)  # captures the graph
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ctx.solve(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
 def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     """The mixed form on the same workload: throughput against the FP64 form and phi error against FP64."""
     import numpy as np
@@ -252,6 +265,15 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     for _ in range(args.warmup):
         ctx.iterate(want_population=False)
     ms = timed_steps(ctx, stream, args.steps)
+    # the fused LTimes epilogue acts inside a solve (the next iteration takes the sweep's moments):
+    # solves of K iterations with and without it
+    ms_solve = timed_solve(ctx, stream, args.steps)
+    ctx.set_option("fused_ltimes", 1)
+    lt_active = ctx.get_option("fused_ltimes_active")
+    ms_lt = timed_solve(ctx, stream, args.steps)
+    ctx.solve(MIXED_PHI_ITERS)
+    phi_lt = ctx.download("phi")
+    ctx.set_option("fused_ltimes", 0)
     # the fused sweep (rhs formed inside the sweep, no LPlusTimes launch) on the same state
     ctx.set_option("fused_sweep", 1)
     for _ in range(args.warmup):
@@ -274,6 +296,8 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     del phi_fused
     err = float(np.abs(b - a).max() / np.abs(a).max())
     err_l2 = float(np.linalg.norm(b - a) / np.linalg.norm(a))
+    lt_err = phi_errors(phi_lt, a)
+    del phi_lt
     # moment 0 (DGZ host nesting: phi chunks are [M][G][Z], one chunk per group set)
     M = (w["legendre"] + 1) ** 2
     a0, b0 = a.reshape(M, -1)[0], b.reshape(M, -1)[0]
@@ -292,7 +316,13 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
                            "identical_to_unfused_simt": fused_same,
                            "what": "LPlusTimes formed inside the sweep (rhs neither written nor read), same tiles; "
                                    "compared bit for bit with the unfused iteration whose LPlusTimes is the SIMT "
-                                   "kernel (same arithmetic)"}}
+                                   "kernel (same arithmetic)"},
+           "fused_ltimes": {"ms_per_iteration": ms_lt, "unfused_ms_per_iteration": ms_solve,
+                            "speedup_vs_unfused": ms_solve / ms_lt, "active": lt_active,
+                            "phi_rel_err_vs_fp64": lt_err,
+                            "what": "solves of %d iterations (replayed graphs): every sweep but the last adds the "
+                                    "next iteration's moments phi = L psi (FP32 reductions per k-slice of a tile) "
+                                    "and the next iteration runs no LTimes" % args.steps}}
     ctx.close()
     return out
 

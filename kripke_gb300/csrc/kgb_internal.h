@@ -151,6 +151,7 @@ struct ScatterBlockPlan {
 struct ScatterZonePlan {
   int64_t off[4];
   int G, zpi;            // groups; zones per item of one 128-thread group
+  int nh, qw, zw;        // a zone's quads in nh parts of qw (<= 8); zw zones per warp
   uint32_t slot;         // floats between staged zone blocks
   const int *gp_lo, *gp_hi;
   int *err;              // raised when a copy's bounded wait gives up

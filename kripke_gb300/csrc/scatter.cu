@@ -206,7 +206,11 @@ __global__ void __launch_bounds__(kBlkThreads, 2)
 // of that material: one elected thread brings each zone's contiguous [G][MM]
 // phi block into the group's buffer with one bulk copy (an mbarrier counts the
 // bytes); a thread then owns 4 destination groups x MM moments of one zone in
-// registers and walks the source groups g' over its warp's nonzero range, in
+// registers.  A warp covers at most 8 group quads of each of its zw zones (with
+// 64 groups, two warps split a zone's quads), so its source-group range is that
+// of its own destination groups -- with downscatter the low groups' warps stop
+// early -- and its matrix loads are one 128-byte row.  It walks the source
+// groups g' over its warp's nonzero range, in
 // steps of 4 so that the offset of row g' within its 16-byte word is a
 // compile-time constant (rows are MM floats; (MM g') mod 4 depends on g' mod 4
 // only): a row is read as 16-byte broadcasts, a matrix row as one 16-byte load
@@ -268,15 +272,18 @@ __global__ void __launch_bounds__(kZoneThreads, 1)
   const int tid = threadIdx.x, gi = tid / kZoneGroup, gt = tid % kZoneGroup;
   float *buf = zone_smem + (size_t)L1 * G * G + (size_t)gi * zpi * pl.slot;
   const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&full[gi]);
-  const int c = gt / GQ, q = gt - (gt / GQ) * GQ;  // zone slot, group quad
-  const bool lane_ok = c < zpi;
+  // warp -> (row of zw zones, part h of the quads); lane -> (zone of the row, quad of the part)
+  const int gw = gt / 32, ln = gt % 32, h = gw % pl.nh, lz = ln / pl.qw;
+  const int c = (gw / pl.nh) * pl.zw + lz, q = h * pl.qw + ln % pl.qw;  // zone slot, group quad
+  const bool lane_ok = lz < pl.zw && q < GQ && c < zpi;
+  const int qr = q < GQ ? q : GQ - 1;  // quad read by idle lanes (results unused)
   const int cr = lane_ok ? c : zpi - 1;  // slot read by idle lanes (results unused)
   // this warp's source-group range, rounded out to whole steps of 4
   int lo = G, hi = -1;
   if (lane_ok)
     for (int i = 0; i < 4; ++i) {
-      lo = min(lo, pl.gp_lo[4 * q + i]);
-      hi = max(hi, pl.gp_hi[4 * q + i]);
+      lo = min(lo, pl.gp_lo[4 * qr + i]);
+      hi = max(hi, pl.gp_hi[4 * qr + i]);
     }
   lo = __reduce_min_sync(0xffffffffu, lo) & ~3;
   hi = (__reduce_max_sync(0xffffffffu, hi) + 4) & ~3;
@@ -360,7 +367,7 @@ __global__ void __launch_bounds__(kZoneThreads, 1)
           }
           float4 sl[L1];
 #pragma unroll
-          for (int l = 0; l < L1; ++l) sl[l] = *reinterpret_cast<const float4 *>(sS + ((size_t)l * G + gp) * G + 4 * q);
+          for (int l = 0; l < L1; ++l) sl[l] = *reinterpret_cast<const float4 *>(sS + ((size_t)l * G + gp) * G + 4 * qr);
 #pragma unroll
           for (int k = 0; k < MM; ++k) {
             const float p = v[R + k];
@@ -449,7 +456,18 @@ uint32_t zoneSlot(int G, int L) {
   if ((slot / 4) % 2 == 0) slot += 4;
   return slot;
 }
-int zoneItemZones(int G) { return std::max(1, kZoneGroup / (G / 4)); }
+// a zone's G/4 quads in nh parts of qw <= 8 (one warp each), zw = 32 / qw zones per warp
+void zoneLanes(int G, int &nh, int &qw, int &zw) {
+  const int gq = G / 4;
+  nh = (gq + 7) / 8;
+  qw = (gq + nh - 1) / nh;
+  zw = 32 / qw;
+}
+int zoneItemZones(int G) {
+  int nh, qw, zw;
+  zoneLanes(G, nh, qw, zw);
+  return (kZoneGroup / 32 / nh) * zw;
+}
 }  // namespace
 
 size_t scatter_block_smem(int G, int L) {
@@ -468,6 +486,7 @@ void launch_scatter_block(const float *phi, float *phi_out, const float *sigsT, 
     ScatterZonePlan pl{};
     pl.G = G;
     pl.zpi = zoneItemZones(G);
+    zoneLanes(G, pl.nh, pl.qw, pl.zw);
     pl.slot = zoneSlot(G, L);
     pl.gp_lo = gp_lo;
     pl.gp_hi = gp_hi;
