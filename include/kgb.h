@@ -184,11 +184,16 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * FP64 default; 0 = divide in every cell, the mixed default); "moments_tensor"
  * (1 = LTimes and LPlusTimes on the tensor cores with exact digit products when
  * the shapes fit; 0 = SIMT kernels; default: tensor for FP64, SIMT for the
- * mixed form); "moments_tf32" (mixed form: 1 = LTimes and LPlusTimes as
- * split-TF32 tensor-core GEMMs -- each FP32 operand split exactly into three
+ * mixed form); "moments_tf32" (mixed form: 1 = LTimes and LPlusTimes may run
+ * as split-TF32 tensor-core GEMMs -- each FP32 operand split exactly into three
  * TF32 pieces, six products, FP32 accumulation -- when moments <= 32 and there
  * are at least 32 directions, a multiple of 4 (LTimes) or of 16 up to 256
- * (LPlusTimes); ahead of "moments_tensor"; the default; 0 = off);
+ * (LPlusTimes); ahead of "moments_tensor"; the default; 0 = off), with
+ * "moments_tf32_lplustimes" (1 = LPlusTimes may, the default) and
+ * "moments_tf32_ltimes" (1 = LTimes may; default 0: the tensor core's
+ * accumulation truncates, and LTimes, whose directions weigh alike, would bias
+ * phi towards zero by up to about one unit in the last place per iteration,
+ * where LPlusTimes adds its dominant moment last);
  * "scattering_tensor" (1 = the single-material zones' scattering on the tensor
  * cores, exact digit products, when groups <= 64; the default in both forms);
  * "scattering_block" (mixed form: 1 = the single-material zones' scattering by
@@ -230,7 +235,9 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
  * kernel runs on the tensor cores), "sweep_reciprocals_active" (1 when the
  * sweep uses tabulated reciprocals), "graph_active" (1 when the last
  * kgb_solve replayed a graph), "fused_sweep_active" (1 when the last
- * iteration formed rhs inside the sweep), "fused_ltimes_active" (1 when
+ * iteration formed rhs inside the sweep), "moments_tf32_ltimes" and
+ * "moments_tf32_lplustimes" (1 when that transform runs the TF32 kernel),
+ * "fused_ltimes_active" (1 when
  * kgb_solve fuses the LTimes epilogue on this problem),
  * "psi_row_exponents_active" and
  * "phi_row_exponents_active" (1 when the solver loop records them on this

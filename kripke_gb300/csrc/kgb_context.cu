@@ -444,10 +444,12 @@ int planTf32From(kgb_ctx *ctx, const std::vector<double> &lt_src, const std::vec
 }
 
 bool tf32LtActive(const kgb_ctx *ctx) {
-  return ctx->prec == KGB_MIXED && ctx->allow_tf32 && ctx->use_tf32_lt && ctx->tf32_lt_img != nullptr;
+  return ctx->prec == KGB_MIXED && ctx->allow_tf32 && ctx->allow_tf32_lt && ctx->use_tf32_lt &&
+         ctx->tf32_lt_img != nullptr;
 }
 bool tf32LpActive(const kgb_ctx *ctx) {
-  return ctx->prec == KGB_MIXED && ctx->allow_tf32 && ctx->use_tf32_lp && ctx->tf32_lp_img != nullptr;
+  return ctx->prec == KGB_MIXED && ctx->allow_tf32 && ctx->allow_tf32_lp && ctx->use_tf32_lp &&
+         ctx->tf32_lp_img != nullptr;
 }
 
 template <typename T>

@@ -179,7 +179,10 @@ struct kgb_ctx {
   // split-TF32 tensor-core LTimes / LPlusTimes of the mixed form (tf32_moments.cu): B images
   // of the forward operators and of the adjoint's (exchanged by AdjointView)
   bool allow_tf32 = true;                          // option "moments_tf32"
-  bool use_tf32_lt = true, use_tf32_lp = true;     // autotuner's choice
+  // per transform (options "moments_tf32_ltimes", "moments_tf32_lplustimes"): the TF32 LTimes'
+  // truncating accumulations bias phi, so it is opt-in; LPlusTimes' leading moment comes last
+  bool allow_tf32_lt = false, allow_tf32_lp = true;
+  bool use_tf32_lt = false, use_tf32_lp = true;    // autotuner's choice
   float *tf32_lt_img = nullptr, *tf32_lp_img = nullptr;
   float *tf32_lt_img_adj = nullptr, *tf32_lp_img_adj = nullptr;
   // row exponents of psi for the tensor-core LTimes (FP64), written by the solver's sweep:

@@ -41,9 +41,17 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
   }
   if (!std::strcmp(key, "moments_tf32")) {
     ctx->allow_tf32 = value != 0;
-    ctx->use_tf32_lt = ctx->use_tf32_lp = value != 0;
+    ctx->use_tf32_lt = value != 0 && ctx->allow_tf32_lt;
+    ctx->use_tf32_lp = value != 0 && ctx->allow_tf32_lp;
     ctx->dirty_ell = true;
     ctx->adj_stale = true;
+    ++ctx->gen;
+    return KGB_OK;
+  }
+  const bool tf32_lt = !std::strcmp(key, "moments_tf32_ltimes");
+  if (tf32_lt || !std::strcmp(key, "moments_tf32_lplustimes")) {  // one transform, within "moments_tf32"
+    (tf32_lt ? ctx->allow_tf32_lt : ctx->allow_tf32_lp) = value != 0;
+    (tf32_lt ? ctx->use_tf32_lt : ctx->use_tf32_lp) = value != 0;
     ++ctx->gen;
     return KGB_OK;
   }
@@ -157,7 +165,8 @@ int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_
     return r ? r : checkDeviceError(ctx);
   };
   for (int lt = 1; lt >= 0 && !rc; --lt) {
-    const bool tf32 = ctx->prec == KGB_MIXED && ctx->allow_tf32 && (lt ? ctx->tf32_lt_img : ctx->tf32_lp_img);
+    const bool tf32 = ctx->prec == KGB_MIXED && ctx->allow_tf32 && (lt ? ctx->allow_tf32_lt : ctx->allow_tf32_lp) &&
+                      (lt ? ctx->tf32_lt_img : ctx->tf32_lp_img);
     const bool tc = lt ? ctx->tc_lt : ctx->tc_lp;
     float best_t = 0.f;
     int best_mode = -1;

@@ -472,8 +472,11 @@ __global__ void __launch_bounds__(kThreads, 1) tf32x3_kernel(const __grid_consta
           mmaTf32(dcol, amid + ks * 8, dh, idesc, 1u);
           mmaTf32(dcol, ahi + ks * 8, dm, idesc, 1u);
         }
+        // the leading products in descending K order: the accumulator truncates (towards zero)
+        // at each step, and in LPlusTimes the first K step holds moment 0, which dominates the
+        // sum; added last, only one truncation happens at the sum's full magnitude
 #pragma unroll
-        for (int ks = 0; ks < kChunk / 8; ++ks) {
+        for (int ks = kChunk / 8 - 1; ks >= 0; --ks) {
           const uint32_t boff = (uint32_t)((c * kChunk + ks * 8) / 4) * lbo;
           mmaTf32(dcol, ahi + ks * 8, matDesc(bHi + boff, lbo, 128), idesc, 1u);
         }

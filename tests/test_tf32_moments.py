@@ -1,14 +1,21 @@
 """The mixed form's LTimes and LPlusTimes as split-TF32 tensor-core GEMMs (tf32_moments.cu).
 
-Each operand is split as hi + lo (both TF32, rounded to nearest) and every product taken as
-hi hi + hi lo + lo hi with FP32 accumulation in tensor memory, so an output carries about the
-FP32 rounding error of the SIMT kernels it replaces.  Checked through the C ABI against the FP64
-oracle (whose kernels equal the reference's bit for bit): elementwise within
-8 * 2^-22 * sum_k |a_k b_k| + 2^-20 * |C| of the FP64 result, and with a largest error at most
-twice that of the FP32 SIMT kernel on the same inputs -- on tail tiles, several tiles per CTA,
-every supported width, and in the accumulating form of the kernel entry points (bulk
-reduce-adds).  Whole mixed solves with the TF32 kernels stay within the mixed form's 1e-6 of the
-FP64 oracle (2-norm ratio).
+Each FP32 element of A is split exactly into three TF32 pieces (truncation), B likewise on the
+host (rounding), and every product taken as the six terms up to 2^-20 of the leading one, the
+small terms first, the leading ones last, with FP32 accumulation in tensor memory.  Checked
+through the C ABI against the FP64 oracle (whose kernels equal the reference's bit for bit):
+elementwise within 8 * 2^-22 * sum_k |a_k b_k| + 2^-20 * |C| of the FP64 result, and with a
+largest error at most twice that of the FP32 SIMT kernel on the same inputs -- on tail tiles,
+several tiles per CTA, every supported width, and in the accumulating form of the kernel entry
+points (bulk reduce-adds).  Whole mixed solves with the TF32 kernels stay within the mixed form's
+1e-6 of the FP64 oracle (2-norm ratio).
+
+The tensor core's accumulation truncates, so each accumulation at a sum's full magnitude pulls it
+towards zero by up to one unit in the last place, and over a source iteration with strong
+scattering that bias adds up where the SIMT kernels' round-to-nearest errors cancel.  LPlusTimes
+adds its leading products in descending moment order (moment 0, which dominates, last), which
+brings it to the SIMT kernel's error; LTimes has no dominant direction, so its TF32 kernel is
+opt-in ("moments_tf32_ltimes") and the mixed default keeps the SIMT LTimes.
 """
 import numpy as np
 import pytest
@@ -27,6 +34,7 @@ def run_both(ctx, op, fill):
     out = []
     for tf32 in (1, 0):
         ctx.set_option("moments_tf32", tf32)
+        ctx.set_option("moments_tf32_ltimes", tf32)
         fill()
         op()
         out.append(ctx.get_option("moments_tf32_ltimes" if op == ctx.ltimes else "moments_tf32_lplustimes"))
@@ -99,6 +107,7 @@ def test_tf32_solve_against_fp64(oracle, kgb, kw):
     """A mixed solve with the TF32 kernels in its loop against the FP64 oracle, and against the same
     mixed solve with the FP32 SIMT kernels."""
     p, ctx = pair(oracle, kgb, precision=kgb.MIXED, **kw)
+    ctx.set_option("moments_tf32_ltimes", 1)
     want_parts = p.solve(8)
     parts = ctx.solve(8)
     assert ctx.get_option("moments_tf32_ltimes") == 1 and ctx.get_option("moments_tf32_lplustimes") == 1
@@ -116,6 +125,35 @@ def test_tf32_solve_against_fp64(oracle, kgb, kw):
     assert m_tf <= 2e-6
     np.testing.assert_allclose(parts, want_parts, rtol=2e-6)
     ctx.close()
+
+
+def test_tf32_defaults_and_bias_under_strong_scattering(kgb):
+    """The mixed default runs the TF32 LPlusTimes and the SIMT LTimes.  On a problem with
+    scattering ratios up to 0.9 (one of the seeded uneven batch problems: 27 x 37 x 15 zones, 32
+    groups, 48 directions, P4), after 10 iterations, the default's phi error against FP64 stays
+    within 1.6x the all-SIMT error (the leading moment added last), while the TF32 LTimes, opt-in,
+    shows the bias of its truncating accumulations."""
+    from kripke_gb300.batching import uneven_inputs
+    im, idd = uneven_inputs(48, seed=2026, precision=kgb.MIXED)[18], uneven_inputs(48, seed=2026, precision=kgb.FP64)[18]
+    c = kgb.Context(0)
+    c.generate(idd)
+    c.solve(10)
+    ref = c.download("phi")
+    c.close()
+    errs = {}
+    for name, opts in (("default", {}), ("simt", {"moments_tf32": 0}), ("tf32_lt", {"moments_tf32_ltimes": 1})):
+        c = kgb.Context(0)
+        c.generate(im)
+        for k, v in opts.items():
+            c.set_option(k, v)
+        c.solve(10)
+        errs[name] = (np.linalg.norm(c.download("phi") - ref) / np.linalg.norm(ref),
+                      c.get_option("moments_tf32_ltimes"), c.get_option("moments_tf32_lplustimes"))
+        c.close()
+    print("phi error vs FP64 (2-norm):", {k: "%.3e" % v[0] for k, v in errs.items()})
+    assert errs["default"][1:] == (0, 1) and errs["simt"][1:] == (0, 0) and errs["tf32_lt"][1:] == (1, 1)
+    assert errs["default"][0] <= 1.6 * errs["simt"][0] and errs["default"][0] <= 1e-6
+    assert errs["tf32_lt"][0] <= 1e-6
 
 
 def test_tf32_not_in_fp64(kgb, oracle):
