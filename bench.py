@@ -285,7 +285,8 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     ctx.set_option("fused_sweep", 0)
     kernels = {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "moments_tf32_ltimes",
                                               "moments_tf32_lplustimes", "moments_tensor_ltimes",
-                                              "moments_tensor_lplustimes", "scattering_tensor_active")}
+                                              "moments_tensor_lplustimes", "scattering_tensor_active",
+                                              "scattering_block_active")}
     parts = ctx.solve(MIXED_PHI_ITERS)
     fp64_ctx.solve(MIXED_PHI_ITERS)
     a, b = fp64_ctx.download("phi"), ctx.download("phi")
@@ -567,7 +568,9 @@ def run_gpu(args, world, rank, local):
     ctx.iterate(want_population=False)
     tuned = ctx.autotune() if not args.no_autotune else None
     active = {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "sweep_reciprocals_active",
-                                             "moments_tensor_ltimes", "moments_tensor_lplustimes", "scattering_tensor_active")}
+                                             "moments_tensor_ltimes", "moments_tensor_lplustimes", "moments_tf32_ltimes",
+                                             "moments_tf32_lplustimes", "scattering_tensor_active",
+                                             "scattering_block_active")}
 
     # warm-up (the solve starts from psi = 0, like SteadyStateSolver)
     ctx.fill("psi", 0.0)

@@ -238,7 +238,8 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "moments_tf32_lplustimes")) *value = tf32LpActive(ctx) ? 1 : 0;
   else if (!std::strcmp(key, "graph")) *value = ctx->use_graph ? 1 : 0;
   else if (!std::strcmp(key, "scattering_tensor")) *value = ctx->allow_tc_sc ? 1 : 0;
-  else if (!std::strcmp(key, "scattering_tensor_active")) *value = (ctx->tc_sc && ctx->use_tc_sc) ? 1 : 0;
+  else if (!std::strcmp(key, "scattering_tensor_active"))  // the zone-blocked kernel, when active, takes precedence
+    *value = (ctx->tc_sc && ctx->use_tc_sc && !blockScatterActive(ctx)) ? 1 : 0;
   else if (!std::strcmp(key, "graph_active")) *value = ctx->graph_active ? 1 : 0;
   else if (!std::strcmp(key, "block_jacobi")) *value = ctx->block_jacobi ? 1 : 0;
   else if (!std::strcmp(key, "fused_sweep")) *value = ctx->fuse_sweep ? 1 : 0;
