@@ -114,6 +114,10 @@ struct kgb_ctx {
   int tz = 4;
   int tx = 4, ty = 4;  // sweep tile footprint
   bool tiles_set = false;  // the caller chose the tile shape: setup keeps it
+  // FP32 sweeps on the streamed kernel (sweep_stream.cu) where it applies, with
+  // stream_ns k-slices of operands in flight per block
+  bool allow_stream = true;
+  int stream_ns = 2;
 
   // device state (element type T = double or float by precision)
   void *psi = nullptr, *rhs = nullptr, *phi = nullptr, *phi_out = nullptr, *sigt = nullptr;
@@ -372,6 +376,7 @@ int fillField(kgb_ctx *ctx, const FieldInfo *f, double v);
 int sweepSolver(kgb_ctx *ctx, bool fused_pop = false, bool fused_rhs = false, int *rowexp = nullptr,
                 bool fused_lt = false);
 bool fusedLtUsable(const kgb_ctx *ctx);
+bool streamUsable(const kgb_ctx *ctx);
 ScatterArgsBase scatterArgs(kgb_ctx *ctx);
 int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp = nullptr, int *outexp = nullptr);
 int doLPlusTimes(kgb_ctx *ctx, bool acc);

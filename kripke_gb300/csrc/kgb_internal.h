@@ -71,6 +71,11 @@ struct SweepArgs {
   // divides Ds, or 32 when 32 divides Ds).
   int *rowexp;
   int rexp_w;
+  // streamed FP32 sweep (sweep_stream.cu): stages of slice operands in flight
+  // (0: the per-step kernel of sweep.cu), and the word a bounded wait that
+  // gives up sets
+  int stream_ns;
+  int *err;
 };
 
 // Largest moment count (Legendre order 4) of the fused LPlusTimes prologue.
@@ -82,6 +87,19 @@ constexpr int kSweepThreads = 128;
 
 template <typename T>
 void launch_sweep_step(const SweepArgs<T> &a, int ntiles, int nwave, cudaStream_t s);
+
+// Streamed FP32 sweep (sweep_stream.cu): each block's rhs and sigt of a whole
+// k-slice of its tile arrive in shared memory by one TMA copy each, several
+// slices ahead.  It applies to the divide form (no reciprocal tables, fused
+// prologue or epilogue) when a block's 128 chains are whole groups whose
+// operand boxes meet TMA's 16-byte rules: directions per set 4, 8, 16 or 32,
+// D and G multiples of 4.  Tile footprints 4x4 and 4x2 (wider tiles measured
+// slower: their face registers cut the resident warps).
+constexpr int kStreamMaxStages = 4;
+bool sweep_stream_applies(int D, int G, int Ds, int Gs, int tx, int ty);
+// launches one hyperplane step (a.stream_ns stages); false when a tensor map
+// cannot be encoded (nothing launched)
+bool launch_sweep_step_stream(const SweepArgs<float> &a, int ntiles, int nwave, cudaStream_t s);
 
 // Classes of the distinct sigt values for the sweep's reciprocal tables, on the
 // device: class_insert records every distinct bit pattern of sig in an

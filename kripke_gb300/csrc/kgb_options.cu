@@ -65,6 +65,15 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->sweep_streams = (int)std::min<int64_t>(value, ctx->max_streams);
     return KGB_OK;
   }
+  if (!std::strcmp(key, "sweep_stream")) {
+    ctx->allow_stream = value != 0;
+    return KGB_OK;
+  }
+  if (!std::strcmp(key, "sweep_stream_stages")) {
+    if (value < 1 || value > kStreamMaxStages) return fail(ctx, KGB_ERR_ARG, "sweep_stream_stages must be 1 to 4");
+    ctx->stream_ns = (int)value;
+    return KGB_OK;
+  }
   if (!std::strcmp(key, "fused_sweep")) {
     ctx->fuse_sweep = value != 0;
     return KGB_OK;
@@ -103,7 +112,7 @@ int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_
   if (!rc) rc = ensureRhs(ctx);
   if (rc) return rc;
   const int xys[3] = {44, 42, 22};
-  const int tzs[4] = {2, 4, 8, 16};
+  const int tzs[5] = {2, 4, 8, 16, 32};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -111,31 +120,48 @@ int kgb_autotune(kgb_ctx *ctx, double *best_ms, int32_t *tile_xy, int32_t *tile_
   ctx->timing = false;
   float best = 1e30f;
   int bxy = 44, btz = 4;
+  // the streamed FP32 sweep against the per-step kernel, where both exist
+  const bool allow_stream = ctx->allow_stream;
+  bool bstream = allow_stream;
   // the sweep variant the solver runs: fused population partials unless the FP64
   // count comes from the next iteration's moments
   const bool pop = !lagPopulation(ctx);
+  // one sweep shape: the mean of two timed sweeps after a warm-up one
+  auto timeShape = [&](float &ms) -> int {
+    int r = buildTiles(ctx);
+    if (!r) r = sweepSolver(ctx, pop);  // warm-up
+    if (r) return r;
+    CK(cudaEventRecord(e0, ctx->stream));
+    for (int k = 0; k < 2 && !r; ++k) r = sweepSolver(ctx, pop);
+    if (r) return r;
+    CK(cudaEventRecord(e1, ctx->stream));
+    CK(cudaEventSynchronize(e1));
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    ms *= 0.5f;
+    return KGB_OK;
+  };
   for (int xy : xys)
-    for (int tz : tzs) {
-      if (tz > 2 * ctx->nzs && tz != 2) continue;
-      ctx->tx = xy / 10;
-      ctx->ty = xy % 10;
-      ctx->tz = tz;
-      if ((rc = buildTiles(ctx))) break;
-      if ((rc = sweepSolver(ctx, pop))) break;  // warm-up
-      CK(cudaEventRecord(e0, ctx->stream));
-      for (int r = 0; r < 2; ++r)
-        if ((rc = sweepSolver(ctx, pop))) break;
-      CK(cudaEventRecord(e1, ctx->stream));
-      CK(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      CK(cudaEventElapsedTime(&ms, e0, e1));
-      ms *= 0.5f;
-      if (ms < best) {
-        best = ms;
-        bxy = xy;
-        btz = tz;
+    for (int streamed = 1; streamed >= 0 && !rc; --streamed)
+      for (int tz : tzs) {
+        if (tz > 2 * ctx->nzs && tz != 2) continue;
+        ctx->tx = xy / 10;
+        ctx->ty = xy % 10;
+        ctx->allow_stream = true;
+        const bool can_stream = allow_stream && streamUsable(ctx);
+        if (streamed && !can_stream) continue;  // no streamed variant of this shape here
+        if (tz == 32 && !streamed) continue;
+        ctx->allow_stream = streamed != 0;
+        ctx->tz = tz;
+        float ms = 0.f;
+        if ((rc = timeShape(ms))) break;
+        if (ms < best) {
+          best = ms;
+          bxy = xy;
+          btz = tz;
+          bstream = streamed != 0;
+        }
       }
-    }
+  ctx->allow_stream = bstream;
   ctx->timing = timing;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -243,6 +269,9 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "graph_active")) *value = ctx->graph_active ? 1 : 0;
   else if (!std::strcmp(key, "block_jacobi")) *value = ctx->block_jacobi ? 1 : 0;
   else if (!std::strcmp(key, "fused_sweep")) *value = ctx->fuse_sweep ? 1 : 0;
+  else if (!std::strcmp(key, "sweep_stream")) *value = ctx->allow_stream ? 1 : 0;
+  else if (!std::strcmp(key, "sweep_stream_stages")) *value = ctx->stream_ns;
+  else if (!std::strcmp(key, "sweep_stream_active")) *value = streamUsable(ctx) ? 1 : 0;
   else if (!std::strcmp(key, "sweep_streams")) *value = ctx->sweep_streams;
   else if (!std::strcmp(key, "scattering_block")) *value = ctx->allow_blk_sc ? 1 : 0;
   else if (!std::strcmp(key, "scattering_block_active")) *value = blockScatterActive(ctx) ? 1 : 0;

@@ -102,6 +102,12 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool
     a.vol = ctx->vol_d;
     a.vol_uniform = ctx->vol_uniform;
   }
+  // the streamed FP32 kernel where it applies
+  const bool stream = sizeof(T) == 4 && !fused_rhs && !fused_lt && streamUsable(ctx);
+  if (stream) {
+    a.stream_ns = ctx->stream_ns;
+    a.err = ctx->err_d;
+  }
   FamScope fs(ctx, "sweep");
   // parts of the wave's subdomain list, one per stream
   const int np = std::max(1, std::min(ctx->sweep_streams, nwave));
@@ -123,6 +129,14 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool
     if (nt == 0) continue;
     for (int i = 0; i < np; ++i) {
       part[i].tile_off = ctx->tile_off[s];
+      if constexpr (sizeof(T) == 4) {
+        if (stream) {
+          if (!launch_sweep_step_stream(part[i], nt, pn[i], streamOf(i)))
+            return fail(ctx, KGB_ERR_CUDA, "cuTensorMapEncodeTiled failed for the streamed sweep");
+          CKN(1);
+          continue;
+        }
+      }
       launch_sweep_step<T>(part[i], nt, pn[i], streamOf(i));
       CKN(1);
     }
@@ -138,6 +152,13 @@ int sweepWaveAny(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, b
                  int *rowexp, bool fused_lt) {
   return ctx->prec == KGB_FP64 ? sweepWave<double>(ctx, wave_dev, nwave, fused_pop, fused_rhs, rowexp, false)
                                : sweepWave<float>(ctx, wave_dev, nwave, fused_pop, fused_rhs, nullptr, fused_lt);
+}
+
+// The streamed FP32 sweep (sweep_stream.cu): allowed, the divide form, and a
+// chain layout whose operand boxes it can copy.
+bool streamUsable(const kgb_ctx *ctx) {
+  return ctx->prec == KGB_MIXED && ctx->allow_stream && !ctx->use_recip &&
+         sweep_stream_applies(ctx->D, ctx->G, ctx->Ds, ctx->Gs, ctx->tx, ctx->ty);
 }
 
 // The fused LTimes epilogue: the mixed forward sweep with its population fused, no
