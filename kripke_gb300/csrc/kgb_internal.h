@@ -88,13 +88,13 @@ constexpr int kSweepThreads = 128;
 template <typename T>
 void launch_sweep_step(const SweepArgs<T> &a, int ntiles, int nwave, cudaStream_t s);
 
-// Streamed FP32 sweep (sweep_stream.cu): each block's rhs and sigt of a whole
-// k-slice of its tile arrive in shared memory by one TMA copy each, several
-// slices ahead.  It applies to the divide form (no reciprocal tables, fused
-// prologue or epilogue) when a block's 128 chains are whole groups whose
+// Streamed FP32 sweep (sweep_stream.cu): each block's rhs, sigt and entering
+// faces of a whole k-slice of its tile arrive in shared memory by TMA box
+// copies, slices ahead.  It applies to the divide form (no reciprocal tables,
+// fused prologue or epilogue) when a block's 128 chains are whole groups whose
 // operand boxes meet TMA's 16-byte rules: directions per set 4, 8, 16 or 32,
-// D and G multiples of 4.  Tile footprints 4x4 and 4x2 (wider tiles measured
-// slower: their face registers cut the resident warps).
+// D and G multiples of 4.  Tile footprints 4x4 and 4x2 (8x4 needs 150+
+// registers a thread for its k faces).
 constexpr int kStreamMaxStages = 4;
 bool sweep_stream_applies(int D, int G, int Ds, int Gs, int tx, int ty);
 // launches one hyperplane step (a.stream_ns stages); false when a tensor map

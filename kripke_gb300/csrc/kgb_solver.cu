@@ -107,6 +107,7 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool
   if (stream) {
     a.stream_ns = ctx->stream_ns;
     a.err = ctx->err_d;
+    a.nsdom = ctx->dc.num();  // the plane arrays' extent
   }
   FamScope fs(ctx, "sweep");
   // parts of the wave's subdomain list, one per stream

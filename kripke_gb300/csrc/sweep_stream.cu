@@ -6,29 +6,40 @@
 // of TX x TY x tz zones on hyperplanes, one thread per (group, direction)
 // chain, upwind faces in registers inside a tile and in the plane arrays
 // between tiles.  What differs is how a k-slice's operands reach the block.
-// The per-step kernel loads each cell's rhs and sigt when it sweeps the slice,
-// so every slice starts with a memory round trip that a quarter-occupied SM
-// cannot hide (the FP32 sweep measured about a quarter of HBM bandwidth).
-// Here a block's 128 chains are whole groups (g0 .. g0+GB-1, every direction
-// of the set), so the rhs of a whole slice of its tile is one box of the
-// [nz][ny][nx][G][D] array -- {Ds directions, GB groups, TX zones, TY zones, 1}
-// -- and its sigt one box of [nz][ny][nx][G]; one thread issues both copies
-// for slice kk + ns while the block sweeps slice kk, so ns slices of operands
-// are in flight per block, whatever the occupancy.  Boxes of partial tiles
-// reach past the mesh (or start before it, in the reversed orientations) and
-// read zeros there; those cells are not swept.
+// The per-step kernel loads each cell's rhs and sigt and the slice's entering
+// faces when it sweeps the slice, so every slice starts with a memory round
+// trip that a quarter-occupied SM cannot hide (the FP32 sweep measured about a
+// quarter of HBM bandwidth), and the faces it holds in registers bound the
+// tile footprint.  Here a block's 128 chains are whole groups (g0 .. g0+GB-1,
+// every direction of the set), so everything a slice reads is a handful of
+// boxes: its rhs is one box of the [nz][ny][nx][G][D] array -- {Ds directions,
+// GB groups, TX zones, TY zones, 1} -- its sigt one box of [nz][ny][nx][G],
+// its entering i and j faces one box each of the plane arrays (TY and TX rows
+// of the block's 128 chains), and the tile's entering k faces one box, loaded
+// once.  One thread issues a slice's copies ns slices ahead of the block, so
+// operands are in flight whatever the occupancy, and the entering faces need no
+// registers until they are used, which lets a 4x4 footprint keep five blocks
+// per SM.  Boxes of partial tiles reach past the mesh (or start before it, in
+// the reversed orientations): zeros or other tiles' rows land in shared memory
+// there, and those cells are not swept.
 //
 // Per cell the arithmetic is the per-step kernel's, written as the same
 // expressions (the reference's association, the same contractions), and the
 // fused population partial sums the cells in the same order, so psi, the
 // planes and the partials are bit for bit those of sweep.cu at the same tiles.
 //
-// Synchronisation: stage s of ns holds slices s, s+ns, ...; the copy of a slice
-// completes mbarrier full[s] (one arrival with the byte count); after a slice
-// the block synchronises and thread 0 refills the stage it just left.  A wait
-// is bounded (0.2 s of globaltimer); one that gives up sets *a.err and the
-// block carries on with whatever the stage holds, so the launch ends and the
-// host reports KGB_ERR_TIMEOUT.
+// Synchronisation: stage s of ns holds slices s, s+ns, ...; the copies of a
+// slice complete mbarrier full[s] (one arrival with the byte count); after a
+// slice the block synchronises and thread 0 refills the stage it just left.
+// The outgoing faces are plain stores: a face row is read by TMA only in the
+// next hyperplane step's launch.  A wait is bounded (0.2 s of globaltimer);
+// one that gives up sets *a.err and the block carries on with whatever the
+// stage holds, so the launch ends and the host reports KGB_ERR_TIMEOUT.
+//
+// Measured on a 64^3-zone, 64-group, 128-direction mixed sweep (GB300): 6.3 ms
+// at 4x4x8-16 tiles against 9.9 ms for the per-step kernel's best (4x2x16);
+// L2 eviction hints (streamed operands first, faces last) measured 0.2-0.3 ms
+// slower and are not used.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -69,25 +80,48 @@ __device__ __forceinline__ bool waitStage(uint64_t *bar, uint32_t parity) {
   return true;
 }
 
-// Bytes of one stage: the rhs box, then the sigt box (128-byte aligned)
+// Bytes of one stage: the rhs box, the sigt box (padded to 128 bytes), then
+// the slice's entering i faces (TY rows of the block's 128 chains) and j faces
+// (TX rows).  The k faces of the tile have their own buffer, filled once.
 __host__ __device__ __forceinline__ uint32_t rhsBoxBytes(int tx, int ty) { return (uint32_t)(tx * ty * kSweepThreads * 4); }
 __host__ __device__ __forceinline__ uint32_t sigBoxBytes(int tx, int ty, int gb) { return (uint32_t)(tx * ty * gb * 4); }
+__host__ __device__ __forceinline__ uint32_t faceRowBytes() { return (uint32_t)(kSweepThreads * 4); }
 __host__ __device__ __forceinline__ uint32_t stageBytes(int tx, int ty, int gb) {
-  return rhsBoxBytes(tx, ty) + ((sigBoxBytes(tx, ty, gb) + 127u) & ~127u);
+  return rhsBoxBytes(tx, ty) + ((sigBoxBytes(tx, ty, gb) + 127u) & ~127u) + (uint32_t)(tx + ty) * faceRowBytes();
+}
+__host__ __device__ __forceinline__ uint32_t streamSmemBytes(int tx, int ty, int gb, int ns) {
+  return (uint32_t)ns * stageBytes(tx, ty, gb) + (uint32_t)(tx * ty) * faceRowBytes() + 128u;
+}
+
+// The five boxes: rhs [nz][ny][nx][G][D] and sigt [nz][ny][nx][G] (global zones),
+// and the plane arrays of every subdomain as rows of nchain values -- i planes
+// [nsdom*nzs*nys][nchain], j planes [nsdom*nzs*nxs][nchain], k planes
+// [nsdom*nys][nxs][nchain].
+struct StreamMaps {
+  CUtensorMap rhs, sig, ipl, jpl, kpl;
+};
+
+__device__ __forceinline__ void tmaLoad2(uint32_t dst, const CUtensorMap *m, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(m), "r"(x), "r"(y), "r"(bar)
+      : "memory");
 }
 
 template <int TX, int TY, bool POP, int MINB>
 __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const __grid_constant__ SweepArgs<float> a,
-                                                                   const __grid_constant__ CUtensorMap rmap,
-                                                                   const __grid_constant__ CUtensorMap smap) {
+                                                                   const __grid_constant__ StreamMaps maps) {
   extern __shared__ __align__(128) unsigned char sraw[];
-  __shared__ __align__(8) uint64_t full[kStreamMaxStages];
+  __shared__ __align__(8) uint64_t full[kStreamMaxStages], kbar;
   const int ns = a.stream_ns;
   const int GB = kSweepThreads / a.Ds;  // groups per block
   const uint32_t rbytes = rhsBoxBytes(TX, TY), sbytes = sigBoxBytes(TX, TY, GB);
+  const uint32_t foff = rbytes + ((sbytes + 127u) & ~127u);  // the face rows within a stage
   const uint32_t stage = stageBytes(TX, TY, GB);
   const uint32_t sbase = smemU32(sraw);
   unsigned char *const al = sraw + (((sbase + 127u) & ~127u) - sbase);
+  const float *const kfs = reinterpret_cast<const float *>(al + (size_t)ns * stage);  // the tile's k faces
 
   const int sdom = a.wave[blockIdx.z];
   const int tile = a.tile_off + blockIdx.y;
@@ -104,36 +138,54 @@ __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const
   const int lg = (int)threadIdx.x / a.Ds;  // group within the block
 
   const int ib = t.x * TX, jb = t.y * TY, kb = t.z * a.tz;
-  // the boxes start at the tile's lowest global zone in i and j
-  const int i0 = sd.io + (sid > 0 ? ib : a.nxs - ib - TX);
-  const int j0 = sd.jo + (sjd > 0 ? jb : a.nys - jb - TY);
+  // the tile's lowest zone in i and j within the zone set (boxes start there)
+  const int ilo = sid > 0 ? ib : a.nxs - ib - TX;
+  const int jlo = sjd > 0 ? jb : a.nys - jb - TY;
   const int kend = min(a.tz, a.nzs - kb);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < ns; ++s)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemU32(&full[s])), "r"(1));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemU32(&kbar)), "r"(1));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  // plane rows of this subdomain's chunks
+  const int irow0 = (int)(sd.ip / nchain), jrow0 = (int)(sd.jp / nchain), krow0 = (int)(sd.kp / ((int64_t)nchain * a.nxs));
   auto issue = [&](int kk, int s) {
     const int kq = kb + kk;
-    const int kg = sd.ko + (skd > 0 ? kq : a.nzs - 1 - kq);
+    const int k = skd > 0 ? kq : a.nzs - 1 - kq;
+    const int kg = sd.ko + k;
     const uint32_t dst = smemU32(al + (size_t)s * stage);
     const uint32_t bar = smemU32(&full[s]);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(rbytes + sbytes) : "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"(rbytes + sbytes + (uint32_t)(TX + TY) * faceRowBytes())
+                 : "memory");
     asm volatile(
         "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
         "%6}], [%7];" ::"r"(dst),
-        "l"(&rmap), "r"(sd.dlo), "r"(g0), "r"(i0), "r"(j0), "r"(kg), "r"(bar)
+        "l"(&maps.rhs), "r"(sd.dlo), "r"(g0), "r"(sd.io + ilo), "r"(sd.jo + jlo), "r"(kg), "r"(bar)
         : "memory");
     asm volatile(
         "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
         "[%6];" ::"r"(dst + rbytes),
-        "l"(&smap), "r"(g0), "r"(i0), "r"(j0), "r"(kg), "r"(bar)
+        "l"(&maps.sig), "r"(g0), "r"(sd.io + ilo), "r"(sd.jo + jlo), "r"(kg), "r"(bar)
         : "memory");
+    tmaLoad2(dst + foff, &maps.ipl, cb * kSweepThreads, irow0 + k * a.nys + jlo, bar);
+    tmaLoad2(dst + foff + TY * faceRowBytes(), &maps.jpl, cb * kSweepThreads, jrow0 + k * a.nxs + ilo, bar);
   };
-  if (threadIdx.x == 0)
+  if (threadIdx.x == 0) {
+    const uint32_t kb_ = smemU32(&kbar);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(kb_),
+                 "r"((uint32_t)(TX * TY) * faceRowBytes())
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+            "r"(smemU32(kfs)),
+        "l"(&maps.kpl), "r"(cb * kSweepThreads), "r"(ilo), "r"(krow0 + jlo), "r"(kb_)
+        : "memory");
     for (int s = 0; s < ns && s < kend; ++s) issue(s, s);
+  }
 
   F32Acc pop;
   const double wd = POP ? a.w[d] : 0.0;
@@ -141,14 +193,14 @@ __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const
   // Per-thread bases and strides, so a cell costs few integer instructions:
   // psi of this chain at zone 0 and its stride between successive cells along i
   // of the sweep; the plane arrays at this chain, their k-slab strides and this
-  // tile's row offsets within a slab; this thread's rhs and sigt entries of the
-  // box for cell (ii, jj) at cells q0 + ii*qi + jj*qj of the box.
+  // tile's row offsets within a slab; box positions of cell (ii, jj): q0 + ii*qi
+  // + jj*qj, face row iq0 + ii*qi of the j faces, jq0 + jj*qjr of the i faces.
   const int64_t GD = (int64_t)a.G * a.D;
   float *const pchain = a.psi + (int64_t)g * a.D + d;
   const int64_t istep = sid > 0 ? GD : -GD;
   const int isg = sid > 0 ? 1 : -1;
-  const int q0 = (sjd > 0 ? 0 : TY - 1) * TX + (sid > 0 ? 0 : TX - 1);
-  const int qi = sid > 0 ? 1 : -1, qj = sjd > 0 ? TX : -TX;
+  const int iq0 = sid > 0 ? 0 : TX - 1, jq0 = sjd > 0 ? 0 : TY - 1;
+  const int qi = sid > 0 ? 1 : -1, qjr = sjd > 0 ? 1 : -1;
   int jloc[TY], joff[TY], ioff[TX];
   bool iv[TX], jv[TY];
   float cxr[TX], cyr[TY];
@@ -173,53 +225,41 @@ __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const
   float *const jpc = a.jplane + sd.jp + c;  // [nzs][nxs][nchain]
   float *const kpc = a.kplane + sd.kp + c;  // [nys][nxs][nchain]
   const int64_t islab = (int64_t)a.nys * nchain, jslab = (int64_t)a.nxs * nchain;
+
+  bool ok = waitStage(&kbar, 0u);
   float bo[TX][TY];
 #pragma unroll
   for (int ii = 0; ii < TX; ++ii)
 #pragma unroll
     for (int jj = 0; jj < TY; ++jj)
-      bo[ii][jj] = (iv[ii] && jv[jj]) ? kpc[(int64_t)jloc[jj] * jslab + ioff[ii]] : 0.f;
-  // the incoming faces of a slice, loaded one slice ahead
-  float lfn[TY], frn[TX];
-  auto loadFaces = [&](int kk) {
-    const int kq = kb + kk;
-    const int k = skd > 0 ? kq : a.nzs - 1 - kq;
-    const float *ik = ipc + (int64_t)k * islab;
-    const float *jk = jpc + (int64_t)k * jslab;
-#pragma unroll
-    for (int jj = 0; jj < TY; ++jj) lfn[jj] = jv[jj] ? ik[joff[jj]] : 0.f;
-#pragma unroll
-    for (int ii = 0; ii < TX; ++ii) frn[ii] = iv[ii] ? jk[ioff[ii]] : 0.f;
-  };
-  if (kend > 0) loadFaces(0);
+      bo[ii][jj] = kfs[((jq0 + jj * qjr) * TX + iq0 + ii * qi) * kSweepThreads + threadIdx.x];
 
-  bool ok = true;
   for (int kk = 0; kk < kend; ++kk) {
     const int s = kk % ns;
     const int kq = kb + kk;
     const int k = skd > 0 ? kq : a.nzs - 1 - kq;
     const float czk = a.cz[(int64_t)d * a.nz + sd.ko + k];
-    float lfc[TY], fr[TX];
-#pragma unroll
-    for (int jj = 0; jj < TY; ++jj) lfc[jj] = lfn[jj];
-#pragma unroll
-    for (int ii = 0; ii < TX; ++ii) fr[ii] = frn[ii];
-    if (kk + 1 < kend) loadFaces(kk + 1);
     if (!waitStage(&full[s], (uint32_t)(kk / ns) & 1u)) ok = false;
-    const float *__restrict__ rs = reinterpret_cast<const float *>(al + (size_t)s * stage) + threadIdx.x;
-    const float *__restrict__ ss = reinterpret_cast<const float *>(al + (size_t)s * stage + rbytes) + lg;
+    const unsigned char *const st = al + (size_t)s * stage;
+    const float *__restrict__ rs = reinterpret_cast<const float *>(st) + threadIdx.x;
+    const float *__restrict__ ss = reinterpret_cast<const float *>(st + rbytes) + lg;
+    const float *__restrict__ ifs = reinterpret_cast<const float *>(st + foff) + threadIdx.x;
+    const float *__restrict__ jfs = reinterpret_cast<const float *>(st + foff + TY * faceRowBytes()) + threadIdx.x;
+    float fr[TX];
+#pragma unroll
+    for (int ii = 0; ii < TX; ++ii) fr[ii] = jfs[(iq0 + ii * qi) * kSweepThreads];
     float *const ik = ipc + (int64_t)k * islab;
     const int64_t zslice = (int64_t)(sd.ko + k) * a.ny;
 #pragma unroll
     for (int jj = 0; jj < TY; ++jj) {
       if (!jv[jj]) continue;
-      float lf = lfc[jj];
+      float lf = ifs[(jq0 + jj * qjr) * kSweepThreads];
       const int64_t z0 = (zslice + (sd.jo + jloc[jj])) * a.nx + sd.io + iloc0;  // zone of cell (0, jj)
       float *pc = pchain + z0 * GD;
 #pragma unroll
       for (int ii = 0; ii < TX; ++ii) {
         if (iv[ii]) {
-          const int q = q0 + ii * qi + jj * qj;
+          const int q = (jq0 + jj * qjr) * TX + iq0 + ii * qi;
           const float rv = rs[q * kSweepThreads];
           const float sv = ss[q * GB];
           // the per-step kernel's expressions (sweep.cu), so the two agree bit for bit
@@ -285,18 +325,17 @@ bool encode(CUtensorMap *m, const float *base, int rank, const cuuint64_t *dims,
 }
 
 template <int TX, int TY, bool POP, int MINB>
-void launchStreamAs(const SweepArgs<float> &a, dim3 grid, cudaStream_t s, const CUtensorMap &rm,
-                    const CUtensorMap &sm) {
-  const size_t smem = (size_t)a.stream_ns * stageBytes(TX, TY, kSweepThreads / a.Ds) + 128;
+void launchStreamAs(const SweepArgs<float> &a, dim3 grid, cudaStream_t s, const StreamMaps &m) {
+  const size_t smem = streamSmemBytes(TX, TY, kSweepThreads / a.Ds, a.stream_ns);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(sweep_stream_kernel<TX, TY, POP, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  sweep_stream_kernel<TX, TY, POP, MINB><<<grid, kSweepThreads, smem, s>>>(a, rm, sm);
+  sweep_stream_kernel<TX, TY, POP, MINB><<<grid, kSweepThreads, smem, s>>>(a, m);
 }
 
 template <int TX, int TY, int MINB>
-void launchStream(const SweepArgs<float> &a, dim3 grid, cudaStream_t s, const CUtensorMap &rm, const CUtensorMap &sm) {
-  if (a.pop) launchStreamAs<TX, TY, true, MINB>(a, grid, s, rm, sm);
-  else launchStreamAs<TX, TY, false, MINB>(a, grid, s, rm, sm);
+void launchStream(const SweepArgs<float> &a, dim3 grid, cudaStream_t s, const StreamMaps &m) {
+  if (a.pop) launchStreamAs<TX, TY, true, MINB>(a, grid, s, m);
+  else launchStreamAs<TX, TY, false, MINB>(a, grid, s, m);
 }
 
 }  // namespace
@@ -310,7 +349,8 @@ bool sweep_stream_applies(int D, int G, int Ds, int Gs, int tx, int ty) {
 
 bool launch_sweep_step_stream(const SweepArgs<float> &a, int ntiles, int nwave, cudaStream_t s) {
   const int gb = kSweepThreads / a.Ds;
-  CUtensorMap rm, sm;
+  const cuuint64_t nch = (cuuint64_t)a.Ds * a.Gs, ns = (cuuint64_t)a.nsdom;
+  StreamMaps m;
   const cuuint64_t rdims[5] = {(cuuint64_t)a.D, (cuuint64_t)a.G, (cuuint64_t)a.nx, (cuuint64_t)a.ny, (cuuint64_t)a.nz};
   const cuuint64_t rstr[4] = {(cuuint64_t)a.D * 4, (cuuint64_t)a.G * a.D * 4, (cuuint64_t)a.nx * a.G * a.D * 4,
                               (cuuint64_t)a.ny * a.nx * a.G * a.D * 4};
@@ -318,13 +358,19 @@ bool launch_sweep_step_stream(const SweepArgs<float> &a, int ntiles, int nwave, 
   const cuuint64_t sdims[4] = {(cuuint64_t)a.G, (cuuint64_t)a.nx, (cuuint64_t)a.ny, (cuuint64_t)a.nz};
   const cuuint64_t sstr[3] = {(cuuint64_t)a.G * 4, (cuuint64_t)a.nx * a.G * 4, (cuuint64_t)a.ny * a.nx * a.G * 4};
   const cuuint32_t sbox[4] = {(cuuint32_t)gb, (cuuint32_t)a.tx, (cuuint32_t)a.ty, 1};
-  if (!encode(&rm, a.rhs, 5, rdims, rstr, rbox) || !encode(&sm, a.sigt, 4, sdims, sstr, sbox)) return false;
-  const int nchain = a.Ds * a.Gs;
-  dim3 grid(nchain / kSweepThreads, ntiles, nwave);
-  // 4x2 at seven blocks per SM (72 registers, a few cold values spilled): 7.44
-  // against 8.04 ms per 64^3 x 64-group x 128-direction sweep without the bound
-  if (a.tx == 4 && a.ty == 4) launchStream<4, 4, 1>(a, grid, s, rm, sm);
-  else launchStream<4, 2, 7>(a, grid, s, rm, sm);
+  const cuuint64_t idims[2] = {nch, ns * a.nzs * a.nys}, jdims[2] = {nch, ns * a.nzs * a.nxs};
+  const cuuint64_t kdims[3] = {nch, (cuuint64_t)a.nxs, ns * a.nys};
+  const cuuint64_t pstr[2] = {nch * 4, nch * 4 * a.nxs};
+  const cuuint32_t ibox[2] = {kSweepThreads, (cuuint32_t)a.ty}, jbox[2] = {kSweepThreads, (cuuint32_t)a.tx};
+  const cuuint32_t kbox[3] = {kSweepThreads, (cuuint32_t)a.tx, (cuuint32_t)a.ty};
+  if (!encode(&m.rhs, a.rhs, 5, rdims, rstr, rbox) || !encode(&m.sig, a.sigt, 4, sdims, sstr, sbox) ||
+      !encode(&m.ipl, a.iplane, 2, idims, pstr, ibox) || !encode(&m.jpl, a.jplane, 2, jdims, pstr, jbox) ||
+      !encode(&m.kpl, a.kplane, 3, kdims, pstr, kbox))
+    return false;
+  dim3 grid((unsigned)(nch / kSweepThreads), ntiles, nwave);
+  // occupancy bounds: 4x4 at five blocks per SM (92 registers), 4x2 at seven (72)
+  if (a.tx == 4 && a.ty == 4) launchStream<4, 4, 5>(a, grid, s, m);
+  else launchStream<4, 2, 7>(a, grid, s, m);
   return true;
 }
 
