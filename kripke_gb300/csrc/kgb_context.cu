@@ -765,7 +765,11 @@ int buildTiles(kgb_ctx *ctx) {
   int rc = dmalloc(ctx, &ctx->tiles_d, tiles.size());
   if (rc) return rc;
   const int64_t nchain = (int64_t)ctx->Gs * ctx->Ds;
-  const int64_t nslots = (int64_t)tiles.size() * ctx->dc.num() * ((nchain + kSweepThreads - 1) / kSweepThreads);
+  // population partials: one per (tile, subdomain, chain block); the streamed FP32
+  // sweep's blocks may hold fewer chains (whole groups) than the per-step kernel's
+  const int sbt = ctx->prec == KGB_FP64 ? 0 : stream_block_chains(ctx->Ds, ctx->Gs);
+  const int64_t ncb = std::max<int64_t>((nchain + kSweepThreads - 1) / kSweepThreads, sbt > 0 ? nchain / sbt : 0);
+  const int64_t nslots = (int64_t)tiles.size() * ctx->dc.num() * ncb;
   if (ctx->pop_slots) cudaFree(ctx->pop_slots);
   ctx->pop_slots = nullptr;
   if ((rc = dmalloc(ctx, &ctx->pop_slots, nslots))) return rc;

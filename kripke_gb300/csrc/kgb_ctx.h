@@ -202,6 +202,7 @@ struct kgb_ctx {
   // fused population partials, one per (tile, subdomain, chain block)
   double *pop_slots = nullptr;
   int64_t npop_slots = 0;
+  int64_t npop_used = 0;  // partials the last sweep wrote (its kernel's chain blocks)
   double vol_uniform = 0.0;
   double pop_scale = 0.0;  // w(d) / ell(0,d) when L's moment-0 row is proportional to w, else 0
 

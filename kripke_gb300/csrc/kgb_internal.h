@@ -92,10 +92,13 @@ void launch_sweep_step(const SweepArgs<T> &a, int ntiles, int nwave, cudaStream_
 // faces of a whole k-slice of its tile arrive in shared memory by TMA box
 // copies, slices ahead.  It applies to the divide form (no reciprocal tables,
 // fused prologue or epilogue) when a block's 128 chains are whole groups whose
-// operand boxes meet TMA's 16-byte rules: directions per set 4, 8, 16 or 32,
-// D and G multiples of 4.  Tile footprints 4x4 and 4x2 (8x4 needs 150+
-// registers a thread for its k faces).
+// operand boxes meet TMA's 16-byte rules: a multiple of 4 directions per set
+// (at most 32), blocks of GB whole groups (GB a multiple of 4 dividing the
+// group set, GB x Ds a whole number of warps, at most 128 chains), D and G
+// multiples of 4.  Tile footprints 4x4 and 4x2 (8x4 needs 150+ registers a
+// thread for its k faces).
 constexpr int kStreamMaxStages = 4;
+int stream_block_chains(int Ds, int Gs);  // chains per block, 0: not streamable
 bool sweep_stream_applies(int D, int G, int Ds, int Gs, int tx, int ty);
 // launches one hyperplane step (a.stream_ns stages); false when a tensor map
 // cannot be encoded (nothing launched)

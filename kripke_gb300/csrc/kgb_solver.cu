@@ -109,6 +109,11 @@ int sweepWave(kgb_ctx *ctx, const int *wave_dev, int nwave, bool fused_pop, bool
     a.err = ctx->err_d;
     a.nsdom = ctx->dc.num();  // the plane arrays' extent
   }
+  {
+    const int64_t nchain = (int64_t)ctx->Gs * ctx->Ds;
+    const int64_t ncb = stream ? nchain / stream_block_chains(ctx->Ds, ctx->Gs) : (nchain + kSweepThreads - 1) / kSweepThreads;
+    ctx->npop_used = (int64_t)ctx->tile_off.back() * ctx->dc.num() * ncb;
+  }
   FamScope fs(ctx, "sweep");
   // parts of the wave's subdomain list, one per stream
   const int np = std::max(1, std::min(ctx->sweep_streams, nwave));
@@ -541,7 +546,7 @@ int iterateDevice(kgb_ctx *ctx, double q, double *part_slot, double *prev_slot, 
   if (ctx->fuse_active) ctx->rhs_stale = true;
   if (part_slot) {
     FamScope fs(ctx, "population");
-    launch_sum_partials(ctx->pop_slots, ctx->npop_slots, part_slot, ctx->stream);
+    launch_sum_partials(ctx->pop_slots, ctx->npop_used, part_slot, ctx->stream);
     CKN(1);
   }
   return KGB_OK;

@@ -42,5 +42,20 @@ __device__ __forceinline__ double blockSum128(double v) {
   return r;
 }
 
+// The same for a block of any whole number of warps up to kSweepThreads (the
+// streamed sweep's GB x Ds chains); with 128 threads it sums as blockSum128.
+__device__ __forceinline__ double blockSumWarps(double v) {
+  __shared__ double part[kSweepThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += part[i];
+  __syncthreads();
+  return r;
+}
+
 }  // namespace
 }  // namespace kgb

@@ -83,14 +83,15 @@ __device__ __forceinline__ bool waitStage(uint64_t *bar, uint32_t parity) {
 // Bytes of one stage: the rhs box, the sigt box (padded to 128 bytes), then
 // the slice's entering i faces (TY rows of the block's 128 chains) and j faces
 // (TX rows).  The k faces of the tile have their own buffer, filled once.
-__host__ __device__ __forceinline__ uint32_t rhsBoxBytes(int tx, int ty) { return (uint32_t)(tx * ty * kSweepThreads * 4); }
+// bt = chains per block (gb groups x Ds directions).
+__host__ __device__ __forceinline__ uint32_t rhsBoxBytes(int tx, int ty, int bt) { return (uint32_t)(tx * ty * bt * 4); }
 __host__ __device__ __forceinline__ uint32_t sigBoxBytes(int tx, int ty, int gb) { return (uint32_t)(tx * ty * gb * 4); }
-__host__ __device__ __forceinline__ uint32_t faceRowBytes() { return (uint32_t)(kSweepThreads * 4); }
-__host__ __device__ __forceinline__ uint32_t stageBytes(int tx, int ty, int gb) {
-  return rhsBoxBytes(tx, ty) + ((sigBoxBytes(tx, ty, gb) + 127u) & ~127u) + (uint32_t)(tx + ty) * faceRowBytes();
+__host__ __device__ __forceinline__ uint32_t faceRowBytes(int bt) { return (uint32_t)(bt * 4); }
+__host__ __device__ __forceinline__ uint32_t stageBytes(int tx, int ty, int gb, int bt) {
+  return rhsBoxBytes(tx, ty, bt) + ((sigBoxBytes(tx, ty, gb) + 127u) & ~127u) + (uint32_t)(tx + ty) * faceRowBytes(bt);
 }
-__host__ __device__ __forceinline__ uint32_t streamSmemBytes(int tx, int ty, int gb, int ns) {
-  return (uint32_t)ns * stageBytes(tx, ty, gb) + (uint32_t)(tx * ty) * faceRowBytes() + 128u;
+__host__ __device__ __forceinline__ uint32_t streamSmemBytes(int tx, int ty, int gb, int bt, int ns) {
+  return (uint32_t)ns * stageBytes(tx, ty, gb, bt) + (uint32_t)(tx * ty) * faceRowBytes(bt) + 128u;
 }
 
 // The five boxes: rhs [nz][ny][nx][G][D] and sigt [nz][ny][nx][G] (global zones),
@@ -115,10 +116,12 @@ __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const
   extern __shared__ __align__(128) unsigned char sraw[];
   __shared__ __align__(8) uint64_t full[kStreamMaxStages], kbar;
   const int ns = a.stream_ns;
-  const int GB = kSweepThreads / a.Ds;  // groups per block
-  const uint32_t rbytes = rhsBoxBytes(TX, TY), sbytes = sigBoxBytes(TX, TY, GB);
+  const int BT = blockDim.x;            // chains per block: GB whole groups
+  const int GB = BT / a.Ds;             // groups per block
+  const uint32_t rbytes = rhsBoxBytes(TX, TY, BT), sbytes = sigBoxBytes(TX, TY, GB);
+  const uint32_t frow = faceRowBytes(BT);
   const uint32_t foff = rbytes + ((sbytes + 127u) & ~127u);  // the face rows within a stage
-  const uint32_t stage = stageBytes(TX, TY, GB);
+  const uint32_t stage = stageBytes(TX, TY, GB, BT);
   const uint32_t sbase = smemU32(sraw);
   unsigned char *const al = sraw + (((sbase + 127u) & ~127u) - sbase);
   const float *const kfs = reinterpret_cast<const float *>(al + (size_t)ns * stage);  // the tile's k faces
@@ -130,7 +133,7 @@ __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const
   const int sid = a.flip ? -sd.id : sd.id, sjd = a.flip ? -sd.jd : sd.jd, skd = a.flip ? -sd.kd : sd.kd;
   const int4 t = a.tiles[tile];
   const int nchain = a.Ds * a.Gs;
-  const int c = cb * kSweepThreads + threadIdx.x;  // every block is full: Gs is a multiple of GB
+  const int c = cb * BT + threadIdx.x;  // every block is full: Gs is a multiple of GB
   const int gl = c / a.Ds;
   const int g = sd.glo + gl;
   const int d = sd.dlo + (c - gl * a.Ds);
@@ -159,7 +162,7 @@ __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const
     const uint32_t dst = smemU32(al + (size_t)s * stage);
     const uint32_t bar = smemU32(&full[s]);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
-                 "r"(rbytes + sbytes + (uint32_t)(TX + TY) * faceRowBytes())
+                 "r"(rbytes + sbytes + (uint32_t)(TX + TY) * frow)
                  : "memory");
     asm volatile(
         "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
@@ -171,18 +174,18 @@ __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const
         "[%6];" ::"r"(dst + rbytes),
         "l"(&maps.sig), "r"(g0), "r"(sd.io + ilo), "r"(sd.jo + jlo), "r"(kg), "r"(bar)
         : "memory");
-    tmaLoad2(dst + foff, &maps.ipl, cb * kSweepThreads, irow0 + k * a.nys + jlo, bar);
-    tmaLoad2(dst + foff + TY * faceRowBytes(), &maps.jpl, cb * kSweepThreads, jrow0 + k * a.nxs + ilo, bar);
+    tmaLoad2(dst + foff, &maps.ipl, cb * BT, irow0 + k * a.nys + jlo, bar);
+    tmaLoad2(dst + foff + TY * frow, &maps.jpl, cb * BT, jrow0 + k * a.nxs + ilo, bar);
   };
   if (threadIdx.x == 0) {
     const uint32_t kb_ = smemU32(&kbar);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(kb_),
-                 "r"((uint32_t)(TX * TY) * faceRowBytes())
+                 "r"((uint32_t)(TX * TY) * frow)
                  : "memory");
     asm volatile(
         "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
             "r"(smemU32(kfs)),
-        "l"(&maps.kpl), "r"(cb * kSweepThreads), "r"(ilo), "r"(krow0 + jlo), "r"(kb_)
+        "l"(&maps.kpl), "r"(cb * BT), "r"(ilo), "r"(krow0 + jlo), "r"(kb_)
         : "memory");
     for (int s = 0; s < ns && s < kend; ++s) issue(s, s);
   }
@@ -232,7 +235,7 @@ __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const
   for (int ii = 0; ii < TX; ++ii)
 #pragma unroll
     for (int jj = 0; jj < TY; ++jj)
-      bo[ii][jj] = kfs[((jq0 + jj * qjr) * TX + iq0 + ii * qi) * kSweepThreads + threadIdx.x];
+      bo[ii][jj] = kfs[((jq0 + jj * qjr) * TX + iq0 + ii * qi) * BT + threadIdx.x];
 
   for (int kk = 0; kk < kend; ++kk) {
     const int s = kk % ns;
@@ -244,23 +247,23 @@ __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const
     const float *__restrict__ rs = reinterpret_cast<const float *>(st) + threadIdx.x;
     const float *__restrict__ ss = reinterpret_cast<const float *>(st + rbytes) + lg;
     const float *__restrict__ ifs = reinterpret_cast<const float *>(st + foff) + threadIdx.x;
-    const float *__restrict__ jfs = reinterpret_cast<const float *>(st + foff + TY * faceRowBytes()) + threadIdx.x;
+    const float *__restrict__ jfs = reinterpret_cast<const float *>(st + foff + TY * frow) + threadIdx.x;
     float fr[TX];
 #pragma unroll
-    for (int ii = 0; ii < TX; ++ii) fr[ii] = jfs[(iq0 + ii * qi) * kSweepThreads];
+    for (int ii = 0; ii < TX; ++ii) fr[ii] = jfs[(iq0 + ii * qi) * BT];
     float *const ik = ipc + (int64_t)k * islab;
     const int64_t zslice = (int64_t)(sd.ko + k) * a.ny;
 #pragma unroll
     for (int jj = 0; jj < TY; ++jj) {
       if (!jv[jj]) continue;
-      float lf = ifs[(jq0 + jj * qjr) * kSweepThreads];
+      float lf = ifs[(jq0 + jj * qjr) * BT];
       const int64_t z0 = (zslice + (sd.jo + jloc[jj])) * a.nx + sd.io + iloc0;  // zone of cell (0, jj)
       float *pc = pchain + z0 * GD;
 #pragma unroll
       for (int ii = 0; ii < TX; ++ii) {
         if (iv[ii]) {
           const int q = (jq0 + jj * qjr) * TX + iq0 + ii * qi;
-          const float rv = rs[q * kSweepThreads];
+          const float rv = rs[q * BT];
           const float sv = ss[q * GB];
           // the per-step kernel's expressions (sweep.cu), so the two agree bit for bit
           const float num = rv + lf * cxr[ii] + fr[ii] * cyr[jj] + bo[ii][jj] * czk;
@@ -295,7 +298,7 @@ __global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const
   if (POP) {
     double v = pop.value() * wd;
     if (a.vol_uniform > 0.0) v *= a.vol_uniform;
-    const double b = blockSum128(v);
+    const double b = blockSumWarps(v);
     if (threadIdx.x == 0) a.pop[((int64_t)tile * a.nsdom + sdom) * gridDim.x + cb] = b;
   }
 }
@@ -326,10 +329,11 @@ bool encode(CUtensorMap *m, const float *base, int rank, const cuuint64_t *dims,
 
 template <int TX, int TY, bool POP, int MINB>
 void launchStreamAs(const SweepArgs<float> &a, dim3 grid, cudaStream_t s, const StreamMaps &m) {
-  const size_t smem = streamSmemBytes(TX, TY, kSweepThreads / a.Ds, a.stream_ns);
+  const int bt = stream_block_chains(a.Ds, a.Gs);
+  const size_t smem = streamSmemBytes(TX, TY, bt / a.Ds, bt, a.stream_ns);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(sweep_stream_kernel<TX, TY, POP, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  sweep_stream_kernel<TX, TY, POP, MINB><<<grid, kSweepThreads, smem, s>>>(a, m);
+  sweep_stream_kernel<TX, TY, POP, MINB><<<grid, bt, smem, s>>>(a, m);
 }
 
 template <int TX, int TY, int MINB>
@@ -340,15 +344,23 @@ void launchStream(const SweepArgs<float> &a, dim3 grid, cudaStream_t s, const St
 
 }  // namespace
 
+int stream_block_chains(int Ds, int Gs) {
+  // Whole groups per block, GB a multiple of 4 (16-byte sigt boxes) dividing the
+  // group set, at most 128 chains and a whole number of warps: 4, 8, 16 or 32
+  // directions per set fill 128 chains, 12 and 24 fill 96.
+  if (Ds < 4 || Ds % 4 != 0 || Ds > kSweepThreads / 4) return 0;
+  for (int gb = kSweepThreads / Ds / 4 * 4; gb >= 4; gb -= 4)
+    if (Gs % gb == 0 && (gb * Ds) % 32 == 0) return gb * Ds;
+  return 0;
+}
+
 bool sweep_stream_applies(int D, int G, int Ds, int Gs, int tx, int ty) {
   const bool shape = tx == 4 && (ty == 4 || ty == 2);
-  if (!shape || Ds < 4 || Ds > 32 || kSweepThreads % Ds != 0) return false;
-  const int gb = kSweepThreads / Ds;  // 4 .. 32 groups per block: 16-byte sigt boxes
-  return D % 4 == 0 && G % 4 == 0 && Gs % gb == 0;
+  return shape && D % 4 == 0 && G % 4 == 0 && stream_block_chains(Ds, Gs) > 0;
 }
 
 bool launch_sweep_step_stream(const SweepArgs<float> &a, int ntiles, int nwave, cudaStream_t s) {
-  const int gb = kSweepThreads / a.Ds;
+  const int bt = stream_block_chains(a.Ds, a.Gs), gb = bt / a.Ds;
   const cuuint64_t nch = (cuuint64_t)a.Ds * a.Gs, ns = (cuuint64_t)a.nsdom;
   StreamMaps m;
   const cuuint64_t rdims[5] = {(cuuint64_t)a.D, (cuuint64_t)a.G, (cuuint64_t)a.nx, (cuuint64_t)a.ny, (cuuint64_t)a.nz};
@@ -361,13 +373,13 @@ bool launch_sweep_step_stream(const SweepArgs<float> &a, int ntiles, int nwave, 
   const cuuint64_t idims[2] = {nch, ns * a.nzs * a.nys}, jdims[2] = {nch, ns * a.nzs * a.nxs};
   const cuuint64_t kdims[3] = {nch, (cuuint64_t)a.nxs, ns * a.nys};
   const cuuint64_t pstr[2] = {nch * 4, nch * 4 * a.nxs};
-  const cuuint32_t ibox[2] = {kSweepThreads, (cuuint32_t)a.ty}, jbox[2] = {kSweepThreads, (cuuint32_t)a.tx};
-  const cuuint32_t kbox[3] = {kSweepThreads, (cuuint32_t)a.tx, (cuuint32_t)a.ty};
+  const cuuint32_t ibox[2] = {(cuuint32_t)bt, (cuuint32_t)a.ty}, jbox[2] = {(cuuint32_t)bt, (cuuint32_t)a.tx};
+  const cuuint32_t kbox[3] = {(cuuint32_t)bt, (cuuint32_t)a.tx, (cuuint32_t)a.ty};
   if (!encode(&m.rhs, a.rhs, 5, rdims, rstr, rbox) || !encode(&m.sig, a.sigt, 4, sdims, sstr, sbox) ||
       !encode(&m.ipl, a.iplane, 2, idims, pstr, ibox) || !encode(&m.jpl, a.jplane, 2, jdims, pstr, jbox) ||
       !encode(&m.kpl, a.kplane, 3, kdims, pstr, kbox))
     return false;
-  dim3 grid((unsigned)(nch / kSweepThreads), ntiles, nwave);
+  dim3 grid((unsigned)(nch / bt), ntiles, nwave);
   // occupancy bounds: 4x4 at five blocks per SM (92 registers), 4x2 at seven (72)
   if (a.tx == 4 && a.ty == 4) launchStream<4, 4, 5>(a, grid, s, m);
   else launchStream<4, 2, 7>(a, grid, s, m);

@@ -4,9 +4,10 @@ Both kernels evaluate the same diamond-difference recurrence (Kernel/SweepSubdom
 with the same expressions, and the running faces cross tile boundaries through the plane arrays
 unrounded, so psi, the planes and every iterate are bit for bit the same whatever the kernel and
 the tile shape; the fused population partials are summed in the same order at the same tiles.
-Shapes: 128 Gauss-Legendre directions (16 per octant set, 8 groups per 128-chain block) and
-direction sets of 8 (16 groups per block), partial tiles at the downwind ends, zone sets, group
-sets, a perturbed (non-uniform) mesh, the reversed (adjoint) orientation, and 1 to 4 stages.
+Shapes: 128 Gauss-Legendre directions (16 per octant set, 8 groups per 128-chain block),
+direction sets of 8 (16 groups per block), 12 (8 groups, 96-chain blocks) and 24 (4 groups, 96
+chains), partial tiles at the downwind ends, zone sets, group sets, a perturbed (non-uniform)
+mesh, the reversed (adjoint) orientation, and 1 to 4 stages.
 """
 import numpy as np
 import pytest
@@ -29,7 +30,8 @@ def sweep_with(ctx, rhs, xy, tz, stream, stages=2):
     return [ctx.download(n) for n in ("psi", "i_plane", "j_plane", "k_plane")]
 
 
-@pytest.mark.parametrize("kw", [dict(), dict(zones=(10, 7, 10), zsets=(2, 1, 2)), dict(gset=2), dict(dset=16), dict(perturb=1)])
+@pytest.mark.parametrize("kw", [dict(), dict(zones=(10, 7, 10), zsets=(2, 1, 2)), dict(gset=2), dict(dset=16),
+                                dict(perturb=1), dict(quad=(8, 12)), dict(quad=(8, 24), groups=12)])
 def test_streamed_sweep_bitwise(oracle, kgb, kw):
     p, ctx = pair(oracle, kgb, precision=1, **dict(BASE, **kw))
     rhs = np.random.default_rng(11).uniform(0.0, 2.0, ctx.field_bytes("rhs") // 8)
@@ -86,8 +88,8 @@ def test_stream_applies_to_the_mixed_form_only(oracle, kgb):
     p.sweep_solver(); ctx.sweep_solver()
     check(ctx.download("psi"), p.get("psi"), 1e-12)
     ctx.close()
-    # 12 directions per set (96 directions): no whole-group 128-chain blocks
-    p, ctx = pair(oracle, kgb, precision=1, **dict(BASE, quad=(8, 12)))
+    # 6 directions per set (48 directions): no 16-byte direction runs
+    p, ctx = pair(oracle, kgb, precision=1, **dict(BASE, quad=(4, 12)))
     ctx.set_option("sweep_tile_xy", 42)
     assert ctx.get_option("sweep_stream_active") == 0
     ctx.upload("rhs", rhs[:ctx.field_bytes("rhs") // 8])
