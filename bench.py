@@ -527,6 +527,7 @@ def batch_report(local, problems=BATCH_PROBLEMS, niter=10):
         out[name] = {"value": U / t_batch, "unit": "unknowns/s", "unknowns": U, "ms_per_iteration": t_batch * 1e3,
                      "graph_active": b.get_option("graph_active"), "kernels_per_iteration": kernels,
                      "per_problem_kernels": b.get_option("per_problem_kernels"),
+                     "per_problem_sweeps": b.get_option("per_problem_sweeps"),
                      "autotuned": tune, "phase_ms": phases,
                      "one_by_one": {"value": U / t_seq, "ms_per_iteration": t_seq * 1e3,
                                     "how": "each problem's own context, default options, solved in turn"},

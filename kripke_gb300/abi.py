@@ -485,7 +485,8 @@ class Batch:
         ms = ctypes.c_double()
         self._check(self.lib.kgb_batch_autotune(self.h, ctypes.byref(ms)), "kgb_batch_autotune")
         return {"iteration_ms": ms.value, "sweep_tile_xy": self.get_option("sweep_tile_xy"),
-                "sweep_tile_z": self.get_option("sweep_tile_z"), "rows_per_item": self.get_option("rows_per_item")}
+                "sweep_tile_z": self.get_option("sweep_tile_z"), "rows_per_item": self.get_option("rows_per_item"),
+                "per_problem_sweeps": self.get_option("per_problem_sweeps")}
 
     def solve(self, niter, source_strength=1.0):
         """Particle counts [niter][problems]."""

@@ -46,6 +46,9 @@ struct kgb_batch {
   int64_t barrier_wait_ns = 2000000000;
   bool use_graph = true;
   int own_mode = -1;  // 1: each problem's own LTimes/scattering/LPlusTimes kernels; 0: batched SIMT; -1: by precision
+  // 1: each problem's own sweeps (per-step launches, the streamed FP32 sweep where it
+  // applies) on parallel branches; 0: the persistent launch over all problems; -1: by precision
+  int sweep_mode = -1;
   // the problems' psi row-exponent records (FP64, views[i].psi_exp) hold for their current psi:
   // set by a solve's reset and by every batched sweep, which records them; cleared by a new plan
   bool rec_ok = false;
@@ -176,6 +179,7 @@ void groupRows(const std::vector<BatchRows> &rows, KeyFn key, std::vector<BatchR
 }
 
 bool perProblem(const kgb_batch *b) { return b->own_mode < 0 ? b->prec == KGB_FP64 : b->own_mode == 1; }
+bool ownSweeps(const kgb_batch *b) { return b->sweep_mode < 0 ? b->prec != KGB_FP64 : b->sweep_mode == 1; }
 
 template <typename T>
 int planT(kgb_batch *b) {
@@ -183,6 +187,11 @@ int planT(kgb_batch *b) {
   const int n = (int)b->inst.size();
   if (n == 0) return fail(b, KGB_ERR_STATE, "the batch has no problems");
   b->views.assign(n, InstanceView{});
+  if (ownSweeps(b))  // the problems sweep with the batch's tiles (before their views: new tiles, new generation)
+    for (int i = 0; i < n; ++i) {
+      const int rc = instance_tiles(b->inst[i], b->tx, b->ty, b->tz);
+      if (rc) return fail(b, rc, "problem " + std::to_string(i) + ": " + kgb_last_error(b->inst[i]));
+    }
   for (int i = 0; i < n; ++i) {
     int rc = instance_view(b->inst[i], &b->views[i]);
     if (rc) return fail(b, rc, "problem " + std::to_string(i) + ": " + kgb_last_error(b->inst[i]));
@@ -323,8 +332,12 @@ int planT(kgb_batch *b) {
   b->sweep_grid = batch_sweep_grid<T>(b->tx, b->ty, b->nsm);
   if (b->sweep_grid <= 0) return fail(b, KGB_ERR_CUDA, "the persistent sweep has no resident blocks");
   b->row_grid = b->nsm * 16;
-  b->kernels_per_iter = perProblem(b) ? 3 * (int64_t)n + 2
-                                      : (int64_t)b->lt_cls.size() + b->lp_cls.size() + b->sc_cls.size() + 2;
+  b->kernels_per_iter = perProblem(b) ? 3 * (int64_t)n : (int64_t)b->lt_cls.size() + b->lp_cls.size() + b->sc_cls.size();
+  if (ownSweeps(b)) {
+    for (int i = 0; i < n; ++i) b->kernels_per_iter += instance_sweep_launches(b->inst[i]);
+  } else {
+    b->kernels_per_iter += 2;  // the persistent sweep and the population sums
+  }
   BCK(cudaStreamSynchronize(b->stream));
   b->planned = true;
   return KGB_OK;
@@ -351,12 +364,15 @@ int ensurePlan(kgb_batch *b) {
 // Each problem's own kernels for one phase (the tensor-core digit products in
 // FP64), spread over kForks streams forked from and joined back to the batch
 // stream -- parallel branches of the captured graph.
-int forkPhase(kgb_batch *b, InstanceOp op) {
+// pop: the batch's population slots of this iteration (Sweep: each problem's count
+// of the new psi goes to pop[i]; FP64 problems record psi's row exponents).
+int forkPhase(kgb_batch *b, InstanceOp op, double *pop = nullptr) {
   BCK(cudaEventRecord(b->fork_ev, b->stream));
   for (int k = 0; k < kgb_batch::kForks; ++k) BCK(cudaStreamWaitEvent(b->aux[k], b->fork_ev, 0));
   for (size_t i = 0; i < b->inst.size(); ++i) {
-    const int *rx = op == InstanceOp::LTimes && b->rec_ok ? b->views[i].psi_exp : nullptr;
-    const int rc = instance_op(b->inst[i], op, b->q, b->aux[i % kgb_batch::kForks], rx);
+    const bool sweep = op == InstanceOp::Sweep;
+    const int *rx = (op == InstanceOp::LTimes && b->rec_ok) || sweep ? b->views[i].psi_exp : nullptr;
+    const int rc = instance_op(b->inst[i], op, b->q, b->aux[i % kgb_batch::kForks], rx, sweep ? pop + i : nullptr);
     if (rc) return fail(b, rc, "problem " + std::to_string(i) + ": " + kgb_last_error(b->inst[i]));
   }
   for (int k = 0; k < kgb_batch::kForks; ++k) {
@@ -399,14 +415,21 @@ int enqueueIteration(kgb_batch *b, double *pop_out, cudaEvent_t *ev = nullptr) {
                               std::min(c.n, b->row_grid), b->stream);
   }
   BCK(cudaGetLastError());
-  BCK(cudaMemsetAsync(b->bar, 0, 2 * sizeof(unsigned int), b->stream));
   if (ev) BCK(cudaEventRecord(ev[3], b->stream));
-  BatchSweepPlan p{b->sweep_items, b->step_off, b->nsteps, b->zero,
-                   b->nzero,          b->bar,      b->err_d, (unsigned long long)b->barrier_wait_ns};
-  BCK(launch_batch_sweep<T>((const SweepArgs<T> *)b->sweep_args, p, b->tx, b->ty, b->sweep_grid, b->stream));
-  b->rec_ok = true;  // the sweep recorded psi's row exponents (FP64 problems with a record)
-  if (ev) BCK(cudaEventRecord(ev[4], b->stream));
-  launch_batch_pop_finish(b->slot_ptrs, b->slot_n, (int)b->inst.size(), pop_out, b->stream);
+  if (ownSweeps(b)) {
+    // each problem's own sweep and population sum on parallel branches
+    if ((rc = forkPhase(b, InstanceOp::Sweep, pop_out))) return rc;
+    b->rec_ok = true;
+    if (ev) BCK(cudaEventRecord(ev[4], b->stream));
+  } else {
+    BCK(cudaMemsetAsync(b->bar, 0, 2 * sizeof(unsigned int), b->stream));
+    BatchSweepPlan p{b->sweep_items, b->step_off, b->nsteps, b->zero,
+                     b->nzero,          b->bar,      b->err_d, (unsigned long long)b->barrier_wait_ns};
+    BCK(launch_batch_sweep<T>((const SweepArgs<T> *)b->sweep_args, p, b->tx, b->ty, b->sweep_grid, b->stream));
+    b->rec_ok = true;  // the sweep recorded psi's row exponents (FP64 problems with a record)
+    if (ev) BCK(cudaEventRecord(ev[4], b->stream));
+    launch_batch_pop_finish(b->slot_ptrs, b->slot_n, (int)b->inst.size(), pop_out, b->stream);
+  }
   if (ev) BCK(cudaEventRecord(ev[5], b->stream));
   BCK(cudaGetLastError());
   return KGB_OK;
@@ -482,12 +505,12 @@ int checkBarrier(kgb_batch *b) {
     BCK(cudaMemsetAsync(b->err_d, 0, sizeof(int), b->stream));
     return fail(b, KGB_ERR_TIMEOUT, "a grid barrier of the persistent sweep gave up waiting");
   }
-  // the problems' own tensor-core kernels report their bounded waits through their contexts
-  if (perProblem(b))
+  // the problems' own kernels report their bounded waits through their contexts
+  if (perProblem(b) || ownSweeps(b))
     for (size_t i = 0; i < b->inst.size(); ++i)
       if (instance_check(b->inst[i]) != KGB_OK)
         return fail(b, KGB_ERR_TIMEOUT,
-                    "problem " + std::to_string(i) + ": a tensor-core kernel's bounded wait gave up");
+                    "problem " + std::to_string(i) + ": a kernel's bounded wait gave up");
   return KGB_OK;
 }
 
@@ -618,6 +641,8 @@ int kgb_batch_set_option(kgb_batch *b, const char *key, int64_t value) {
     b->use_graph = value != 0;
   } else if (k == "per_problem_kernels") {
     b->own_mode = value < 0 ? -1 : (value != 0 ? 1 : 0);
+  } else if (k == "per_problem_sweeps") {
+    b->sweep_mode = value < 0 ? -1 : (value != 0 ? 1 : 0);
   } else {
     return fail(b, KGB_ERR_ARG, "unknown option '" + k + "'");
   }
@@ -635,6 +660,7 @@ int kgb_batch_get_option(kgb_batch *b, const char *key, int64_t *value) {
   else if (k == "barrier_wait_ns") *value = b->barrier_wait_ns;
   else if (k == "graph") *value = b->use_graph;
   else if (k == "per_problem_kernels") *value = perProblem(b);
+  else if (k == "per_problem_sweeps") *value = ownSweeps(b);
   else if (k == "graph_active") *value = b->graph_active;
   else if (k == "sweep_grid") *value = b->sweep_grid;
   else if (k == "sweep_steps") *value = b->nsteps;
@@ -681,21 +707,30 @@ int kgb_batch_autotune(kgb_batch *b, double *best_ms) {
   int bx = b->tx, by = b->ty, bz = b->tz;
   const int xys[3][2] = {{2, 2}, {4, 2}, {4, 4}};
   const int zs[4] = {2, 4, 8, 16};
-  for (auto &xy : xys)
-    for (int z : zs) {
-      b->tx = xy[0];
-      b->ty = xy[1];
-      b->tz = z;
-      if ((rc = plan(b)) || (rc = ensurePop(b, 1))) return rc;
-      float ms = 0.f;
-      if ((rc = timeIteration(b, &ms))) return rc;
-      if (ms < best) {
-        best = ms;
-        bx = xy[0];
-        by = xy[1];
-        bz = z;
+  // the persistent sweep or each problem's own sweeps, unless the caller fixed the choice
+  const int fixed_sweep = b->sweep_mode;
+  int bsweep = ownSweeps(b) ? 1 : 0;
+  for (int sm = 0; sm < 2; ++sm) {
+    if (fixed_sweep >= 0 && sm != fixed_sweep) continue;
+    b->sweep_mode = sm;
+    for (auto &xy : xys)
+      for (int z : zs) {
+        b->tx = xy[0];
+        b->ty = xy[1];
+        b->tz = z;
+        if ((rc = plan(b)) || (rc = ensurePop(b, 1))) return rc;
+        float ms = 0.f;
+        if ((rc = timeIteration(b, &ms))) return rc;
+        if (ms < best) {
+          best = ms;
+          bx = xy[0];
+          by = xy[1];
+          bz = z;
+          bsweep = sm;
+        }
       }
-    }
+  }
+  b->sweep_mode = fixed_sweep >= 0 ? fixed_sweep : bsweep;
   b->tx = bx;
   b->ty = by;
   b->tz = bz;

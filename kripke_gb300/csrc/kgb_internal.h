@@ -346,8 +346,14 @@ int instance_view(kgb_ctx *ctx, InstanceView *v);
 // kernels the context chooses (tensor-core or SIMT): LTimes (phi = L psi),
 // LPlusTimes (rhs = L+ phi_out), or scattering then source (phi_out = S phi + q).
 // psi_exp (LTimes): psi's row exponents as the batched sweep recorded them, or null.
-enum class InstanceOp { LTimes, Scatter, LPlusTimes };
-int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s, const int *psi_exp = nullptr);
+// Sweep: the problem's own sweep of every octant (its tiles and kernels, the
+// streamed FP32 sweep where it applies) with the population of the new psi
+// summed into *pop; with psi_exp (FP64), psi's row exponents are recorded there.
+enum class InstanceOp { LTimes, Scatter, LPlusTimes, Sweep };
+int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s, const int *psi_exp = nullptr,
+                double *pop = nullptr);
+int instance_tiles(kgb_ctx *ctx, int tx, int ty, int tz);  // sets the problem's sweep tiles
+int64_t instance_sweep_launches(const kgb_ctx *ctx);       // kernels one Sweep op launches
 // Reports (KGB_ERR_TIMEOUT) and clears a bounded wait of one of the context's
 // tensor-core kernels that gave up; the caller has synchronised the streams
 // those kernels ran on.

@@ -674,7 +674,7 @@ int instance_view(kgb_ctx *ctx, InstanceView *v) {
   return KGB_OK;
 }
 
-int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s, const int *psi_exp) {
+int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s, const int *psi_exp, double *pop) {
   cudaStream_t keep = ctx->stream;
   ctx->stream = s;
   // a batched iteration runs each problem's LTimes and then its scattering (same
@@ -684,6 +684,13 @@ int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s, const int
   switch (op) {
     case InstanceOp::LTimes: rc = doLTimes(ctx, false, psi_exp, pe); break;
     case InstanceOp::LPlusTimes: rc = doLPlusTimes(ctx, false); break;
+    case InstanceOp::Sweep:
+      rc = sweepSolver(ctx, true, false, const_cast<int *>(psi_exp), false);
+      if (!rc && pop) {
+        launch_sum_partials(ctx->pop_slots, ctx->npop_used, pop, s);
+        if (cudaGetLastError() != cudaSuccess) rc = fail(ctx, KGB_ERR_CUDA, "population partial sum launch failed");
+      }
+      break;
     default:
       rc = doScattering(ctx, false, pe);
       if (!rc) rc = doSource(ctx, q);
@@ -693,6 +700,18 @@ int instance_op(kgb_ctx *ctx, InstanceOp op, double q, cudaStream_t s, const int
   return rc;
 }
 int instance_check(kgb_ctx *ctx) { return checkDeviceError(ctx); }
+int instance_tiles(kgb_ctx *ctx, int tx, int ty, int tz) {
+  if (ctx->tx == tx && ctx->ty == ty && ctx->tz == tz && ctx->tiles_d) return KGB_OK;
+  ctx->tx = tx;
+  ctx->ty = ty;
+  ctx->tz = tz;
+  ctx->tiles_set = true;
+  return buildTiles(ctx);
+}
+int64_t instance_sweep_launches(const kgb_ctx *ctx) {
+  const int np = std::max(1, std::min(ctx->sweep_streams, ctx->dc.num()));
+  return (int64_t)ctx->nsteps * np + 1;  // the steps' parts and the population sum
+}
 }  // namespace kgb
 
 extern "C" {

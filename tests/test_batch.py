@@ -1,5 +1,6 @@
 """Batched problems: one launch per kernel family, the sweeps of every problem
-in one persistent launch, a solve replayed from a CUDA graph.
+in one persistent launch (or each problem's own sweeps on parallel graph
+branches), a solve replayed from a CUDA graph.
 
 Parity: each problem's psi equals, bit for bit, that of the same problem's
 own context run with the batch's sweep tiles (and the SIMT kernels when the
@@ -63,6 +64,31 @@ def test_batch_equals_single_contexts(kgb, prec, own, tiles):
         # fused sweep partials: the same sums in another order
         np.testing.assert_allclose(parts[:, i], want, rtol=1e-13)
         np.testing.assert_array_equal(psis[i], psi)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_batch_sweep_modes_agree(kgb, prec):
+    """The persistent launch over all problems and each problem's own sweeps (the streamed FP32
+    sweep where a problem's direction sets allow it: 16 and 24 directions per set here) give the
+    same psi bit for bit; the particle counts are the same sums grouped by other blocks."""
+    precision = kgb.FP64 if prec == "fp64" else kgb.MIXED
+    inputs = uneven_inputs(5, seed=17, zones=(5, 12), groups=(8, 16), directions=(96, 128, 192), legendre=(2, 4),
+                           precision=precision)
+    b = make_batch(kgb, inputs, precision)
+    runs = []
+    for tiles in ((42, 4), (44, 8)):
+        for mode in (0, 1):
+            b.set_option("sweep_tile_xy", tiles[0])
+            b.set_option("sweep_tile_z", tiles[1])
+            b.set_option("per_problem_sweeps", mode)
+            parts = b.solve(4)
+            assert b.get_option("per_problem_sweeps") == mode and b.get_option("graph_active") == 1
+            runs.append((parts, [b.context(i).download("psi") for i in range(len(b))]))
+    for parts, psis in runs[1:]:
+        np.testing.assert_allclose(parts, runs[0][0], rtol=1e-12)
+        for got, want in zip(psis, runs[0][1]):
+            np.testing.assert_array_equal(got, want)
 
 
 @pytest.mark.gpu
