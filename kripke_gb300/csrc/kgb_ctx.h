@@ -118,6 +118,9 @@ struct kgb_ctx {
   // stream_ns k-slices of operands in flight per block
   bool allow_stream = true;
   int stream_ns = 2;
+  // mixed LTimes on the TMA-fed SIMT kernel (ltimes_stream.cu), lt_stream_ns stages
+  bool allow_lt_stream = true;
+  int lt_stream_ns = 2;
 
   // device state (element type T = double or float by precision)
   void *psi = nullptr, *rhs = nullptr, *phi = nullptr, *phi_out = nullptr, *sigt = nullptr;

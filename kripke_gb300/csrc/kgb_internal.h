@@ -142,6 +142,13 @@ int launch_tf32_lplustimes(const float *phi_out, float *rhs, int64_t rows, int D
                            bool accumulate, int *err, int nsm, cudaStream_t s);
 bool launch_ltimes_record(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M,
                           int *outexp, int rexp_w, int G, cudaStream_t s);
+// FP32 LTimes phi = L psi (not accumulated) on the TMA-fed SIMT kernel
+// (ltimes_stream.cu): directions a multiple of 32, 13 <= M <= 32, ns = 2..4
+// shared-memory stages; bit for bit the register-tiled kernel.  Nonzero return:
+// not launched.
+bool ltimes_stream_applies(int D, int M);
+int launch_ltimes_stream(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M, int ns,
+                         int *err, int nsm, cudaStream_t s);
 
 struct ScatterArgsBase {
   int64_t Z;                  // zones (rows = Z * destination groups); with zlist, the list's length

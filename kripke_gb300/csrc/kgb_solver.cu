@@ -329,6 +329,14 @@ int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp, int *outexp) {
     CKN(1);
     return KGB_OK;
   }
+  if (ctx->prec == KGB_MIXED && !acc && ctx->allow_lt_stream && ltimes_stream_applies(ctx->D, ctx->M)) {
+    // the TMA-fed SIMT kernel (bit for bit the register-tiled one)
+    if (launch_ltimes_stream(as<float>(ctx->psi), as<float>(ctx->phi), as<float>(ctx->ell), rows, ctx->D, ctx->M,
+                             ctx->lt_stream_ns, ctx->err_d, ctx->nsm, ctx->stream))
+      return fail(ctx, KGB_ERR_CUDA, "streamed LTimes launch failed");
+    CKN(1);
+    return KGB_OK;
+  }
   if (ctx->prec == KGB_FP64)
     launch_ltimes<double>(as<double>(ctx->psi), as<double>(ctx->phi), as<double>(ctx->ell), rows, ctx->D, ctx->M, acc, ctx->stream);
   else
