@@ -94,8 +94,7 @@ void launch_sweep_step(const SweepArgs<T> &a, int ntiles, int nwave, cudaStream_
 // fused prologue or epilogue) when a block's 128 chains are whole groups whose
 // operand boxes meet TMA's 16-byte rules: a multiple of 4 directions per set
 // (at most 32), blocks of GB whole groups (GB a multiple of 4 dividing the
-// group set, GB x Ds a whole number of warps, at most 128 chains), D and G
-// multiples of 4.  Tile footprints 4x4 and 4x2 (8x4 needs 150+ registers a
+// group set, GB x Ds = 128 or 96 chains), D and G multiples of 4.  Tile footprints 4x4 and 4x2 (8x4 needs 150+ registers a
 // thread for its k faces).
 constexpr int kStreamMaxStages = 4;
 int stream_block_chains(int Ds, int Gs);  // chains per block, 0: not streamable

@@ -110,14 +110,15 @@ __device__ __forceinline__ void tmaLoad2(uint32_t dst, const CUtensorMap *m, int
       : "memory");
 }
 
-template <int TX, int TY, bool POP, int MINB>
-__global__ void __launch_bounds__(kSweepThreads, MINB) sweep_stream_kernel(const __grid_constant__ SweepArgs<float> a,
+template <int TX, int TY, bool POP, int MINB, int BT>
+__global__ void __launch_bounds__(BT, MINB) sweep_stream_kernel(const __grid_constant__ SweepArgs<float> a,
                                                                    const __grid_constant__ StreamMaps maps) {
   extern __shared__ __align__(128) unsigned char sraw[];
   __shared__ __align__(8) uint64_t full[kStreamMaxStages], kbar;
   const int ns = a.stream_ns;
-  const int BT = blockDim.x;            // chains per block: GB whole groups
-  const int GB = BT / a.Ds;             // groups per block
+  // BT chains per block (GB whole groups), a compile-time constant so that the
+  // per-cell shared-memory offsets are (measured: a runtime block size cost 10 %)
+  const int GB = BT / a.Ds;
   const uint32_t rbytes = rhsBoxBytes(TX, TY, BT), sbytes = sigBoxBytes(TX, TY, GB);
   const uint32_t frow = faceRowBytes(BT);
   const uint32_t foff = rbytes + ((sbytes + 127u) & ~127u);  // the face rows within a stage
@@ -327,30 +328,35 @@ bool encode(CUtensorMap *m, const float *base, int rank, const cuuint64_t *dims,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int TX, int TY, bool POP, int MINB>
+template <int TX, int TY, bool POP, int MINB, int BT>
 void launchStreamAs(const SweepArgs<float> &a, dim3 grid, cudaStream_t s, const StreamMaps &m) {
-  const int bt = stream_block_chains(a.Ds, a.Gs);
-  const size_t smem = streamSmemBytes(TX, TY, bt / a.Ds, bt, a.stream_ns);
+  const size_t smem = streamSmemBytes(TX, TY, BT / a.Ds, BT, a.stream_ns);
   if (smem > 48 * 1024)
-    cudaFuncSetAttribute(sweep_stream_kernel<TX, TY, POP, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  sweep_stream_kernel<TX, TY, POP, MINB><<<grid, bt, smem, s>>>(a, m);
+    cudaFuncSetAttribute(sweep_stream_kernel<TX, TY, POP, MINB, BT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+  sweep_stream_kernel<TX, TY, POP, MINB, BT><<<grid, BT, smem, s>>>(a, m);
 }
 
 template <int TX, int TY, int MINB>
-void launchStream(const SweepArgs<float> &a, dim3 grid, cudaStream_t s, const StreamMaps &m) {
-  if (a.pop) launchStreamAs<TX, TY, true, MINB>(a, grid, s, m);
-  else launchStreamAs<TX, TY, false, MINB>(a, grid, s, m);
+void launchStream(const SweepArgs<float> &a, dim3 grid, cudaStream_t s, const StreamMaps &m, int bt) {
+  if (bt == 96) {
+    if (a.pop) launchStreamAs<TX, TY, true, MINB, 96>(a, grid, s, m);
+    else launchStreamAs<TX, TY, false, MINB, 96>(a, grid, s, m);
+  } else {
+    if (a.pop) launchStreamAs<TX, TY, true, MINB, 128>(a, grid, s, m);
+    else launchStreamAs<TX, TY, false, MINB, 128>(a, grid, s, m);
+  }
 }
 
 }  // namespace
 
 int stream_block_chains(int Ds, int Gs) {
   // Whole groups per block, GB a multiple of 4 (16-byte sigt boxes) dividing the
-  // group set, at most 128 chains and a whole number of warps: 4, 8, 16 or 32
-  // directions per set fill 128 chains, 12 and 24 fill 96.
+  // group set, 128 or 96 chains (the kernel's two compiled block sizes): 4, 8, 16
+  // or 32 directions per set fill 128 chains, 12 and 24 fill 96.
   if (Ds < 4 || Ds % 4 != 0 || Ds > kSweepThreads / 4) return 0;
   for (int gb = kSweepThreads / Ds / 4 * 4; gb >= 4; gb -= 4)
-    if (Gs % gb == 0 && (gb * Ds) % 32 == 0) return gb * Ds;
+    if (Gs % gb == 0 && (gb * Ds == 128 || gb * Ds == 96)) return gb * Ds;
   return 0;
 }
 
@@ -381,8 +387,8 @@ bool launch_sweep_step_stream(const SweepArgs<float> &a, int ntiles, int nwave, 
     return false;
   dim3 grid((unsigned)(nch / bt), ntiles, nwave);
   // occupancy bounds: 4x4 at five blocks per SM (92 registers), 4x2 at seven (72)
-  if (a.tx == 4 && a.ty == 4) launchStream<4, 4, 5>(a, grid, s, m);
-  else launchStream<4, 2, 7>(a, grid, s, m);
+  if (a.tx == 4 && a.ty == 4) launchStream<4, 4, 5>(a, grid, s, m, bt);
+  else launchStream<4, 2, 7>(a, grid, s, m, bt);
   return true;
 }
 
