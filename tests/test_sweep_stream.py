@@ -59,6 +59,17 @@ def test_streamed_solve_populations_bitwise(oracle, kgb):
     np.testing.assert_allclose(runs[0][0], p.solve(4), rtol=1e-5)
 
 
+def test_streamed_block_jacobi_bitwise(oracle, kgb):
+    """Block Jacobi sweeps every zone set in one launch from zeroed planes: same bits either kernel."""
+    p, ctx = pair(oracle, kgb, precision=1, **dict(BASE, zones=(10, 8, 10), zsets=(2, 2, 1)))
+    ctx.set_option("block_jacobi", 1)
+    rhs = np.random.default_rng(13).uniform(0.0, 2.0, ctx.field_bytes("rhs") // 8)
+    want = sweep_with(ctx, rhs, 44, 3, 0)
+    got = sweep_with(ctx, rhs, 44, 3, 1)
+    for g, w in zip(got, want):
+        np.testing.assert_array_equal(g, w)
+
+
 def test_streamed_adjoint_bitwise(oracle, kgb):
     """The reversed orientation (the adjoint's transposed sweep) through unrolled gradients."""
     p, ctx = pair(oracle, kgb, precision=1, **dict(BASE, zones=(9, 8, 10), zsets=(1, 2, 1)))
