@@ -270,6 +270,26 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     for _ in range(args.warmup):
         ctx.iterate(want_population=False)
     ms = timed_steps(ctx, stream, args.steps)
+    # per-family times (CUDA events around each family on the context's stream) over the same
+    # number of further iterations, and each family's algorithmic bytes against the copy bandwidth
+    ctx.reset_timers()
+    ctx.set_timing(True)
+    timed_steps(ctx, stream, args.steps)
+    fam_ms = {f: ctx.kernel_time(f)[0] / args.steps for f in ("sweep", "ltimes", "lplustimes", "scattering",
+                                                              "source", "population")}
+    ctx.set_timing(False)
+    alg = algorithmic(w, 4)
+    hbm = peaks()["hbm_gbs"]
+    traffic = {}
+    traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_file):
+        traffic = json.load(open(traffic_file))
+    fam_roof = {}
+    for f in ("sweep", "ltimes", "lplustimes", "scattering"):
+        if fam_ms[f] > 0:
+            gbs = alg[f]["bytes"] / (fam_ms[f] * 1e-3) / 1e9
+            fam_roof[f] = {"achieved_gbs": gbs, "frac_of_hbm": gbs / hbm, "algorithmic_bytes": alg[f]["bytes"],
+                           "traffic": traffic.get("mixed/" + f)}
     # the fused LTimes epilogue acts inside a solve (the next iteration takes the sweep's moments):
     # solves of K iterations with and without it
     ms_solve = timed_solve(ctx, stream, args.steps)
@@ -311,6 +331,10 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     del a, b, a0, b0
     out = {"value": unknowns(w) / (ms * 1e-3), "unit": "unknowns/s", "ms_per_step": ms,
            "speedup_vs_fp64": fp64_ms / ms, "phi_rel_err_vs_fp64": err, "phi_rel_err_l2": err_l2,
+           "kernel_ms_per_step": fam_ms,
+           "roofline": {"peak_gbs": hbm, "bytes": "algorithmic: inputs read once, outputs written once (the "
+                                                   "sweep's entering and leaving faces not counted)",
+                        "families": fam_roof},
            "phi0_rel_err_max": err0,
            "phi_err_definition": "after %d iterations from psi = 0: max|phi_mixed - phi_fp64| / max|phi_fp64| over "
                                  "all moments, groups and zones; also the 2-norm ratio and the max-abs relative "
