@@ -502,8 +502,14 @@ int planTensorScatter(kgb_ctx *ctx) {
     CK(cudaStreamSynchronize(ctx->stream));  // the host list is freed on return
     return KGB_OK;
   }
-  // digit images (N blocks of 32 columns): forward B[k][n] = S(n <- k), adjoint B[k][n] = S(k <- n)
+  // digit images (N blocks of 32 columns): forward B[k][n] = S(n <- k), adjoint B[k][n] = S(k <- n);
+  // they depend on the scattering tables only, so a new mix of zones keeps them
   const int kpad = (G + 31) / 32 * 32, nbk = (G + 31) / 32;
+  if (!ctx->tcsc_img_stale && ctx->tc_sc_img && ctx->tc_sc_img_adj && ctx->tc_sc_kpad == kpad) {
+    CK(cudaStreamSynchronize(ctx->stream));  // the host list is freed on return
+    ctx->tc_sc = true;
+    return KGB_OK;
+  }
   std::vector<double> b((size_t)G * G);
   std::vector<uint16_t> img, all;
   std::vector<int> ex, allex;
@@ -532,6 +538,7 @@ int planTensorScatter(kgb_ctx *ctx) {
   }
   ctx->tc_sc_kpad = kpad;
   ctx->tc_sc = true;
+  ctx->tcsc_img_stale = false;
   return KGB_OK;
 }
 
@@ -648,6 +655,7 @@ int prepareT(kgb_ctx *ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->dirty_sigs = false;
     ctx->dirty_tcsc = true;
+    ctx->tcsc_img_stale = true;
     ++ctx->gen;
     ctx->adj_stale = true;
   }

@@ -233,6 +233,7 @@ struct kgb_ctx {
   // (material, order) matrix (transposed for the forward operator, as is for
   // the adjoint), the zones of each material, and the other zones (SIMT)
   bool tc_sc = false, use_tc_sc = true, allow_tc_sc = true, dirty_tcsc = true;
+  bool tcsc_img_stale = true;  // the scattering's digit images predate sigs (zone lists aside)
   // zone-blocked FP32 scattering of the single-material zones (mixed form, scatter.cu)
   bool allow_blk_sc = true, use_blk_sc = true;
   uint16_t *tc_sc_img = nullptr, *tc_sc_img_adj = nullptr;

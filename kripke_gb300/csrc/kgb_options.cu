@@ -94,6 +94,7 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
   if (!std::strcmp(key, "scattering_block")) {
     ctx->allow_blk_sc = ctx->use_blk_sc = value != 0;
     ctx->dirty_tcsc = true;  // the zone lists are (re)built with the scattering plan
+    ctx->tcsc_img_stale = true;
     ++ctx->gen;
     return KGB_OK;
   }
@@ -106,6 +107,7 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->allow_tc_sc = value != 0;
     ctx->use_tc_sc = value != 0;
     ctx->dirty_tcsc = true;
+    ctx->tcsc_img_stale = true;
     return KGB_OK;
   }
   if (!std::strcmp(key, "sweep_reciprocals")) {

@@ -602,20 +602,28 @@ int solveIterations(kgb_ctx *ctx, int niter, double q) {
 int solveGraph(kgb_ctx *ctx, int niter, double q, const kgb_ctx::SolveGraph **out) {
   *out = nullptr;
   auto &v = ctx->solve_graphs;
+  for (auto &e : v)
+    if (e.gen == ctx->gen && e.niter == niter && e.q == q && e.stream == ctx->stream) {
+      *out = &e;
+      return KGB_OK;
+    }
+  // A solve of this shape captured before the tables changed: its executable graph is
+  // updated in place from the new capture when the topology is the same (new buffers
+  // or kernel arguments only), which costs far less than instantiating a new one.
+  cudaGraphExec_t stale_x = nullptr;
   for (auto it = v.begin(); it != v.end();) {
     if (it->gen != ctx->gen) {
-      cudaGraphExecDestroy(it->x);
+      if (!stale_x && it->niter == niter && it->q == q && it->stream == ctx->stream) {
+        stale_x = it->x;
+      } else {
+        cudaGraphExecDestroy(it->x);
+      }
       cudaGraphDestroy(it->g);
       it = v.erase(it);
     } else {
       ++it;
     }
   }
-  for (auto &e : v)
-    if (e.niter == niter && e.q == q && e.stream == ctx->stream) {
-      *out = &e;
-      return KGB_OK;
-    }
   if (v.size() >= 4) {
     cudaGraphExecDestroy(v.front().x);
     cudaGraphDestroy(v.front().g);
@@ -623,6 +631,7 @@ int solveGraph(kgb_ctx *ctx, int niter, double q, const kgb_ctx::SolveGraph **ou
   }
   if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
     cudaGetLastError();
+    if (stale_x) cudaGraphExecDestroy(stale_x);
     return KGB_OK;
   }
   const int64_t l0 = ctx->launches;
@@ -636,8 +645,20 @@ int solveGraph(kgb_ctx *ctx, int niter, double q, const kgb_ctx::SolveGraph **ou
   const int64_t captured = ctx->launches - l0;
   ctx->launches = l0;  // counted when replayed
   cudaGraphExec_t x = nullptr;
-  if (rc || e != cudaSuccess || !g || cudaGraphInstantiate(&x, g, 0) != cudaSuccess) {
+  if (!rc && e == cudaSuccess && g && stale_x) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(stale_x, g, &info) == cudaSuccess) {
+      x = stale_x;
+    } else {
+      cudaGetLastError();
+      cudaGraphExecDestroy(stale_x);
+    }
+    stale_x = nullptr;
+  }
+  if (stale_x) cudaGraphExecDestroy(stale_x);
+  if (rc || e != cudaSuccess || !g || (!x && cudaGraphInstantiate(&x, g, 0) != cudaSuccess)) {
     cudaGetLastError();
+    if (x) cudaGraphExecDestroy(x);
     if (g) cudaGraphDestroy(g);
     ctx->err = err0;
     return KGB_OK;

@@ -680,6 +680,12 @@ void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhal
   texp.assign((size_t)nhalf * NB, 0);
   uint64_t bias = 0;
   for (int j = 0; j < S; ++j) bias |= 0x80ull << (8 * j);
+  // f16 patterns of every digit value -128 .. 128, built once
+  static const std::vector<uint16_t> halfDigits = [] {
+    std::vector<uint16_t> t(257);
+    for (int v = -128; v <= 128; ++v) t[v + 128] = halfOfDigit(v);
+    return t;
+  }();
   for (int n = 0; n < N; ++n) {
     int emax = 1;
     for (int k = 0; k < K; ++k) {
@@ -704,7 +710,7 @@ void tc_build_b(const double *b, int K, int N, int kpad, int S, int NB, int nhal
       const uint64_t y = f + bias;  // balanced digits: byte - 128
       for (int j = 1; j <= S; ++j) {
         const int dg = (int)((y >> (8 * (S - j))) & 0xFFu) - 128;
-        const uint16_t bf = halfOfDigit(neg ? -dg : dg);
+        const uint16_t bf = halfDigits[(neg ? -dg : dg) + 128];
         const int rowi = (j - 1) * NB + nl;
         const size_t off = (size_t)h * kpad * S * NB + (size_t)(k / 8) * (S * NB * 8) + (size_t)(rowi / 8) * 64 +
                            (size_t)(rowi % 8) * 8 + (k % 8);
