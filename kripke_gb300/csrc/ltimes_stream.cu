@@ -22,6 +22,7 @@
 #include <cudaTypedefs.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "kgb_internal.h"
 
@@ -136,6 +137,7 @@ __global__ void __launch_bounds__(kLsThreads) ltimes_stream_kernel(const __grid_
 
   float acc[4][MB];
   const int swz = lane & 7;  // rows lane + 32 i share their low three bits
+  const bool short_last = w == kLsCompute - 1 && M - MB * w <= 4;
   for (int64_t q = 0; q < nq; ++q) {
     if (q % nk == 0) {
 #pragma unroll
@@ -148,26 +150,33 @@ __global__ void __launch_bounds__(kLsThreads) ltimes_stream_kernel(const __grid_
     if (!ok) break;
     const unsigned char *buf = al + (size_t)s * kLsStageBytes;
     const float *lk = ls + (size_t)(q % nk) * kLsK * 32 + 8 * w;
+    // the chunk's 32 directions into the warp's NM moments (the last warp may hold fewer
+    // real moments than MB: 25 = 7 + 7 + 7 + 4, so it runs the 4-moment loop)
+    auto chunk = [&](auto nm_tag) {
+      constexpr int NM = decltype(nm_tag)::value;
 #pragma unroll 2
-    for (int k4 = 0; k4 < kLsK / 4; ++k4) {
-      float4 a[4];
+      for (int k4 = 0; k4 < kLsK / 4; ++k4) {
+        float4 a[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
-        a[i] = *reinterpret_cast<const float4 *>(buf + (lane + 32 * i) * 128 + ((k4 ^ swz) << 4));
+        for (int i = 0; i < 4; ++i)
+          a[i] = *reinterpret_cast<const float4 *>(buf + (lane + 32 * i) * 128 + ((k4 ^ swz) << 4));
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk) {
-        float l[8];
-        *reinterpret_cast<float4 *>(l) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32);
-        if (MB > 4) *reinterpret_cast<float4 *>(l + 4) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32 + 4);
+        for (int kk = 0; kk < 4; ++kk) {
+          float l[8];
+          *reinterpret_cast<float4 *>(l) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32);
+          if (NM > 4) *reinterpret_cast<float4 *>(l + 4) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32 + 4);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const float x = kk == 0 ? a[i].x : kk == 1 ? a[i].y : kk == 2 ? a[i].z : a[i].w;
+          for (int i = 0; i < 4; ++i) {
+            const float x = kk == 0 ? a[i].x : kk == 1 ? a[i].y : kk == 2 ? a[i].z : a[i].w;
 #pragma unroll
-          for (int m = 0; m + 1 < MB; m += 2) fma2(acc[i][m], acc[i][m + 1], l[m], l[m + 1], x);
-          if (MB & 1) acc[i][MB - 1] = __fmaf_rn(l[MB - 1], x, acc[i][MB - 1]);
+            for (int m = 0; m + 1 < NM; m += 2) fma2(acc[i][m], acc[i][m + 1], l[m], l[m + 1], x);
+            if (NM & 1) acc[i][NM - 1] = __fmaf_rn(l[NM - 1], x, acc[i][NM - 1]);
+          }
         }
       }
-    }
+    };
+    if (MB > 4 && short_last) chunk(std::integral_constant<int, 4>{});
+    else chunk(std::integral_constant<int, MB>{});
     __syncwarp();
     if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sAddr(&empty[s])) : "memory");
     if (q % nk == nk - 1) {
