@@ -10,21 +10,27 @@ namespace api {
 // ---------------------------------------------------------------------------
 // Kernel drivers
 // ---------------------------------------------------------------------------
-// Lanes of one group in the sweep's chain order (chains run over a direction
-// set's directions fastest), for the sweep's row-exponent reduction; 0 when a
-// warp's groups are not aligned runs of a power-of-two length.
+// Runs of lanes of one group in the sweep's chain order (chains run over a
+// direction set's directions fastest), for the sweep's row-exponent reduction:
+// the largest power of two dividing the set size, at most 32 -- a group's chains
+// start at multiples of the set size, so aligned runs of that length never mix
+// two groups (24 directions: runs of 8, three atomics per group and cell); 0
+// below runs of 4, where the atomics would cost the sweep more than the pass
+// they save.
 int psiExpWidth(const kgb_ctx *ctx) {
   const int ds = ctx->Ds;
-  if (ds % 32 == 0) return 32;
-  return (ds > 0 && ds < 32 && (ds & (ds - 1)) == 0) ? ds : 0;
+  if (ds <= 0) return 0;
+  const int w = std::min(ds & -ds, 32);
+  return w >= 4 ? w : 0;
 }
 
 // The solver's sweep records psi's row exponents for the next tensor-core
-// LTimes (FP64, every direction in one K chunk), which then skips its own pass
-// over each row.
+// LTimes (FP64), which then skips its own pass over each row.  With more
+// directions than one K chunk, every chunk scales by the whole row's exponent
+// (as one launch over the whole row would; a pass would take each chunk's own).
 bool psiExpUsable(const kgb_ctx *ctx) {
   return ctx->prec == KGB_FP64 && ctx->allow_row_exp && ctx->psi_exp && ctx->tc_lt && ctx->use_tc_lt &&
-         ctx->D <= ctx->tc_lt_kpad && psiExpWidth(ctx) > 0;
+         psiExpWidth(ctx) > 0;
 }
 
 // Lanes of one zone in the tensor-core LTimes' epilogue (one lane per (zone,
@@ -306,11 +312,11 @@ int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp, int *outexp) {
       const uint16_t *img = ctx->tc_lt_img + (size_t)c * kc * S * 32;
       const int *ex = ctx->tc_lt_exp + (size_t)c * 32;
       if (ctx->prec == KGB_FP64) {
-        const bool one = ctx->D <= kc && !acc;  // the records hold for a whole, fresh phi only
+        const bool one = ctx->D <= kc && !acc;  // phi's record holds for a whole, fresh phi only
         if (outexp && !one) return fail(ctx, KGB_ERR_STATE, "phi exponent record needs one fresh LTimes launch");
         if (outexp) CK(cudaMemsetAsync(outexp, 0, ctx->Z * ctx->M * sizeof(int), ctx->stream));
         tcRows<double>(ctx, as<double>(ctx->psi) + k0, as<double>(ctx->phi), ctx->D, ctx->M, K, kc, ctx->M, 1, img,
-                       ex, acc || c > 0, false, one ? rowexp : nullptr, outexp);
+                       ex, acc || c > 0, false, rowexp, outexp);
       } else {
         if (outexp) return fail(ctx, KGB_ERR_STATE, "phi exponent record: not on the FP32 tensor-core LTimes");
         tcRows<float>(ctx, as<float>(ctx->psi) + k0, as<float>(ctx->phi), ctx->D, ctx->M, K, kc, ctx->M, 1, img, ex,

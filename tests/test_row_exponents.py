@@ -37,7 +37,7 @@ def same(a, b, fields=("psi", "phi", "phi_out", "rhs")):
 
 @pytest.mark.parametrize("kw", [dict(), dict(quad=(8, 16)), dict(quad=(8, 8)), dict(zsets=(2, 1, 2)),
                                 dict(zsets=(5, 3, 1), block_jacobi=True), dict(groups=64, legendre=4),
-                                dict(groups=12)])
+                                dict(groups=12), dict(quad=(8, 12))])
 def test_iterates_bitwise(kgb, kw):
     bj = kw.pop("block_jacobi", False)
     a, b = pair(kgb, **kw)
@@ -60,12 +60,31 @@ def test_iterates_bitwise(kgb, kw):
     same(a, b)
 
 
-def test_unaligned_direction_sets_fall_back(kgb):
-    # 3 directions per set: a warp's groups are not power-of-two runs, nothing is recorded
-    a, b = pair(kgb, quad=(4, 6))
+@pytest.mark.parametrize("quad", [(4, 6), (4, 12)])
+def test_unaligned_direction_sets_fall_back(kgb, quad):
+    # 3 and 6 directions per set: a warp's groups share no aligned run of 4 lanes, nothing is recorded
+    a, b = pair(kgb, quad=quad)
     assert [a.iterate() for _ in range(3)] == [b.iterate() for _ in range(3)]
     assert b.get_option("psi_row_exponents_active") == 0 and b.get_option("moments_tensor_ltimes") == 1
     same(a, b)
+
+
+def test_record_over_two_k_chunks(kgb, oracle):
+    # 192 directions (24 per set: runs of 8 lanes) take two tensor-core LTimes launches, each scaled
+    # by the whole row's recorded exponent instead of its own chunk's: the same 54 bits of every
+    # element relative to the row, so the iterates agree with the pass to FP64 rounding and with
+    # the oracle to 1e-12
+    kw = dict(zones=(6, 5, 7), groups=8, quad=(8, 24), legendre=3, geometry=1, scatter=1, gset=1, dset=8)
+    a, b = pair(kgb, **kw)
+    pa = [a.iterate() for _ in range(4)]
+    pb = [b.iterate() for _ in range(4)]
+    assert b.get_option("psi_row_exponents_active") == 1 and b.get_option("moments_tensor_ltimes") == 1
+    np.testing.assert_allclose(pb, pa, rtol=1e-13)
+    for f in ("psi", "phi"):
+        got, want = b.download(f), a.download(f)
+        assert np.max(np.abs(got - want)) <= 1e-13 * np.max(np.abs(want)), f
+    p = oracle.Problem(**kw)
+    np.testing.assert_allclose(b.solve(5), p.solve(5), rtol=1e-12)
 
 
 def test_converged_solve_bitwise(kgb):
