@@ -202,7 +202,8 @@ __global__ void __launch_bounds__(kBlkThreads, 2)
 
 // Staged zone-blocked scattering (groups a multiple of 4, at most 64; Legendre
 // order <= 4).  A CTA holds one material's transfer matrices ([l][g'][g]) and
-// runs two independent 128-thread groups.  A group's item is a run of zpi zones
+// runs kZoneGroups independent groups of kZoneGroup threads (each single-
+// buffered: while one waits for its copy the others compute).  A group's item is a run of zpi zones
 // of that material: one elected thread brings each zone's contiguous [G][MM]
 // phi block into the group's buffer with one bulk copy (an mbarrier counts the
 // bytes); a thread then owns 4 destination groups x MM moments of one zone in
@@ -220,8 +221,9 @@ __global__ void __launch_bounds__(kBlkThreads, 2)
 // thread are contiguous in phi_out and 16-byte aligned, stored (or added to,
 // one FP32 add per element) as 16-byte words, while the next item's copies are
 // in flight.
-constexpr int kZoneThreads = 256;  // two groups
-constexpr int kZoneGroup = 128;
+constexpr int kZoneThreads = 256;
+constexpr int kZoneGroup = 64;                         // threads of one group
+constexpr int kZoneGroups = kZoneThreads / kZoneGroup;  // independent groups per CTA
 constexpr uint64_t kZoneWaitNs = 200000000ull;  // 0.2 s
 
 __device__ __forceinline__ uint64_t zoneNowNs() {
@@ -265,8 +267,8 @@ __global__ void __launch_bounds__(kZoneThreads, 1)
                         const int *__restrict__ zl, const __grid_constant__ ScatterZonePlan pl, bool accumulate) {
   constexpr int MM = (LMAX + 1) * (LMAX + 1), L1 = LMAX + 1;
   extern __shared__ __align__(16) float zone_smem[];
-  __shared__ __align__(8) uint64_t full[2];
-  __shared__ int bad[2];
+  __shared__ __align__(8) uint64_t full[kZoneGroups];
+  __shared__ int bad[kZoneGroups];
   const int G = pl.G, GQ = G / 4, zpi = pl.zpi;
   float *sS = zone_smem;  // [L1][G][G]
   const int tid = threadIdx.x, gi = tid / kZoneGroup, gt = tid % kZoneGroup;
@@ -288,14 +290,14 @@ __global__ void __launch_bounds__(kZoneThreads, 1)
   lo = __reduce_min_sync(0xffffffffu, lo) & ~3;
   hi = (__reduce_max_sync(0xffffffffu, hi) + 4) & ~3;
   if (tid == 0) {
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < kZoneGroups; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&full[i])));
       bad[i] = 0;
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  const int stride = 2 * gridDim.x, first = 2 * blockIdx.x + gi;
+  const int stride = kZoneGroups * gridDim.x, first = kZoneGroups * blockIdx.x + gi;
   const uint32_t zbytes = (uint32_t)G * MM * 4;
   uint32_t ph = 0;
   bool pending = false;  // a copy issued by this group and not yet waited for (elected thread)
@@ -472,8 +474,8 @@ int zoneItemZones(int G) {
 
 size_t scatter_block_smem(int G, int L) {
   const int MM = (L + 1) * (L + 1), MP = (MM + 3) / 4 * 4;
-  if (G % 4 == 0)  // staged form: the matrices and two groups' zone buffers
-    return sizeof(float) * ((size_t)(L + 1) * G * G + (size_t)2 * zoneItemZones(G) * zoneSlot(G, L));
+  if (G % 4 == 0)  // staged form: the matrices and every group's zone buffer
+    return sizeof(float) * ((size_t)(L + 1) * G * G + (size_t)kZoneGroups * zoneItemZones(G) * zoneSlot(G, L));
   const int Gw = G < 32 ? G : 32, zpc = (kBlkThreads / 32) * (32 / Gw) / ((G + 31) / 32);
   return sizeof(float) * (((size_t)(L + 1) * G * G + 3) / 4 * 4 + (size_t)zpc * G * MP);
 }
@@ -496,7 +498,7 @@ void launch_scatter_block(const float *phi, float *phi_out, const float *sigsT, 
     for (int m = 0; m < 3; ++m) most = std::max(most, (off[m + 1] - off[m] + pl.zpi - 1) / pl.zpi);
     if (most == 0) return;
     const size_t smem = scatter_block_smem(G, L);
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((most + 1) / 2, nsm));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((most + kZoneGroups - 1) / kZoneGroups, nsm));
     auto go = [&](auto kernel) {
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       kernel<<<grid, kZoneThreads, smem, s>>>(phi, phi_out, sigsT, zl, pl, accumulate);
