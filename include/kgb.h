@@ -204,6 +204,18 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * "sweep_streams" (1 to 4: each sweep step launches its subdomains in that
  * many parts on as many streams, so one part's wave tail overlaps the others'
  * blocks; default 2);
+ * "sweep_stream" (mixed form: 1 = the sweep runs on the streamed kernel --
+ * each k-slice's rhs, sigt and entering faces copied into shared memory by
+ * TMA boxes, slices ahead -- where a block of 128 or 96 chains holds whole
+ * groups (4 to 32 directions per set, a multiple of 4; D and G multiples of 4;
+ * footprints 44 and 42; the divide form; no fused prologue or epilogue); bit
+ * for bit the per-step kernel's psi and planes; the default; 0 = off);
+ * "sweep_stream_stages" (1 to 4 slices of operands in flight per block;
+ * default 2);
+ * "ltimes_stream" (mixed form: 1 = the solver's LTimes on the TMA-fed SIMT
+ * kernel when directions are a multiple of 32 and 13 <= moments <= 32, bit for
+ * bit the register-tiled kernel; the default; 0 = off) and
+ * "ltimes_stream_stages" (2 to 4, default 2);
  * "block_jacobi" (0 = the sweep method, default; 1 = block Jacobi, used by
  * kgb_sweep_solver and so by every solve, iterate and adjoint call);
  * "fused_sweep" (mixed form, Legendre order <= 4: 1 = the solver loop forms
@@ -241,11 +253,13 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value);
  * kgb_solve fuses the LTimes epilogue on this problem),
  * "psi_row_exponents_active" and
  * "phi_row_exponents_active" (1 when the solver loop records them on this
- * problem) and "psi_row_exponents_valid" (1 when psi's record matches the
- * current psi). */
+ * problem), "psi_row_exponents_valid" (1 when psi's record matches the
+ * current psi) and "sweep_stream_active" (1 when the sweep runs on the
+ * streamed kernel with the current tiles). */
 int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value);
 /* Autotuner: times every sweep tile shape (footprint 4x4, 4x2, 2x2 x depth
- * 2, 4, 8, 16 zones) and both LTimes / LPlusTimes paths (tensor-core digit
+ * 2, 4, 8, 16 zones; in the mixed form also the streamed kernel at 4x4 and 4x2,
+ * depth up to 32) and both LTimes / LPlusTimes paths (tensor-core digit
  * products or SIMT) on this problem with CUDA events, keeps the fastest and
  * returns the sweep time (best_ms), footprint (as 44/42/22) and depth.  It
  * sweeps the current rhs and recomputes phi and rhs: psi, phi, rhs and the
@@ -345,7 +359,11 @@ int kgb_batch_context(kgb_batch *b, int32_t index, kgb_ctx **ctx);
  * of a moment / scattering work item), "graph" (1: capture solves, the
  * default), "per_problem_kernels" (1: each problem's own LTimes,
  * scattering and LPlusTimes kernels; 0: batched SIMT; -1: by precision, the
- * default), "barrier_wait_ns" (how long a grid-barrier wait of the persistent
+ * default), "per_problem_sweeps" (1: each problem's own sweeps -- its
+ * per-step launches, the streamed FP32 sweep where it applies -- on parallel
+ * graph branches, with the batch's tiles; 0: one persistent launch over all
+ * problems; -1: by precision, the default; psi is bit for bit the same
+ * either way), "barrier_wait_ns" (how long a grid-barrier wait of the persistent
  * sweep waits before it gives up; default 2e9; a solve whose wait gave up
  * returns KGB_ERR_TIMEOUT with its results undefined, and the batch stays
  * usable).  Read-only:
@@ -354,10 +372,10 @@ int kgb_batch_context(kgb_batch *b, int32_t index, kgb_ctx **ctx);
  * "kernels_per_iteration". */
 int kgb_batch_set_option(kgb_batch *b, const char *key, int64_t value);
 int kgb_batch_get_option(kgb_batch *b, const char *key, int64_t *value);
-/* Times every sweep tile shape (4x4, 4x2, 2x2 x depth 2, 4, 8, 16), row item
- * size (256, 1024, 4096) and, unless "per_problem_kernels" was set, both
- * transform modes on the batch and keeps the fastest; overwrites the
- * problems' state. */
+/* Times every sweep tile shape (4x4, 4x2, 2x2 x depth 2, 4, 8, 16) in both
+ * sweep modes (unless "per_problem_sweeps" was set), row item size (256,
+ * 1024, 4096) and, unless "per_problem_kernels" was set, both transform modes
+ * on the batch and keeps the fastest; overwrites the problems' state. */
 int kgb_batch_autotune(kgb_batch *b, double *best_ms);
 /* niter source iterations from psi = 0 for every problem (SteadyStateSolver
  * each); part (may be NULL) receives the particle counts [niter][n]. */
