@@ -81,7 +81,7 @@ __device__ __forceinline__ bool waitStage(uint64_t *bar, uint32_t parity) {
 }
 
 // Bytes of one stage: the rhs box, the sigt box (padded to 128 bytes), then
-// the slice's entering i faces (TY rows of the block's 128 chains) and j faces
+// the slice's entering i faces (TY rows of the block's bt chains) and j faces
 // (TX rows).  The k faces of the tile have their own buffer, filled once.
 // bt = chains per block (gb groups x Ds directions).
 __host__ __device__ __forceinline__ uint32_t rhsBoxBytes(int tx, int ty, int bt) { return (uint32_t)(tx * ty * bt * 4); }
