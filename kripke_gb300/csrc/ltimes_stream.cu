@@ -4,13 +4,20 @@
 // Kernel::LTimes (src/Kripke/Kernel/LTimes.cpp:54-65): phi(z,g,m) =
 // sum_d ell(m,d) psi(z,g,d) over the (zone, group) rows of the device nesting.
 // The arithmetic is the register-tiled kernel's of moments.cu: a block takes
-// 128-row tiles, each of its four compute warps keeps MB moments of the tile's
-// rows (4 rows a thread) in registers and walks the directions in ascending
-// order with paired FP32 multiply-adds, so every output is the same FMA chain
-// -- bit for bit the register-tiled and row-per-thread kernels.  What differs
-// is the operand path.  There every thread copied its share of each
-// 32-direction chunk with cp.async and the block synchronised twice a chunk;
-// here a fifth warp issues one TMA copy per chunk (a {32 directions, 128 rows}
+// 128-row tiles, each thread keeps MB = ceil(M/4) moments of four rows in
+// registers and walks the directions in ascending order with paired FP32
+// multiply-adds, so every output is the same FMA chain -- bit for bit the
+// register-tiled and row-per-thread kernels.  Each compute warp takes 32 rows
+// of the tile for all moments (its four lane groups a quarter of the moments
+// each), so a psi read serves four lanes and a warp's reads of one direction
+// quad cover eight rows in one shared-memory wavefront: half the wavefronts of
+// giving each warp all 128 rows for a quarter of the moments (measured 2.73
+// against 2.86 ms at 64^3 zones x 64 groups x 128 directions, P4), although
+// the last lane group computes three zero moments when M = 25.  The block is
+// held to 96 registers a thread, so four fit on an SM.  What differs from the
+// register-tiled kernel is the operand path.  There every thread copied its
+// share of each 32-direction chunk with cp.async and the block synchronised
+// twice a chunk; here a fifth warp issues one TMA copy per chunk (a {32 directions, 128 rows}
 // box, 128-byte swizzled so a quarter-warp's 16-byte reads of eight rows fall
 // in distinct banks) into a ring of shared-memory stages, the compute warps
 // wait on the stage's mbarrier and release it by one arrival each on a second
@@ -22,7 +29,6 @@
 #include <cudaTypedefs.h>
 
 #include <mutex>
-#include <type_traits>
 
 #include "kgb_internal.h"
 
@@ -75,7 +81,7 @@ __device__ __forceinline__ void fma2(float &c0, float &c1, float a0, float a1, f
 }
 
 template <int MB>
-__global__ void __launch_bounds__(kLsThreads) ltimes_stream_kernel(const __grid_constant__ CUtensorMap pmap,
+__global__ void __launch_bounds__(kLsThreads, 4) ltimes_stream_kernel(const __grid_constant__ CUtensorMap pmap,
                                                                    float *__restrict__ phi,
                                                                    const float *__restrict__ ell_dm, int64_t rows,
                                                                    int D, int M, int ns, int *err) {
@@ -136,8 +142,11 @@ __global__ void __launch_bounds__(kLsThreads) ltimes_stream_kernel(const __grid_
   }
 
   float acc[4][MB];
-  const int swz = lane & 7;  // rows lane + 32 i share their low three bits
-  const bool short_last = w == kLsCompute - 1 && M - MB * w <= 4;
+  // warp w holds the tile's rows 32 w .. 32 w + 31: lane group mg = lane % 4 the moments
+  // MB mg .. MB mg + MB - 1 of the rows 32 w + rg + 8 i (rg = lane / 4, i = 0..3)
+  const int mg = lane & 3;
+  const int rbase = 32 * w + (lane >> 2);
+  const int swz = rbase & 7;  // the thread's rows share their low three bits
   for (int64_t q = 0; q < nq; ++q) {
     if (q % nk == 0) {
 #pragma unroll
@@ -149,46 +158,40 @@ __global__ void __launch_bounds__(kLsThreads) ltimes_stream_kernel(const __grid_
     const bool ok = __all_sync(0xffffffffu, waitPar(&full[s], (uint32_t)(q / ns) & 1u, abort));
     if (!ok) break;
     const unsigned char *buf = al + (size_t)s * kLsStageBytes;
-    const float *lk = ls + (size_t)(q % nk) * kLsK * 32 + 8 * w;
-    // the chunk's 32 directions into the warp's NM moments (the last warp may hold fewer
-    // real moments than MB: 25 = 7 + 7 + 7 + 4, so it runs the 4-moment loop)
-    auto chunk = [&](auto nm_tag) {
-      constexpr int NM = decltype(nm_tag)::value;
+    const float *lk = ls + (size_t)(q % nk) * kLsK * 32 + 8 * mg;
+    // the chunk's 32 directions into the thread's MB moments of its four rows
 #pragma unroll 2
-      for (int k4 = 0; k4 < kLsK / 4; ++k4) {
-        float4 a[4];
+    for (int k4 = 0; k4 < kLsK / 4; ++k4) {
+      float4 a[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-          a[i] = *reinterpret_cast<const float4 *>(buf + (lane + 32 * i) * 128 + ((k4 ^ swz) << 4));
+      for (int i = 0; i < 4; ++i)
+        a[i] = *reinterpret_cast<const float4 *>(buf + (rbase + 8 * i) * 128 + ((k4 ^ swz) << 4));
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          float l[8];
-          *reinterpret_cast<float4 *>(l) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32);
-          if (NM > 4) *reinterpret_cast<float4 *>(l + 4) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32 + 4);
+      for (int kk = 0; kk < 4; ++kk) {
+        float l[8];
+        *reinterpret_cast<float4 *>(l) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32);
+        if (MB > 4) *reinterpret_cast<float4 *>(l + 4) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32 + 4);
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const float x = kk == 0 ? a[i].x : kk == 1 ? a[i].y : kk == 2 ? a[i].z : a[i].w;
+        for (int i = 0; i < 4; ++i) {
+          const float x = kk == 0 ? a[i].x : kk == 1 ? a[i].y : kk == 2 ? a[i].z : a[i].w;
 #pragma unroll
-            for (int m = 0; m + 1 < NM; m += 2) fma2(acc[i][m], acc[i][m + 1], l[m], l[m + 1], x);
-            if (NM & 1) acc[i][NM - 1] = __fmaf_rn(l[NM - 1], x, acc[i][NM - 1]);
-          }
+          for (int m = 0; m + 1 < MB; m += 2) fma2(acc[i][m], acc[i][m + 1], l[m], l[m + 1], x);
+          if (MB & 1) acc[i][MB - 1] = __fmaf_rn(l[MB - 1], x, acc[i][MB - 1]);
         }
       }
-    };
-    if (MB > 4 && short_last) chunk(std::integral_constant<int, 4>{});
-    else chunk(std::integral_constant<int, MB>{});
+    }
     __syncwarp();
     if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sAddr(&empty[s])) : "memory");
     if (q % nk == nk - 1) {
       const int64_t tile = blockIdx.x + (q / nk) * gridDim.x;
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const int64_t row = tile * kLsRows + lane + 32 * i;
+        const int64_t row = tile * kLsRows + rbase + 8 * i;
         if (row >= rows) continue;
-        float *o = phi + row * M + MB * w;
+        float *o = phi + row * M + MB * mg;
 #pragma unroll
         for (int m = 0; m < MB; ++m)
-          if (MB * w + m < M) o[m] = acc[i][m];
+          if (MB * mg + m < M) o[m] = acc[i][m];
       }
     }
   }
