@@ -9,12 +9,12 @@
 // multiply-adds, so every output is the same FMA chain -- bit for bit the
 // register-tiled and row-per-thread kernels.  Each compute warp takes 32 rows
 // of the tile for all moments (its four lane groups a quarter of the moments
-// each), so a psi read serves four lanes and a warp's reads of one direction
-// quad cover eight rows in one shared-memory wavefront: half the wavefronts of
-// giving each warp all 128 rows for a quarter of the moments (measured 2.73
-// against 2.86 ms at 64^3 zones x 64 groups x 128 directions, P4), although
-// the last lane group computes three zero moments when M = 25.  The block is
-// held to 96 registers a thread, so four fit on an SM.  What differs from the
+// each; the last group carries three zero moments when M = 25).  The block is
+// held to 96 registers a thread so that four fit on an SM: 2.73 ms at 64^3
+// zones x 64 groups x 128 directions, P4, against 2.86 ms at three blocks per
+// SM, and 2.74 ms with each warp on all 128 rows for a quarter of the moments
+// at four blocks (fewer shared-memory wavefronts, 70.6 against 86.7 M at 32^3,
+// but an extra loop for the short last quarter).  What differs from the
 // register-tiled kernel is the operand path.  There every thread copied its
 // share of each 32-direction chunk with cp.async and the block synchronised
 // twice a chunk; here a fifth warp issues one TMA copy per chunk (a {32 directions, 128 rows}
@@ -30,6 +30,7 @@
 
 #include <mutex>
 
+#include "fp32_pair.h"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -70,14 +71,6 @@ __device__ __forceinline__ bool waitPar(uint64_t *bar, uint32_t parity, volatile
   }
   if (!done) *abort = 1;
   return done != 0;
-}
-
-// (c0, c1) = (a0, a1) * x + (c0, c1), each rounded once to nearest (bit for bit two __fmaf_rn)
-__device__ __forceinline__ void fma2(float &c0, float &c1, float a0, float a1, float x) {
-  asm("{\n\t.reg .b64 ra, rb, rc;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %4};\n\tmov.b64 rc, {%0, %1};\n\t"
-      "fma.rn.f32x2 rc, ra, rb, rc;\n\tmov.b64 {%0, %1}, rc;\n\t}"
-      : "+f"(c0), "+f"(c1)
-      : "f"(a0), "f"(a1), "f"(x));
 }
 
 template <int MB>
@@ -175,7 +168,7 @@ __global__ void __launch_bounds__(kLsThreads, 4) ltimes_stream_kernel(const __gr
         for (int i = 0; i < 4; ++i) {
           const float x = kk == 0 ? a[i].x : kk == 1 ? a[i].y : kk == 2 ? a[i].z : a[i].w;
 #pragma unroll
-          for (int m = 0; m + 1 < MB; m += 2) fma2(acc[i][m], acc[i][m + 1], l[m], l[m + 1], x);
+          for (int m = 0; m + 1 < MB; m += 2) fma2Rn(acc[i][m], acc[i][m + 1], l[m], l[m + 1], x);
           if (MB & 1) acc[i][MB - 1] = __fmaf_rn(l[MB - 1], x, acc[i][MB - 1]);
         }
       }

@@ -8,6 +8,7 @@
 // shared memory and is read as a broadcast, 16 bytes per load.  Summation runs
 // over directions (LTimes) or moments (LPlusTimes) in ascending order, as the
 // reference loops.
+#include "fp32_pair.h"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -241,15 +242,6 @@ __global__ void __launch_bounds__(kMomThreads) batch_moments_kernel(const BatchM
 // multiply-adds per 1 + MB/4 shared-memory reads, against MB per one for the
 // row-per-thread kernel.  Each output is one FMA chain over ascending
 // directions, as in ltimesRow, so the results are the same bit for bit.
-// (c0, c1) = (a0, a1) * x + (c0, c1): two FP32 multiply-adds, each rounded once to nearest,
-// in one paired instruction (bit for bit two __fmaf_rn)
-__device__ __forceinline__ void fma2Rn(float &c0, float &c1, float a0, float a1, float x) {
-  asm("{\n\t.reg .b64 ra, rb, rc;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %4};\n\tmov.b64 rc, {%0, %1};\n\t"
-      "fma.rn.f32x2 rc, ra, rb, rc;\n\tmov.b64 {%0, %1}, rc;\n\t}"
-      : "+f"(c0), "+f"(c1)
-      : "f"(a0), "f"(a1), "f"(x));
-}
-
 constexpr int kTileRows = 128;     // rows per tile (4 per thread)
 constexpr int kTileK = 32;         // directions per shared-memory chunk
 constexpr int kTilePitch = kTileK + 4;  // row pitch: the 8 lanes of a quarter-warp hit distinct banks

@@ -14,6 +14,7 @@
 // are contiguous.
 #include <algorithm>
 
+#include "fp32_pair.h"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -374,10 +375,8 @@ __global__ void __launch_bounds__(kZoneThreads, 1)
           for (int k = 0; k < MM; ++k) {
             const float p = v[R + k];
             const float4 s4 = sl[legendreOf(k)];
-            acc[0][k] += s4.x * p;
-            acc[1][k] += s4.y * p;
-            acc[2][k] += s4.z * p;
-            acc[3][k] += s4.w * p;
+            fma2Rn(acc[0][k], acc[1][k], s4.x, s4.y, p);  // acc += s * p, each rounded once
+            fma2Rn(acc[2][k], acc[3][k], s4.z, s4.w, p);
           }
         }
       }
