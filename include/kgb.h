@@ -363,7 +363,9 @@ int kgb_batch_context(kgb_batch *b, int32_t index, kgb_ctx **ctx);
  * per-step launches, the streamed FP32 sweep where it applies -- on parallel
  * graph branches, with the batch's tiles; 0: one persistent launch over all
  * problems; -1: by precision, the default; psi is bit for bit the same
- * either way), "barrier_wait_ns" (how long a grid-barrier wait of the persistent
+ * either way), "branches" (1 to 8, default 8: the streams the problems' own
+ * kernels are spread over, round-robin -- parallel branches of the graph;
+ * the results do not depend on it), "barrier_wait_ns" (how long a grid-barrier wait of the persistent
  * sweep waits before it gives up; default 2e9; a solve whose wait gave up
  * returns KGB_ERR_TIMEOUT with its results undefined, and the batch stays
  * usable).  Read-only:

@@ -53,8 +53,10 @@ struct kgb_batch {
   // set by a solve's reset and by every batched sweep, which records them; cleared by a new plan
   bool rec_ok = false;
 
-  // streams the per-problem moment kernels fork onto (graph branches when captured)
-  static constexpr int kForks = 4;
+  // streams the per-problem kernels fork onto (graph branches when captured); a phase
+  // uses the first `branches` of them
+  static constexpr int kForks = 8;
+  int branches = 8;
   cudaStream_t aux[kForks] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[kForks] = {};
 
@@ -362,20 +364,21 @@ int ensurePlan(kgb_batch *b) {
 }
 
 // Each problem's own kernels for one phase (the tensor-core digit products in
-// FP64), spread over kForks streams forked from and joined back to the batch
+// FP64), spread over the batch's branches (streams forked from and joined back to the batch
 // stream -- parallel branches of the captured graph.
 // pop: the batch's population slots of this iteration (Sweep: each problem's count
 // of the new psi goes to pop[i]; FP64 problems record psi's row exponents).
 int forkPhase(kgb_batch *b, InstanceOp op, double *pop = nullptr) {
   BCK(cudaEventRecord(b->fork_ev, b->stream));
-  for (int k = 0; k < kgb_batch::kForks; ++k) BCK(cudaStreamWaitEvent(b->aux[k], b->fork_ev, 0));
+  const int nb = b->branches;
+  for (int k = 0; k < nb; ++k) BCK(cudaStreamWaitEvent(b->aux[k], b->fork_ev, 0));
   for (size_t i = 0; i < b->inst.size(); ++i) {
     const bool sweep = op == InstanceOp::Sweep;
     const int *rx = (op == InstanceOp::LTimes && b->rec_ok) || sweep ? b->views[i].psi_exp : nullptr;
-    const int rc = instance_op(b->inst[i], op, b->q, b->aux[i % kgb_batch::kForks], rx, sweep ? pop + i : nullptr);
+    const int rc = instance_op(b->inst[i], op, b->q, b->aux[i % nb], rx, sweep ? pop + i : nullptr);
     if (rc) return fail(b, rc, "problem " + std::to_string(i) + ": " + kgb_last_error(b->inst[i]));
   }
-  for (int k = 0; k < kgb_batch::kForks; ++k) {
+  for (int k = 0; k < nb; ++k) {
     BCK(cudaEventRecord(b->join_ev[k], b->aux[k]));
     BCK(cudaStreamWaitEvent(b->stream, b->join_ev[k], 0));
   }
@@ -643,6 +646,9 @@ int kgb_batch_set_option(kgb_batch *b, const char *key, int64_t value) {
     b->own_mode = value < 0 ? -1 : (value != 0 ? 1 : 0);
   } else if (k == "per_problem_sweeps") {
     b->sweep_mode = value < 0 ? -1 : (value != 0 ? 1 : 0);
+  } else if (k == "branches") {
+    if (value < 1 || value > kgb_batch::kForks) return fail(b, KGB_ERR_ARG, "branches must be in [1, 8]");
+    b->branches = (int)value;
   } else {
     return fail(b, KGB_ERR_ARG, "unknown option '" + k + "'");
   }
@@ -661,6 +667,7 @@ int kgb_batch_get_option(kgb_batch *b, const char *key, int64_t *value) {
   else if (k == "graph") *value = b->use_graph;
   else if (k == "per_problem_kernels") *value = perProblem(b);
   else if (k == "per_problem_sweeps") *value = ownSweeps(b);
+  else if (k == "branches") *value = b->branches;
   else if (k == "graph_active") *value = b->graph_active;
   else if (k == "sweep_grid") *value = b->sweep_grid;
   else if (k == "sweep_steps") *value = b->nsteps;

@@ -92,6 +92,31 @@ def test_batch_sweep_modes_agree(kgb, prec):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_batch_branches_agree(kgb, prec):
+    """The branch count only spreads the problems' kernels over more or fewer streams: psi and the
+    particle counts are the same bit for bit for 1, 4 and 8 branches; out-of-range counts are
+    refused."""
+    precision = kgb.FP64 if prec == "fp64" else kgb.MIXED
+    inputs = uneven_inputs(6, seed=23, zones=(5, 10), groups=(8, 16), directions=(96, 128), legendre=(2, 4),
+                           precision=precision)
+    b = make_batch(kgb, inputs, precision)
+    runs = []
+    for nb in (4, 1, 8):
+        b.set_option("branches", nb)
+        assert b.get_option("branches") == nb
+        parts = b.solve(3)
+        runs.append((parts, [b.context(i).download("psi") for i in range(len(b))]))
+    for parts, psis in runs[1:]:
+        np.testing.assert_array_equal(parts, runs[0][0])
+        for got, want in zip(psis, runs[0][1]):
+            np.testing.assert_array_equal(got, want)
+    for bad in (0, 9):
+        with pytest.raises(Exception):
+            b.set_option("branches", bad)
+
+
+@pytest.mark.gpu
 def test_batch_matches_oracle(kgb, oracle):
     inputs = small_set(kgb, n=4, seed=3)
     b = make_batch(kgb, inputs, kgb.FP64)
