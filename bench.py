@@ -557,6 +557,7 @@ def batch_report(local, problems=BATCH_PROBLEMS, niter=10):
                      "graph_active": b.get_option("graph_active"), "kernels_per_iteration": kernels,
                      "per_problem_kernels": b.get_option("per_problem_kernels"),
                      "per_problem_sweeps": b.get_option("per_problem_sweeps"),
+                     "branches": b.get_option("branches"),
                      "autotuned": tune, "phase_ms": phases,
                      "one_by_one": {"value": U / t_seq, "ms_per_iteration": t_seq * 1e3,
                                     "how": "each problem's own context, default options, solved in turn"},
