@@ -153,12 +153,7 @@ __global__ void __launch_bounds__(kLsThreads, 4) ltimes_stream_kernel(const __gr
     const unsigned char *buf = al + (size_t)s * kLsStageBytes;
     const float *lk = ls + (size_t)(q % nk) * kLsK * 32 + 8 * mg;
     // the chunk's 32 directions into the thread's MB moments of its four rows
-#pragma unroll 2
-    for (int k4 = 0; k4 < kLsK / 4; ++k4) {
-      float4 a[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-        a[i] = *reinterpret_cast<const float4 *>(buf + (rbase + 8 * i) * 128 + ((k4 ^ swz) << 4));
+    auto body = [&](int k4, const float4 (&a)[4]) {
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk) {
         float l[8];
@@ -172,6 +167,22 @@ __global__ void __launch_bounds__(kLsThreads, 4) ltimes_stream_kernel(const __gr
           if (MB & 1) acc[i][MB - 1] = __fmaf_rn(l[MB - 1], x, acc[i][MB - 1]);
         }
       }
+    };
+    auto ldA = [&](int k4, float4 (&a)[4]) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        a[i] = *reinterpret_cast<const float4 *>(buf + (rbase + 8 * i) * 128 + ((k4 ^ swz) << 4));
+    };
+    // the next direction quad's psi is read before this one's multiply-adds (2.74 -> 2.64 ms
+    // at 64^3 zones x 64 groups x 128 directions, P4; unrolling alone: 2.67)
+    float4 a[4], b[4];
+    ldA(0, a);
+#pragma unroll
+    for (int k4 = 0; k4 < kLsK / 4; k4 += 2) {
+      ldA(k4 + 1, b);
+      body(k4, a);
+      if (k4 + 2 < kLsK / 4) ldA(k4 + 2, a);
+      body(k4 + 1, b);
     }
     __syncwarp();
     if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sAddr(&empty[s])) : "memory");
