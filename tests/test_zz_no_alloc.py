@@ -5,8 +5,9 @@ memory when they need the particle count (frameworks that own all device
 memory through their own pool, latency-bound loops).  It must give the same FP64
 population as the context-based kgb_population, within the 1e-12 relative
 tolerance of the other FP64 parity tests, on two calls in a row (the second
-call reuses the static scratch the first one left behind).  This file sorts
-last so that a run stopping at the first failure has run every other test.
+call reuses the static scratch the first one left behind), and from a CUDA
+graph that captured the call, on every replay.  This file sorts last so that
+a run stopping at the first failure has run every other test.
 """
 import ctypes
 
@@ -49,6 +50,21 @@ def test_population_noalloc_matches_population():
     for got in results:
         assert got == pytest.approx(want, rel=1e-12)
     assert results[0] == results[1]  # fixed summation order: bitwise repeatable
+
+    # captured into a CUDA graph after the calls above (which looked up the scratch address):
+    # every replay runs both launches again and rewrites the static scratch, bit for bit
+    t_cap = torch.full((1,), -1.0, dtype=torch.float64, device=dev)
+    side = torch.cuda.Stream(dev)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        rc = lib.kgb_population_noalloc(t_psi.data_ptr(), t_w.data_ptr(), t_vol.data_ptr(), Z, G, D,
+                                        t_cap.data_ptr(), side.cuda_stream, err, len(err))
+    assert rc == 0, err.value.decode()
+    for _ in range(2):
+        t_cap.fill_(-1.0)
+        graph.replay()
+        torch.cuda.synchronize(dev)
+        assert float(t_cap.item()) == results[0]
 
     # sizes beyond the static scratch are rejected before any launch
     rc = lib.kgb_population_noalloc(t_psi.data_ptr(), t_w.data_ptr(), t_vol.data_ptr(), 1 << 40, G, D,
