@@ -104,6 +104,7 @@ int prepareAdjointT(kgb_ctx *ctx) {
                                      &ctx->tc_lp_exp_adj, &ctx->tc_lp_nhalf_adj)))
     return rc;
   if ((rc = planTf32From(ctx, ctx->ellp_h, ctx->ell_h, &ctx->tf32_lt_img_adj, &ctx->tf32_lp_img_adj))) return rc;
+  if ((rc = planLtSym(ctx, ctx->ellp_h, &ctx->lt_sym_adj))) return rc;
   ctx->adj_stale = false;
   return KGB_OK;
 }
@@ -138,6 +139,7 @@ struct AdjointView {
     std::swap(c->tc_lt_kpad, c->tc_lt_kpad_adj);
     std::swap(c->tc_lp_nhalf, c->tc_lp_nhalf_adj);
     std::swap(c->tf32_lt_img, c->tf32_lt_img_adj);
+    std::swap(c->lt_sym, c->lt_sym_adj);
     std::swap(c->tf32_lp_img, c->tf32_lp_img_adj);
     std::swap(c->tc_sc_img, c->tc_sc_img_adj);
     std::swap(c->tc_sc_exp, c->tc_sc_exp_adj);

@@ -170,13 +170,15 @@ void freeAll(kgb_ctx *c) {
                   c->gp_lo_adj, c->gp_hi_adj, c->colsum_d, c->e0_d, c->det_d, c->norm_d, c->resp_part, c->resp_d,
                   c->tc_lt_img_adj, c->tc_lp_img_adj, c->tc_lt_exp_adj, c->tc_lp_exp_adj, c->tc_sc_img,
                   c->tc_sc_img_adj, c->tc_sc_exp, c->tc_sc_exp_adj, c->pure_z,  // mixed_z lies inside pure_z
-                  c->psi_exp, c->phi_exp, c->tf32_lt_img, c->tf32_lp_img, c->tf32_lt_img_adj, c->tf32_lp_img_adj};
+                  c->psi_exp, c->phi_exp, c->tf32_lt_img, c->tf32_lp_img, c->tf32_lt_img_adj, c->tf32_lp_img_adj,
+                  c->lt_sym, c->lt_sym_adj};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   c->psi = c->rhs = c->phi = c->phi_out = c->sigt = nullptr;
   c->psi_exp = c->phi_exp = nullptr;
   c->psi_exp_valid = false;
   c->tf32_lt_img = c->tf32_lp_img = c->tf32_lt_img_adj = c->tf32_lp_img_adj = nullptr;
+  c->lt_sym = c->lt_sym_adj = nullptr;
   c->plane[0] = c->plane[1] = c->plane[2] = nullptr;
   c->ell = c->ellp = c->sigsT = c->cx = c->cy = c->cz = nullptr;
   c->w_d = c->vol_d = nullptr;
@@ -443,6 +445,24 @@ int planTf32From(kgb_ctx *ctx, const std::vector<double> &lt_src, const std::vec
   return KGB_OK;
 }
 
+int planLtSym(kgb_ctx *ctx, const std::vector<double> &lt_src, int **table) {
+  if (*table) cudaFree(*table);
+  *table = nullptr;
+  std::vector<int> t;
+  if (ctx->prec != KGB_MIXED || !ltimes_sym_table(lt_src.data(), ctx->D, ctx->M, t)) return KGB_OK;
+  int rc;
+  if ((rc = dmalloc(ctx, table, t.size()))) return rc;
+  if (cudaMemcpyAsync(*table, t.data(), t.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+    return fail(ctx, KGB_ERR_CUDA, "octant-pair table upload failed");
+  return KGB_OK;
+}
+
+bool ltSymActive(const kgb_ctx *ctx) {
+  return ctx->prec == KGB_MIXED && ctx->allow_lt_stream && ctx->allow_lt_sym && ctx->lt_sym != nullptr &&
+         ltimes_stream_applies(ctx->D, ctx->M);
+}
+
 bool tf32LtActive(const kgb_ctx *ctx) {
   return ctx->prec == KGB_MIXED && ctx->allow_tf32 && ctx->allow_tf32_lt && ctx->use_tf32_lt &&
          ctx->tf32_lt_img != nullptr;
@@ -629,6 +649,7 @@ int prepareT(kgb_ctx *ctx) {
     if ((rc = uploadVec<T>(ctx, ctx->ellp, ctx->ellp_h))) return rc;
     if ((rc = planTensorMoments<T>(ctx))) return rc;
     if ((rc = planTf32From(ctx, ctx->ell_h, ctx->ellp_h, &ctx->tf32_lt_img, &ctx->tf32_lp_img))) return rc;
+    if ((rc = planLtSym(ctx, ctx->ell_h, &ctx->lt_sym))) return rc;
     ctx->dirty_ell = false;
     ++ctx->gen;
     ctx->adj_stale = true;

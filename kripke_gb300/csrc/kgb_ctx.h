@@ -121,6 +121,11 @@ struct kgb_ctx {
   // mixed LTimes on the TMA-fed SIMT kernel (ltimes_stream.cu), lt_stream_ns stages
   bool allow_lt_stream = true;
   int lt_stream_ns = 2;
+  // its octant-pair form (ltimes_sym_table): the device table of the L in use (forward: ell;
+  // swapped with lt_sym_adj, ell_plus's, while the adjoint is installed), null when L has no
+  // such structure
+  bool allow_lt_sym = true;
+  int *lt_sym = nullptr, *lt_sym_adj = nullptr;
 
   // device state (element type T = double or float by precision)
   void *psi = nullptr, *rhs = nullptr, *phi = nullptr, *phi_out = nullptr, *sigt = nullptr;
@@ -366,6 +371,8 @@ int need(kgb_ctx *ctx, std::initializer_list<const char *> names);
 int buildReciprocals(kgb_ctx *ctx);
 int planTf32From(kgb_ctx *ctx, const std::vector<double> &lt_src, const std::vector<double> &lp_src, float **lt_img,
                  float **lp_img);
+int planLtSym(kgb_ctx *ctx, const std::vector<double> &lt_src, int **table);
+bool ltSymActive(const kgb_ctx *ctx);
 bool tf32LtActive(const kgb_ctx *ctx);
 bool tf32LpActive(const kgb_ctx *ctx);
 void updatePopScale(kgb_ctx *ctx);

@@ -143,11 +143,19 @@ bool launch_ltimes_record(const float *psi, float *phi, const float *ell_dm, int
                           int *outexp, int rexp_w, int G, cudaStream_t s);
 // FP32 LTimes phi = L psi (not accumulated) on the TMA-fed SIMT kernel
 // (ltimes_stream.cu): directions a multiple of 32, 13 <= M <= 32, ns = 2..4
-// shared-memory stages; bit for bit the register-tiled kernel.  Nonzero return:
-// not launched.
+// shared-memory stages; bit for bit the register-tiled kernel.  sym (device, or
+// null): the octant-pair table of L (ltimes_sym_table), which halves the
+// multiply-adds and sums in another order.  Nonzero return: not launched.
 bool ltimes_stream_applies(int D, int M);
 int launch_ltimes_stream(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M, int ns,
-                         int *err, int nsm, cudaStream_t s);
+                         const int *sym, int *err, int nsm, cudaStream_t s);
+// The octant-pair table of a [D][M] L for launch_ltimes_stream, or false when L
+// has no such structure: per 32-direction chunk the partner column (16..31) of
+// each of its first 16 directions, whose L column is the direction's times a
+// sign that depends on the moment only; then the moment of each of 32 slots
+// (slots 0-15 the moments of sign +1, 16-31 those of sign -1, ascending; -1
+// empty).  D/2 + 32 entries.
+bool ltimes_sym_table(const double *L, int D, int M, std::vector<int> &table);
 
 struct ScatterArgsBase {
   int64_t Z;                  // zones (rows = Z * destination groups); with zlist, the list's length

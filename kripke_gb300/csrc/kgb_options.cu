@@ -78,6 +78,10 @@ int kgb_set_option(kgb_ctx *ctx, const char *key, int64_t value) {
     ctx->allow_lt_stream = value != 0;
     return KGB_OK;
   }
+  if (!std::strcmp(key, "ltimes_symmetric")) {
+    ctx->allow_lt_sym = value != 0;
+    return KGB_OK;
+  }
   if (!std::strcmp(key, "ltimes_stream_stages")) {
     if (value < 2 || value > 4) return fail(ctx, KGB_ERR_ARG, "ltimes_stream_stages must be 2 to 4");
     ctx->lt_stream_ns = (int)value;
@@ -283,6 +287,8 @@ int kgb_get_option(kgb_ctx *ctx, const char *key, int64_t *value) {
   else if (!std::strcmp(key, "sweep_stream")) *value = ctx->allow_stream ? 1 : 0;
   else if (!std::strcmp(key, "ltimes_stream")) *value = ctx->allow_lt_stream ? 1 : 0;
   else if (!std::strcmp(key, "ltimes_stream_stages")) *value = ctx->lt_stream_ns;
+  else if (!std::strcmp(key, "ltimes_symmetric")) *value = ctx->allow_lt_sym ? 1 : 0;
+  else if (!std::strcmp(key, "ltimes_symmetric_active")) *value = ltSymActive(ctx) ? 1 : 0;
   else if (!std::strcmp(key, "sweep_stream_stages")) *value = ctx->stream_ns;
   else if (!std::strcmp(key, "sweep_stream_active")) *value = streamUsable(ctx) ? 1 : 0;
   else if (!std::strcmp(key, "sweep_streams")) *value = ctx->sweep_streams;

@@ -336,9 +336,11 @@ int doLTimes(kgb_ctx *ctx, bool acc, const int *rowexp, int *outexp) {
     return KGB_OK;
   }
   if (ctx->prec == KGB_MIXED && !acc && ctx->allow_lt_stream && ltimes_stream_applies(ctx->D, ctx->M)) {
-    // the TMA-fed SIMT kernel (bit for bit the register-tiled one)
+    // the TMA-fed SIMT kernel (bit for bit the register-tiled one), or its octant-pair form where
+    // L allows it (half the multiply-adds; option ltimes_symmetric)
     if (launch_ltimes_stream(as<float>(ctx->psi), as<float>(ctx->phi), as<float>(ctx->ell), rows, ctx->D, ctx->M,
-                             ctx->lt_stream_ns, ctx->err_d, ctx->nsm, ctx->stream))
+                             ctx->lt_stream_ns, ltSymActive(ctx) ? ctx->lt_sym : nullptr, ctx->err_d, ctx->nsm,
+                             ctx->stream))
       return fail(ctx, KGB_ERR_CUDA, "streamed LTimes launch failed");
     CKN(1);
     return KGB_OK;

@@ -28,6 +28,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
+#include <cmath>
 #include <mutex>
 
 #include "fp32_pair.h"
@@ -73,11 +75,16 @@ __device__ __forceinline__ bool waitPar(uint64_t *bar, uint32_t parity, volatile
   return done != 0;
 }
 
-template <int MB>
+// SYM: the octant-pair form (MB = 8).  sym holds, per 32-direction chunk, the partner
+// column (16..31) of each of the chunk's first 16 directions, then the moment of each of
+// the 32 slots (-1: empty); lane groups 0 and 1 hold the moments whose L columns repeat
+// with sign +1 on the partners, groups 2 and 3 those with sign -1.
+template <int MB, bool SYM>
 __global__ void __launch_bounds__(kLsThreads, 4) ltimes_stream_kernel(const __grid_constant__ CUtensorMap pmap,
                                                                    float *__restrict__ phi,
                                                                    const float *__restrict__ ell_dm, int64_t rows,
-                                                                   int D, int M, int ns, int *err) {
+                                                                   int D, int M, int ns, const int *__restrict__ sym,
+                                                                   int *err) {
   extern __shared__ __align__(1024) unsigned char sraw[];
   __shared__ __align__(8) uint64_t full[kLsMaxStages], empty[kLsMaxStages];
   __shared__ int abort_flag;
@@ -85,10 +92,20 @@ __global__ void __launch_bounds__(kLsThreads, 4) ltimes_stream_kernel(const __gr
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const uint32_t base = sAddr(sraw);
   unsigned char *const al = sraw + (((base + 1023u) & ~1023u) - base);  // stages: 1024-byte aligned (swizzle)
-  float *const ls = reinterpret_cast<float *>(al + (size_t)ns * kLsStageBytes);  // [D][32]
-  for (int i = tid; i < D * 32; i += blockDim.x) {
-    const int d = i >> 5, c = i & 31, g = c >> 3, j = c & 7, m = MB * g + j;
-    ls[i] = (j < MB && m < M) ? ell_dm[(int64_t)d * M + m] : 0.f;
+  float *const ls = reinterpret_cast<float *>(al + (size_t)ns * kLsStageBytes);  // [D][32] (SYM: [D/2][32])
+  int *const pcol = reinterpret_cast<int *>(ls + (size_t)(SYM ? D / 2 : D) * 32);  // SYM: [D/32][16], slots [32]
+  int *const slotm = pcol + (SYM ? D / 2 : 0);
+  if constexpr (SYM) {
+    for (int i = tid; i < D / 2 + 32; i += blockDim.x) pcol[i] = sym[i];
+    for (int i = tid; i < D / 2 * 32; i += blockDim.x) {
+      const int c = i >> 9, b = (i >> 5) & 15, m = sym[D / 2 + (i & 31)];
+      ls[i] = m >= 0 ? ell_dm[(int64_t)(32 * c + b) * M + m] : 0.f;
+    }
+  } else {
+    for (int i = tid; i < D * 32; i += blockDim.x) {
+      const int d = i >> 5, c = i & 31, g = c >> 3, j = c & 7, m = MB * g + j;
+      ls[i] = (j < MB && m < M) ? ell_dm[(int64_t)d * M + m] : 0.f;
+    }
   }
   if (tid == 0) {
     for (int s = 0; s < ns; ++s) {
@@ -151,38 +168,76 @@ __global__ void __launch_bounds__(kLsThreads, 4) ltimes_stream_kernel(const __gr
     const bool ok = __all_sync(0xffffffffu, waitPar(&full[s], (uint32_t)(q / ns) & 1u, abort));
     if (!ok) break;
     const unsigned char *buf = al + (size_t)s * kLsStageBytes;
-    const float *lk = ls + (size_t)(q % nk) * kLsK * 32 + 8 * mg;
-    // the chunk's 32 directions into the thread's MB moments of its four rows
-    auto body = [&](int k4, const float4 (&a)[4]) {
-#pragma unroll
-      for (int kk = 0; kk < 4; ++kk) {
-        float l[8];
-        *reinterpret_cast<float4 *>(l) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32);
-        if (MB > 4) *reinterpret_cast<float4 *>(l + 4) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32 + 4);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const float x = kk == 0 ? a[i].x : kk == 1 ? a[i].y : kk == 2 ? a[i].z : a[i].w;
-#pragma unroll
-          for (int m = 0; m + 1 < MB; m += 2) fma2Rn(acc[i][m], acc[i][m + 1], l[m], l[m + 1], x);
-          if (MB & 1) acc[i][MB - 1] = __fmaf_rn(l[MB - 1], x, acc[i][MB - 1]);
-        }
-      }
-    };
     auto ldA = [&](int k4, float4 (&a)[4]) {
 #pragma unroll
       for (int i = 0; i < 4; ++i)
         a[i] = *reinterpret_cast<const float4 *>(buf + (rbase + 8 * i) * 128 + ((k4 ^ swz) << 4));
     };
-    // the next direction quad's psi is read before this one's multiply-adds (2.74 -> 2.64 ms
-    // at 64^3 zones x 64 groups x 128 directions, P4; unrolling alone: 2.67)
-    float4 a[4], b[4];
-    ldA(0, a);
+    if constexpr (SYM) {
+      // the chunk's two mirrored octants: for each of the first octant's 16 directions b and
+      // its partner b', x = psi(b) + psi(b') (groups 0, 1) or psi(b) - psi(b') (groups 2, 3),
+      // one rounding, then the slot moments' multiply-adds with L(m, b)
+      const float sg = (mg >> 1) ? -1.f : 1.f;
+      const int c = (int)(q % nk);
+      const float *lk = ls + (size_t)c * 16 * 32 + 8 * mg;
+      const int *pc = pcol + c * 16;
+      auto body = [&](int b4, const float4 (&a)[4]) {
 #pragma unroll
-    for (int k4 = 0; k4 < kLsK / 4; k4 += 2) {
-      ldA(k4 + 1, b);
-      body(k4, a);
-      if (k4 + 2 < kLsK / 4) ldA(k4 + 2, a);
-      body(k4 + 1, b);
+        for (int bb = 0; bb < 4; ++bb) {
+          const int b = 4 * b4 + bb;
+          float l[8];
+          *reinterpret_cast<float4 *>(l) = *reinterpret_cast<const float4 *>(lk + b * 32);
+          *reinterpret_cast<float4 *>(l + 4) = *reinterpret_cast<const float4 *>(lk + b * 32 + 4);
+          const int col = pc[b];
+          const int voff = (((col >> 2) ^ swz) << 4) + ((col & 3) << 2);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float u = bb == 0 ? a[i].x : bb == 1 ? a[i].y : bb == 2 ? a[i].z : a[i].w;
+            const float v = *reinterpret_cast<const float *>(buf + (rbase + 8 * i) * 128 + voff);
+            const float x = __fmaf_rn(sg, v, u);
+#pragma unroll
+            for (int m = 0; m < MB; m += 2) fma2Rn(acc[i][m], acc[i][m + 1], l[m], l[m + 1], x);
+          }
+        }
+      };
+      float4 a[4], b[4];
+      ldA(0, a);
+#pragma unroll
+      for (int b4 = 0; b4 < 4; b4 += 2) {
+        ldA(b4 + 1, b);
+        body(b4, a);
+        if (b4 + 2 < 4) ldA(b4 + 2, a);
+        body(b4 + 1, b);
+      }
+    } else {
+      const float *lk = ls + (size_t)(q % nk) * kLsK * 32 + 8 * mg;
+      // the chunk's 32 directions into the thread's MB moments of its four rows
+      auto body = [&](int k4, const float4 (&a)[4]) {
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          float l[8];
+          *reinterpret_cast<float4 *>(l) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32);
+          if (MB > 4) *reinterpret_cast<float4 *>(l + 4) = *reinterpret_cast<const float4 *>(lk + (4 * k4 + kk) * 32 + 4);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float x = kk == 0 ? a[i].x : kk == 1 ? a[i].y : kk == 2 ? a[i].z : a[i].w;
+#pragma unroll
+            for (int m = 0; m + 1 < MB; m += 2) fma2Rn(acc[i][m], acc[i][m + 1], l[m], l[m + 1], x);
+            if (MB & 1) acc[i][MB - 1] = __fmaf_rn(l[MB - 1], x, acc[i][MB - 1]);
+          }
+        }
+      };
+      // the next direction quad's psi is read before this one's multiply-adds (2.74 -> 2.64 ms
+      // at 64^3 zones x 64 groups x 128 directions, P4; unrolling alone: 2.67)
+      float4 a[4], b[4];
+      ldA(0, a);
+#pragma unroll
+      for (int k4 = 0; k4 < kLsK / 4; k4 += 2) {
+        ldA(k4 + 1, b);
+        body(k4, a);
+        if (k4 + 2 < kLsK / 4) ldA(k4 + 2, a);
+        body(k4 + 1, b);
+      }
     }
     __syncwarp();
     if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sAddr(&empty[s])) : "memory");
@@ -192,10 +247,19 @@ __global__ void __launch_bounds__(kLsThreads, 4) ltimes_stream_kernel(const __gr
       for (int i = 0; i < 4; ++i) {
         const int64_t row = tile * kLsRows + rbase + 8 * i;
         if (row >= rows) continue;
-        float *o = phi + row * M + MB * mg;
+        if constexpr (SYM) {
+          float *o = phi + row * M;
 #pragma unroll
-        for (int m = 0; m < MB; ++m)
-          if (MB * mg + m < M) o[m] = acc[i][m];
+          for (int m = 0; m < MB; ++m) {
+            const int mo = slotm[MB * mg + m];
+            if (mo >= 0) o[mo] = acc[i][m];
+          }
+        } else {
+          float *o = phi + row * M + MB * mg;
+#pragma unroll
+          for (int m = 0; m < MB; ++m)
+            if (MB * mg + m < M) o[m] = acc[i][m];
+        }
       }
     }
   }
@@ -216,20 +280,22 @@ PFN_cuTensorMapEncodeTiled_v12000 encoder() {
   return fn;
 }
 
-template <int MB>
-int launchAs(const CUtensorMap &m, float *phi, const float *ell_dm, int64_t rows, int D, int M, int ns, int *err,
-             int nsm, cudaStream_t s) {
-  const size_t smem = (size_t)ns * kLsStageBytes + (size_t)D * 32 * 4 + 1024;
-  if (cudaFuncSetAttribute(ltimes_stream_kernel<MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+template <int MB, bool SYM>
+int launchAs(const CUtensorMap &m, float *phi, const float *ell_dm, int64_t rows, int D, int M, int ns,
+             const int *sym, int *err, int nsm, cudaStream_t s) {
+  // stages, the L table ([D][32], SYM: [D/2][32] and the partner / slot table) and the alignment slack
+  const size_t smem = (size_t)ns * kLsStageBytes + (SYM ? (size_t)D / 2 * 32 * 4 + (size_t)(D / 2 + 32) * 4
+                                                         : (size_t)D * 32 * 4) + 1024;
+  if (cudaFuncSetAttribute(ltimes_stream_kernel<MB, SYM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return 1;
   int per = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ltimes_stream_kernel<MB>, kLsThreads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ltimes_stream_kernel<MB, SYM>, kLsThreads, smem);
   if (per < 1) return 1;
   const int64_t ntiles = (rows + kLsRows - 1) / kLsRows;
   const int64_t cap = (int64_t)nsm * per;
   const int grid = (int)(ntiles < cap ? (ntiles > 0 ? ntiles : 1) : cap);
-  ltimes_stream_kernel<MB><<<grid, kLsThreads, smem, s>>>(m, phi, ell_dm, rows, D, M, ns, err);
+  ltimes_stream_kernel<MB, SYM><<<grid, kLsThreads, smem, s>>>(m, phi, ell_dm, rows, D, M, ns, sym, err);
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 
@@ -239,8 +305,59 @@ bool ltimes_stream_applies(int D, int M) {
   return D % kLsK == 0 && D <= 1024 && M >= 13 && M <= 32;
 }
 
+// Kernel::LTimes sums L(m, d) psi(d) over all directions (Kernel/LTimes.cpp:54-65).  Kripke's
+// quadrature sets hold the octants one after another, the x sign running fastest, and a real
+// spherical harmonic is even or odd under x -> -x: with 16 directions per octant the two
+// octants of a 32-direction chunk are mirror images (in another order), and the partner's L
+// column is the direction's times a sign that depends on the moment only.  Found here from L
+// alone (|L| equal to 1e-12 of the column's largest, one sign per moment over every chunk).
+bool ltimes_sym_table(const double *L, int D, int M, std::vector<int> &table) {
+  table.clear();
+  if (!ltimes_stream_applies(D, M)) return false;
+  const int nk = D / kLsK;
+  std::vector<int> sign(M, 0), part((size_t)nk * 16, -1);
+  for (int c = 0; c < nk; ++c) {
+    bool used[16] = {};
+    for (int b = 0; b < 16; ++b) {
+      const double *la = L + (size_t)(kLsK * c + b) * M;
+      double top = 0.0;
+      for (int m = 0; m < M; ++m) top = std::max(top, std::fabs(la[m]));
+      const double tol = 1e-12 * top;
+      for (int b2 = 0; b2 < 16 && part[(size_t)c * 16 + b] < 0; ++b2) {
+        if (used[b2]) continue;
+        const double *lb = L + (size_t)(kLsK * c + 16 + b2) * M;
+        bool ok = true;
+        std::vector<int> sg(sign);
+        for (int m = 0; m < M && ok; ++m) {
+          if (std::fabs(std::fabs(lb[m]) - std::fabs(la[m])) > tol) ok = false;
+          else if (std::fabs(la[m]) > tol) {
+            const int t = (la[m] < 0) == (lb[m] < 0) ? 1 : -1;
+            if (sg[m] == 0) sg[m] = t;
+            else if (sg[m] != t) ok = false;
+          }
+        }
+        if (!ok) continue;
+        used[b2] = true;
+        part[(size_t)c * 16 + b] = 16 + b2;
+        sign = sg;
+      }
+      if (part[(size_t)c * 16 + b] < 0) return false;
+    }
+  }
+  std::vector<int> even, odd;
+  for (int m = 0; m < M; ++m) (sign[m] < 0 ? odd : even).push_back(m);
+  if (even.size() > 16 || odd.size() > 16) return false;
+  table = part;
+  for (int k = 0; k < 32; ++k) {
+    const std::vector<int> &v = k < 16 ? even : odd;
+    const size_t i = (size_t)(k & 15);
+    table.push_back(i < v.size() ? v[i] : -1);
+  }
+  return true;
+}
+
 int launch_ltimes_stream(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M, int ns,
-                         int *err, int nsm, cudaStream_t s) {
+                         const int *sym, int *err, int nsm, cudaStream_t s) {
   if (!ltimes_stream_applies(D, M) || ns < 2 || ns > kLsMaxStages || ((uintptr_t)psi & 15u) != 0) return 1;
   PFN_cuTensorMapEncodeTiled_v12000 fn = encoder();
   if (!fn) return 1;
@@ -253,12 +370,13 @@ int launch_ltimes_stream(const float *psi, float *phi, const float *ell_dm, int6
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return 1;
+  if (sym) return launchAs<8, true>(m, phi, ell_dm, rows, D, M, ns, sym, err, nsm, s);
   const int mb = (M + 3) / 4;
-  if (mb == 4) return launchAs<4>(m, phi, ell_dm, rows, D, M, ns, err, nsm, s);
-  if (mb == 5) return launchAs<5>(m, phi, ell_dm, rows, D, M, ns, err, nsm, s);
-  if (mb == 6) return launchAs<6>(m, phi, ell_dm, rows, D, M, ns, err, nsm, s);
-  if (mb == 7) return launchAs<7>(m, phi, ell_dm, rows, D, M, ns, err, nsm, s);
-  return launchAs<8>(m, phi, ell_dm, rows, D, M, ns, err, nsm, s);
+  if (mb == 4) return launchAs<4, false>(m, phi, ell_dm, rows, D, M, ns, nullptr, err, nsm, s);
+  if (mb == 5) return launchAs<5, false>(m, phi, ell_dm, rows, D, M, ns, nullptr, err, nsm, s);
+  if (mb == 6) return launchAs<6, false>(m, phi, ell_dm, rows, D, M, ns, nullptr, err, nsm, s);
+  if (mb == 7) return launchAs<7, false>(m, phi, ell_dm, rows, D, M, ns, nullptr, err, nsm, s);
+  return launchAs<8, false>(m, phi, ell_dm, rows, D, M, ns, nullptr, err, nsm, s);
 }
 
 }  // namespace kgb

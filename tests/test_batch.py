@@ -34,6 +34,7 @@ def single_run(kgb, b, i, niter):
         c.set_option("moments_tf32", 0)
         c.set_option("moments_tensor", 0)
         c.set_option("scattering_tensor", 0)
+        c.set_option("ltimes_symmetric", 0)  # the batched SIMT LTimes sums in ascending direction order
     return np.array(c.solve(niter)), c.download("psi")
 
 

@@ -4,6 +4,12 @@ Both form every output as the same FMA chain over ascending directions (Kernel/L
 restated with paired FP32 multiply-adds), so phi must agree bit for bit; the oracle bounds both.
 Shapes: 96, 128 and 192 directions, Legendre orders 3 and 4 (16 and 25 moments), row counts that
 leave a partial last 128-row tile, and 2 to 4 shared-memory stages.
+
+Its octant-pair form (option ltimes_symmetric, on by default where L allows it) pairs each
+direction of a 32-direction chunk's first 16 with its mirror image among the other 16 and sums
+L(m, b) (psi(b) +- psi(b')): half the multiply-adds, another summation order, so it is held to
+FP32 rounding against the bit-exact kernel and to the oracle; where L has no such pairs (96 and
+192 directions) it must not be chosen.
 """
 import numpy as np
 import pytest
@@ -13,9 +19,10 @@ from tests.test_gpu_parity import check, pair
 pytestmark = pytest.mark.gpu
 
 
-def phi_after_ltimes(ctx, psi, stream, stages=2):
+def phi_after_ltimes(ctx, psi, stream, stages=2, sym=0):
     ctx.set_option("ltimes_stream", stream)
     ctx.set_option("ltimes_stream_stages", stages)
+    ctx.set_option("ltimes_symmetric", sym)
     ctx.upload("psi", psi)
     ctx.iterate(want_population=False)  # phi = L psi first (the solver's LTimes, not accumulated)
     return ctx.download("phi")
@@ -35,3 +42,28 @@ def test_streamed_ltimes_bitwise(oracle, kgb, quad, legendre, zones, groups):
     p.kconst("phi", 0.0)
     p.ltimes()
     check(want, p.get("phi"), 1e-5)
+
+
+@pytest.mark.parametrize("quad,legendre,zones,groups,active", [((8, 16), 4, (9, 7, 5), 8, 1),
+                                                               ((8, 16), 3, (6, 5, 7), 12, 1),
+                                                               ((4, 8), 4, (7, 6, 5), 16, 1),
+                                                               ((8, 12), 4, (6, 5, 7), 8, 0),
+                                                               ((8, 24), 4, (5, 5, 3), 4, 0)])
+def test_octant_pair_ltimes(oracle, kgb, quad, legendre, zones, groups, active):
+    p, ctx = pair(oracle, kgb, precision=1, zones=zones, quad=quad, legendre=legendre, groups=groups, scatter=1,
+                  geometry=1)
+    psi = np.random.default_rng(37).uniform(-1.0, 2.0, ctx.field_bytes("psi") // 8)
+    exact = phi_after_ltimes(ctx, psi, 1)
+    for stages in (2, 3):
+        got = phi_after_ltimes(ctx, psi, 1, stages, sym=1)
+        assert ctx.get_option("ltimes_symmetric_active") == active
+        if active:
+            # |d| <= 8 units of FP32 rounding of the largest output (sums of up to 192 terms of either sign)
+            assert np.max(np.abs(got - exact)) <= 8 * 2.0 ** -24 * np.max(np.abs(exact)) * np.sqrt(quad[0] * quad[1])
+        else:
+            np.testing.assert_array_equal(got, exact)
+    ctx.set_option("ltimes_symmetric", 1)
+    p.set("psi", psi)
+    p.kconst("phi", 0.0)
+    p.ltimes()
+    check(got, p.get("phi"), 1e-5)
