@@ -311,7 +311,7 @@ def mixed_report(args, local, w, fp64_ctx, fp64_ms):
     kernels = {k: ctx.get_option(k) for k in ("sweep_tile_xy", "sweep_tile_z", "moments_tf32_ltimes",
                                               "moments_tf32_lplustimes", "moments_tensor_ltimes",
                                               "moments_tensor_lplustimes", "scattering_tensor_active",
-                                              "scattering_block_active")}
+                                              "scattering_block_active", "ltimes_symmetric_active")}
     parts = ctx.solve(MIXED_PHI_ITERS)
     fp64_ctx.solve(MIXED_PHI_ITERS)
     a, b = fp64_ctx.download("phi"), ctx.download("phi")

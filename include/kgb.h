@@ -216,6 +216,12 @@ int kgb_set_stream(kgb_ctx *ctx, void *cuda_stream);
  * kernel when directions are a multiple of 32 and 13 <= moments <= 32, bit for
  * bit the register-tiled kernel; the default; 0 = off) and
  * "ltimes_stream_stages" (2 to 4, default 2);
+ * "ltimes_symmetric" (mixed form: 1 = where the 16 directions of each
+ * octant are mirrored by the next octant's with L columns equal up to a sign
+ * per moment -- Kripke's sets with 16 directions per octant -- the streamed
+ * LTimes sums L(m,b)(psi(b) +- psi(b')) over octant pairs: half the
+ * multiply-adds, summed in another order than the reference; the default;
+ * 0 = off; read-only "ltimes_symmetric_active");
  * "block_jacobi" (0 = the sweep method, default; 1 = block Jacobi, used by
  * kgb_sweep_solver and so by every solve, iterate and adjoint call);
  * "fused_sweep" (mixed form, Legendre order <= 4: 1 = the solver loop forms

@@ -36,7 +36,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall", "-I" + 
 CU_SOURCES = ["kgb_context.cu", "kgb_solver.cu", "kgb_adjoint_api.cu", "kgb_options.cu", "sweep.cu", "moments.cu", "scatter.cu", "reduce.cu", "xpose.cu", "noalloc.cu", "tc_moments.cu",
               "adjoint.cu", "batch.cu", "tf32_moments.cu", "sweep_stream.cu", "ltimes_stream.cu"]
 CPP_SOURCES = ["generate.cpp"]
-HEADERS = ["kgb_ctx.h", "kgb_internal.h", "kgb_layout.h", "exact_round.h", "sweep_common.h", "fp32_pair.h"]
+HEADERS = ["kgb_ctx.h", "kgb_internal.h", "kgb_layout.h", "exact_round.h", "sweep_common.h", "fp32_pair.h", "ltimes_sym.h"]
 
 
 def _nvcc():

@@ -28,11 +28,10 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
-#include <algorithm>
-#include <cmath>
 #include <mutex>
 
 #include "fp32_pair.h"
+#include "ltimes_sym.h"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -301,59 +300,10 @@ int launchAs(const CUtensorMap &m, float *phi, const float *ell_dm, int64_t rows
 
 }  // namespace
 
-bool ltimes_stream_applies(int D, int M) {
-  return D % kLsK == 0 && D <= 1024 && M >= 13 && M <= 32;
-}
+bool ltimes_stream_applies(int D, int M) { return ltimesStreamShape(D, M); }
 
-// Kernel::LTimes sums L(m, d) psi(d) over all directions (Kernel/LTimes.cpp:54-65).  Kripke's
-// quadrature sets hold the octants one after another, the x sign running fastest, and a real
-// spherical harmonic is even or odd under x -> -x: with 16 directions per octant the two
-// octants of a 32-direction chunk are mirror images (in another order), and the partner's L
-// column is the direction's times a sign that depends on the moment only.  Found here from L
-// alone (|L| equal to 1e-12 of the column's largest, one sign per moment over every chunk).
 bool ltimes_sym_table(const double *L, int D, int M, std::vector<int> &table) {
-  table.clear();
-  if (!ltimes_stream_applies(D, M)) return false;
-  const int nk = D / kLsK;
-  std::vector<int> sign(M, 0), part((size_t)nk * 16, -1);
-  for (int c = 0; c < nk; ++c) {
-    bool used[16] = {};
-    for (int b = 0; b < 16; ++b) {
-      const double *la = L + (size_t)(kLsK * c + b) * M;
-      double top = 0.0;
-      for (int m = 0; m < M; ++m) top = std::max(top, std::fabs(la[m]));
-      const double tol = 1e-12 * top;
-      for (int b2 = 0; b2 < 16 && part[(size_t)c * 16 + b] < 0; ++b2) {
-        if (used[b2]) continue;
-        const double *lb = L + (size_t)(kLsK * c + 16 + b2) * M;
-        bool ok = true;
-        std::vector<int> sg(sign);
-        for (int m = 0; m < M && ok; ++m) {
-          if (std::fabs(std::fabs(lb[m]) - std::fabs(la[m])) > tol) ok = false;
-          else if (std::fabs(la[m]) > tol) {
-            const int t = (la[m] < 0) == (lb[m] < 0) ? 1 : -1;
-            if (sg[m] == 0) sg[m] = t;
-            else if (sg[m] != t) ok = false;
-          }
-        }
-        if (!ok) continue;
-        used[b2] = true;
-        part[(size_t)c * 16 + b] = 16 + b2;
-        sign = sg;
-      }
-      if (part[(size_t)c * 16 + b] < 0) return false;
-    }
-  }
-  std::vector<int> even, odd;
-  for (int m = 0; m < M; ++m) (sign[m] < 0 ? odd : even).push_back(m);
-  if (even.size() > 16 || odd.size() > 16) return false;
-  table = part;
-  for (int k = 0; k < 32; ++k) {
-    const std::vector<int> &v = k < 16 ? even : odd;
-    const size_t i = (size_t)(k & 15);
-    table.push_back(i < v.size() ? v[i] : -1);
-  }
-  return true;
+  return ltimesSymTable(L, D, M, table);
 }
 
 int launch_ltimes_stream(const float *psi, float *phi, const float *ell_dm, int64_t rows, int D, int M, int ns,
