@@ -67,3 +67,26 @@ def test_octant_pair_ltimes(oracle, kgb, quad, legendre, zones, groups, active):
     p.kconst("phi", 0.0)
     p.ltimes()
     check(got, p.get("phi"), 1e-5)
+
+
+def test_octant_pair_ltimes_in_the_adjoint(kgb):
+    """The adjoint iteration runs LTimes with L+ in L's place (and L+'s own octant-pair table):
+    unrolled gradients with the pairs on and off agree to FP32 rounding, and both to FP64."""
+    kw = dict(zones=(6, 5, 4), groups=4, quad=(8, 16), legendre=4, geometry=1, scatter=1)
+    out = {}
+    for name, prec, sym in (("fp64", kgb.FP64, 0), ("pairs", kgb.MIXED, 1), ("ascending", kgb.MIXED, 0)):
+        c = kgb.Context()
+        c.generate(precision=prec, **kw)
+        c.set_option("ltimes_symmetric", sym)
+        c.set_response(np.linspace(0.0, 1.0, 6 * 5 * 4))
+        out[name] = c.gradient_unrolled(6)
+        if prec == kgb.MIXED:
+            assert c.get_option("ltimes_symmetric_active") == sym
+        c.close()
+    for name, tol in (("ascending", 2e-6), ("fp64", 1e-5)):
+        R, dt, ds, dq = out[name]
+        Rp, dtp, dsp, dqp = out["pairs"]
+        assert abs(Rp - R) <= tol * abs(R), name
+        assert abs(dqp - dq) <= tol * abs(dq), name
+        for a, b in ((dtp, dt), (dsp, ds)):
+            assert np.max(np.abs(a - b)) <= tol * np.max(np.abs(b)), name
