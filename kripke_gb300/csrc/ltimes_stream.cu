@@ -17,14 +17,21 @@
 // but an extra loop for the short last quarter).  What differs from the
 // register-tiled kernel is the operand path.  There every thread copied its
 // share of each 32-direction chunk with cp.async and the block synchronised
-// twice a chunk; here a fifth warp issues one TMA copy per chunk (a {32 directions, 128 rows}
-// box, 128-byte swizzled so a quarter-warp's 16-byte reads of eight rows fall
-// in distinct banks) into a ring of shared-memory stages, the compute warps
-// wait on the stage's mbarrier and release it by one arrival each on a second
-// mbarrier, and no block-wide barrier remains in the loop.  Rows past the end
-// read zeros (the box's fill) and are not stored.  Every wait is bounded
-// (0.2 s of globaltimer); one that gives up sets *err, the block stops issuing
-// and finishes the copies it started, and the host reports KGB_ERR_TIMEOUT.
+// twice a chunk; here a fifth warp issues one TMA copy per chunk (a {32
+// directions, 128 rows} box, 128-byte swizzled so a quarter-warp's 16-byte
+// reads of eight rows fall in distinct banks) into a ring of shared-memory
+// stages, the compute warps wait on the stage's mbarrier and release it by one
+// arrival each on a second mbarrier, and no block-wide barrier remains in the
+// loop.  Rows past the end read zeros (the box's fill) and are not stored.
+// Every wait is bounded (0.2 s of globaltimer); one that gives up sets *err,
+// the block stops issuing and finishes the copies it started, and the host
+// reports KGB_ERR_TIMEOUT.
+//
+// The octant-pair form (SYM, the table of ltimes_sym.h) sums each chunk as
+// L(m, b) (psi(b) +- psi(b')) over the chunk's first 16 directions and their
+// mirror images: half the multiply-adds, which bounded the kernel (2.64 ->
+// 2.16 ms at 64^3 x 64 groups x 128 directions, P4), in another order than
+// the reference's ascending sum, so it is held to FP32 rounding of it.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
